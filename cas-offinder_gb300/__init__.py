@@ -1,0 +1,357 @@
+"""Python binding of libcasoff.so, the GB300 Cas-OFFinder search engine.
+
+The engine itself is CUDA C++ behind the C ABI of include/cof.h; this module
+only loads that library with ctypes.  `CasOFFinder` mirrors the reference's
+engine class (Cas_OFFinder, cas-offinder.h:24-107): readInputFile,
+setChrData*, search (loadNextChunk + findPattern + compareAll), and the
+summary table.  Kernel-level calls with the OpenCL kernels' argument contracts
+are `finder_chunk` / `comparer_chunk`.
+
+There is no CPU fallback: importing works without a GPU, but opening an
+engine raises if the library or a CUDA device is missing.
+
+Because the directory name contains a hyphen, load this package with
+`load_package()` from a checkout (or importlib) as `cas_offinder_gb300`.
+"""
+import ctypes
+import os
+import struct
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libcasoff.so")
+CLI_PATH = os.path.join(PKG_DIR, "bin", "cas-offinder")
+
+COF_OK = 0
+STATUS_NAMES = {0: "OK", 1: "CUDA", 2: "ARG", 3: "NOMEM", 4: "INPUT", 5: "IO", 6: "STATE",
+                7: "UNSUPPORTED", 8: "NOT_GENOME", 9: "DEVICE"}
+HEADER = ("##Generated by Cas-OFFinder 3.0.0\n"
+          "#Id\tBulge Type\tcrRNA\tDNA\tChromosome\tLocation\tDirection\tMismatches\tBulge Size\n")
+
+# Every entry point include/cof.h declares (checked by the CPU tests).
+EXPORTS = [
+    "cof_open", "cof_close", "cof_last_error", "cof_open_error", "cof_read_input", "cof_genome_path",
+    "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes",
+    "cof_genome_info", "cof_search", "cof_last_hit_count", "cof_set_summary", "cof_summary_text",
+    "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
+    "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_synchronize",
+    "cofx_synth_record",
+]
+
+_lib = None
+
+
+class CofError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"cof status {status} ({STATUS_NAMES.get(status, '?')}): {message}")
+        self.status = status
+        self.message = message
+
+
+def build():
+    """Compile libcasoff.so and the CLI in-tree (see build.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_cof_build", os.path.join(PKG_DIR, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build()
+
+
+def lib():
+    """The loaded libcasoff.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is missing: build it with cas-offinder_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        c = ctypes
+        vp, u64, u32, sz = c.c_void_p, c.c_uint64, c.c_uint32, c.c_size_t
+        sig = {
+            "cof_open": (c.c_int, [c.c_int, c.POINTER(vp)]),
+            "cof_close": (None, [vp]),
+            "cof_last_error": (c.c_char_p, [vp]),
+            "cof_open_error": (c.c_char_p, []),
+            "cof_read_input": (c.c_int, [vp, c.c_char_p, sz]),
+            "cof_genome_path": (c.c_char_p, [vp]),
+            "cof_input_info": (c.c_int, [vp, c.POINTER(u32), c.POINTER(u32), c.POINTER(u32)]),
+            "cof_genome_load_file": (c.c_int, [vp, c.c_char_p]),
+            "cof_genome_load_text": (c.c_int, [vp, c.c_char_p, u64, c.POINTER(c.c_char_p), c.POINTER(u64), u32]),
+            "cof_genome_load_planes": (c.c_int, [vp, vp, vp, vp, u64, vp, vp, u64, c.POINTER(c.c_char_p),
+                                                 c.POINTER(u64), u32]),
+            "cof_genome_info": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u32)]),
+            "cof_search": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
+            "cof_last_hit_count": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u64)]),
+            "cof_set_summary": (c.c_int, [vp, c.c_int]),
+            "cof_summary_text": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
+            "cof_header_text": (c.c_char_p, []),
+            "cof_finder_chunk": (c.c_int, [vp, c.c_char_p, u64, c.c_char_p, u32, vp, vp, c.POINTER(u32)]),
+            "cof_comparer_chunk": (c.c_int, [vp, c.c_char_p, u64, vp, vp, u32, c.c_char_p, u32, c.c_uint16,
+                                             vp, vp, vp, c.POINTER(u32)]),
+            "cof_plane_words": (u64, [u64]),
+            "cof_pack_text": (u64, [c.c_char_p, u64, vp, vp, vp, vp, vp]),
+            "cof_set_profiling": (c.c_int, [vp, c.c_int]),
+            "cof_kernel_stats": (c.c_int, [vp, c.c_char_p, c.POINTER(u64), c.POINTER(c.c_double),
+                                           c.POINTER(c.c_double)]),
+            "cof_reset_stats": (c.c_int, [vp]),
+            "cof_synchronize": (c.c_int, [vp]),
+            "cofx_synth_record": (u64, [u64, u32, u64, c.c_double, c.c_double, u32, c.c_double, u32, u32, vp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
+
+
+# ---------------------------------------------------------------- packing
+def plane_words(n):
+    return int(lib().cof_plane_words(n))
+
+
+def pack_text(seq: bytes):
+    """Pack a reference-style genome string into (hi, lo, ot, exc_pos, exc_byte) numpy arrays."""
+    L = lib()
+    n = len(seq)
+    W = plane_words(n)
+    hi = np.zeros(W, np.uint32)
+    lo = np.zeros(W, np.uint32)
+    ot = np.zeros(W, np.uint32)
+    ne = int(L.cof_pack_text(seq, n, None, None, None, None, None))
+    ep = np.zeros(ne, np.uint64)
+    eb = np.zeros(ne, np.uint8)
+    L.cof_pack_text(seq, n, _ptr(hi), _ptr(lo), _ptr(ot), _ptr(ep), _ptr(eb))
+    return hi, lo, ot, ep, eb
+
+
+# ---------------------------------------------------------------- engine
+class CasOFFinder:
+    """One CUDA device, one resident genome, one parsed input (see include/cof.h)."""
+
+    def __init__(self, device=0):
+        L = lib()
+        h = ctypes.c_void_p()
+        st = L.cof_open(device, ctypes.byref(h))
+        if st != COF_OK:
+            raise CofError(st, L.cof_open_error().decode())
+        self._L = L
+        self._h = h
+
+    def close(self):
+        if self._h:
+            self._L.cof_close(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != COF_OK:
+            raise CofError(st, self._L.cof_last_error(self._h).decode(errors="replace"))
+
+    # Cas_OFFinder::readInputFile (cas-offinder.cpp:696-751)
+    def readInputFile(self, text):
+        if isinstance(text, str):
+            text = text.encode()
+        self._check(self._L.cof_read_input(self._h, text, len(text)))
+
+    def read_input_path(self, path):
+        with open(path, "rb") as f:
+            self.readInputFile(f.read())
+
+    @property
+    def chrdir(self):
+        return self._L.cof_genome_path(self._h).decode()
+
+    def input_info(self):
+        a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self._L.cof_input_info(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"pattern_len": a.value, "variants": b.value, "bulge_records": c.value}
+
+    # read_fasta / read_twobit + setChrData
+    def load_genome_file(self, path):
+        self._check(self._L.cof_genome_load_file(self._h, os.fsencode(path)))
+
+    def load_genome_text(self, seq: bytes, names, starts):
+        arr_n = (ctypes.c_char_p * max(1, len(names)))(*[n.encode() if isinstance(n, str) else n for n in names])
+        arr_s = (ctypes.c_uint64 * max(1, len(starts)))(*starts)
+        self._check(self._L.cof_genome_load_text(self._h, seq, len(seq), arr_n, arr_s, len(names)))
+
+    def load_genome_planes(self, hi, lo, ot, n, exc_pos, exc_byte, names, starts):
+        arr_n = (ctypes.c_char_p * max(1, len(names)))(*[x.encode() if isinstance(x, str) else x for x in names])
+        arr_s = (ctypes.c_uint64 * max(1, len(starts)))(*starts)
+        self._check(self._L.cof_genome_load_planes(
+            self._h, _ptr(hi), _ptr(lo), _ptr(ot), n, _ptr(exc_pos), _ptr(exc_byte),
+            0 if exc_pos is None else exc_pos.size, arr_n, arr_s, len(names)))
+
+    def genome_info(self):
+        n, r = ctypes.c_uint64(), ctypes.c_uint32()
+        self._check(self._L.cof_genome_info(self._h, ctypes.byref(n), ctypes.byref(r)))
+        return n.value, r.value
+
+    # loadNextChunk + findPattern + compareAll
+    def search(self) -> bytes:
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self._L.cof_search(self._h, ctypes.byref(p), ctypes.byref(n)))
+        return ctypes.string_at(p.value, n.value) if n.value else b""
+
+    def search_view(self):
+        """(address, length) of the rows in the engine's pinned buffer, without a copy."""
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self._L.cof_search(self._h, ctypes.byref(p), ctypes.byref(n)))
+        return p.value, n.value
+
+    def last_hit_count(self):
+        a, b = ctypes.c_uint64(), ctypes.c_uint64()
+        self._check(self._L.cof_last_hit_count(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def set_summary(self, on=True):
+        self._check(self._L.cof_set_summary(self._h, 1 if on else 0))
+
+    def summary(self) -> bytes:
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self._L.cof_summary_text(self._h, ctypes.byref(p), ctypes.byref(n)))
+        return ctypes.string_at(p.value, n.value) if n.value else b""
+
+    # kernel-level entry points (OpenCL argument contracts)
+    def finder_chunk(self, chr_bytes: bytes, worksize: int, pat2: bytes, patternlen: int):
+        loci = np.zeros(max(1, worksize), np.uint32)
+        flag = np.zeros(max(1, worksize), np.uint8)
+        cnt = ctypes.c_uint32()
+        self._check(self._L.cof_finder_chunk(self._h, chr_bytes, worksize, pat2, patternlen, _ptr(loci),
+                                             _ptr(flag), ctypes.byref(cnt)))
+        return loci[:cnt.value].copy(), flag[:cnt.value].copy()
+
+    def comparer_chunk(self, chr_bytes: bytes, loci, flag, comp: bytes, threshold: int):
+        loci = np.ascontiguousarray(loci, np.uint32)
+        flag = np.ascontiguousarray(flag, np.uint8)
+        cap = max(1, 2 * loci.size)
+        mm_loci = np.zeros(cap, np.uint32)
+        mm_count = np.zeros(cap, np.uint16)
+        direction = np.zeros(cap, np.uint8)
+        cnt = ctypes.c_uint32()
+        self._check(self._L.cof_comparer_chunk(self._h, chr_bytes, len(chr_bytes), _ptr(loci), _ptr(flag),
+                                               loci.size, comp, len(comp), threshold, _ptr(mm_loci),
+                                               _ptr(mm_count), _ptr(direction), ctypes.byref(cnt)))
+        k = cnt.value
+        return mm_loci[:k].copy(), mm_count[:k].copy(), direction[:k].tobytes()
+
+    # instrumentation
+    def set_profiling(self, on=True):
+        self._check(self._L.cof_set_profiling(self._h, 1 if on else 0))
+
+    def reset_stats(self):
+        self._check(self._L.cof_reset_stats(self._h))
+
+    def kernel_stats(self, name):
+        a, b, c = ctypes.c_uint64(), ctypes.c_double(), ctypes.c_double()
+        self._check(self._L.cof_kernel_stats(self._h, name.encode(), ctypes.byref(a), ctypes.byref(b),
+                                             ctypes.byref(c)))
+        return {"launches": a.value, "ms": b.value, "units": c.value}
+
+    def synchronize(self):
+        self._check(self._L.cof_synchronize(self._h))
+
+
+# ---------------------------------------------------------------- synthetic genomes
+def synth_record(seed, record, length, gc=0.41, gc_drift=0.0, drift_window=100000, n_frac=0.0,
+                 n_run_min=100, n_run_max=10000) -> bytearray:
+    """One synthetic record (see include/cof_tools.h)."""
+    out = bytearray(length)
+    if length:
+        buf = (ctypes.c_char * length).from_buffer(out)
+        lib().cofx_synth_record(seed, record, length, gc, gc_drift, drift_window, n_frac, n_run_min, n_run_max,
+                                ctypes.cast(buf, ctypes.c_void_p))
+    return out
+
+
+def record_lengths(seed, count, total, lo=47_000_000, hi=249_000_000):
+    """`count` lengths drawn log-uniform in [lo, hi], rescaled to sum to `total`."""
+    rng = np.random.default_rng(seed)
+    raw = np.exp(rng.uniform(np.log(lo), np.log(hi), count))
+    lens = np.floor(raw / raw.sum() * total).astype(np.int64)
+    lens[-1] += total - lens.sum()
+    return [int(x) for x in lens]
+
+
+def write_fasta(path, names, seqs, width=60):
+    with open(path, "wb") as f:
+        for name, s in zip(names, seqs):
+            f.write(b">" + (name.encode() if isinstance(name, str) else name) + b"\n")
+            mv = memoryview(bytes(s))
+            for i in range(0, len(mv), width):
+                f.write(mv[i:i + width])
+                f.write(b"\n")
+
+
+_TWOBIT_CODE = np.full(256, 0, np.uint8)
+for _b, _c in ((b"T", 0), (b"C", 1), (b"A", 2), (b"G", 3), (b"t", 0), (b"c", 1), (b"a", 2), (b"g", 3)):
+    _TWOBIT_CODE[_b[0]] = _c
+
+
+def write_twobit(path, names, seqs, mask_blocks=None):
+    """Write a UCSC .2bit file (version 0, little-endian).  Bytes other than
+    ACGT become N blocks.  `mask_blocks`: optional per-record list of
+    (start, size) soft-mask blocks."""
+    names = [n.encode() if isinstance(n, str) else n for n in names]
+    header = struct.pack("<IIII", 0x1A412743, 0, len(names), 0)
+    index_size = sum(1 + len(n) + 4 for n in names)
+    recs = []
+    for i, s in enumerate(seqs):
+        a = np.frombuffer(bytes(s), np.uint8)
+        isn = ~np.isin(a, np.frombuffer(b"ACGTacgt", np.uint8))
+        starts, sizes = [], []
+        if isn.any():
+            d = np.diff(np.concatenate(([0], isn.astype(np.int8), [0])))
+            st = np.flatnonzero(d == 1)
+            en = np.flatnonzero(d == -1)
+            starts, sizes = st.tolist(), (en - st).tolist()
+        codes = _TWOBIT_CODE[a]
+        pad = (-len(codes)) % 4
+        codes = np.concatenate((codes, np.zeros(pad, np.uint8))).reshape(-1, 4)
+        packed = (codes[:, 0] << 6 | codes[:, 1] << 4 | codes[:, 2] << 2 | codes[:, 3]).astype(np.uint8)
+        mb = (mask_blocks[i] if mask_blocks else []) or []
+        rec = struct.pack("<II", len(a), len(starts))
+        rec += struct.pack(f"<{len(starts)}I", *starts) + struct.pack(f"<{len(sizes)}I", *sizes)
+        rec += struct.pack("<I", len(mb))
+        rec += struct.pack(f"<{len(mb)}I", *[m[0] for m in mb]) + struct.pack(f"<{len(mb)}I", *[m[1] for m in mb])
+        rec += struct.pack("<I", 0) + packed.tobytes()
+        recs.append(rec)
+    with open(path, "wb") as f:
+        f.write(header)
+        off = 16 + index_size
+        for n, r in zip(names, recs):
+            f.write(bytes([len(n)]) + n + struct.pack("<I", off))
+            off += len(r)
+        for r in recs:
+            f.write(r)
+
+
+def reference_text(seqs):
+    """The reference's in-memory genome for records `seqs`: upper-cased,
+    joined by ';', with the start offset of each record (read_fasta.cpp:41-45)."""
+    starts, parts, pos = [], [], 0
+    for i, s in enumerate(seqs):
+        if i:
+            parts.append(b";")
+            pos += 1
+        starts.append(pos)
+        b = bytes(s).upper()
+        parts.append(b)
+        pos += len(b)
+    return b"".join(parts), starts

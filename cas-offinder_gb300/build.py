@@ -1,0 +1,94 @@
+#!/usr/bin/env python3
+"""Builds libcasoff.so (CUDA kernels + C ABI) and the cas-offinder CLI in-tree.
+
+Outputs (git-ignored):
+  cas-offinder_gb300/lib/libcasoff.so
+  cas-offinder_gb300/bin/cas-offinder
+Objects go to cas-offinder_gb300/_build/.  Translation units compile in
+parallel; a unit is rebuilt when its source or any header is newer than its
+object.  CUDA code is compiled for sm_103a only.
+"""
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+BUILD = os.path.join(PKG, "_build")
+LIB = os.path.join(PKG, "lib", "libcasoff.so")
+CLI = os.path.join(PKG, "bin", "cas-offinder")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
+              "--expt-relaxed-constexpr", *ARCH]
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
+
+CU_SOURCES = ["kernels.cu", "engine.cu"]
+CPP_SOURCES = ["input.cpp", "genome_io.cpp", "synth.cpp"]
+
+
+def nvcc():
+    for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _headers():
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    hs.append(os.path.join(ROOT, "include", "cof.h"))
+    return hs
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def _run(cmd):
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+    return r.stderr
+
+
+def build(verbose=False):
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    os.makedirs(os.path.dirname(CLI), exist_ok=True)
+    hdrs = _headers()
+    jobs = []
+    objs = []
+    for src in CU_SOURCES + CPP_SOURCES:
+        path = os.path.join(CSRC, src)
+        if not os.path.exists(path):
+            continue
+        obj = os.path.join(BUILD, src + ".o")
+        objs.append(obj)
+        if not _stale(obj, [path] + hdrs):
+            continue
+        if src.endswith(".cu"):
+            cmd = [nvcc(), *NVCC_FLAGS, "-c", path, "-o", obj]
+        else:
+            cmd = ["g++", *CXX_FLAGS, "-c", path, "-o", obj]
+        jobs.append(cmd)
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
+        for out in ex.map(_run, jobs):
+            if verbose and out:
+                print(out, file=sys.stderr)
+    if _stale(LIB, objs):
+        _run([nvcc(), "-shared", *ARCH, "-o", LIB, *objs, "-cudart", "static", "-lpthread"])
+    cli_src = os.path.join(CSRC, "cli.cpp")
+    if _stale(CLI, [cli_src, LIB] + hdrs):
+        _run(["g++", *CXX_FLAGS, cli_src, "-o", CLI, "-L" + os.path.dirname(LIB), "-lcasoff",
+              "-Wl,-rpath,$ORIGIN/../lib"])
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,826 @@
+// libcasoff.so: the C ABI of include/cof.h on top of the GB300 kernels.
+//
+// One handle = one CUDA device, one stream, one resident genome and one
+// parsed input file (a "job").  A search walks the genome in segments of
+// kSegPositions start positions: the finder appends that segment's oriented
+// candidates to a queue, the comparer tests them against every compare
+// variant and appends hit keys.  Hits are then sorted on the device into the
+// reference's row order and formatted into TSV rows on the device.  The host
+// only waits twice per search: for the hit count and for the text size.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cof.h"
+#include "cof_internal.h"
+#include "kernels.cuh"
+
+namespace {
+
+using namespace cof;
+
+constexpr uint64_t kSegPositions = 1ull << 26;  // start positions per finder/comparer pass
+constexpr uint64_t kSegWords = kSegPositions / 32;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  template <typename T>
+  T* as() const {
+    return (T*)p;
+  }
+};
+
+struct HostPinned {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~HostPinned() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMallocHost(&p, bytes ? bytes : 1);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+};
+
+// A genome resident on the device.
+struct DevGenome {
+  uint64_t n = 0;
+  uint32_t n_rec = 0;
+  uint64_t n_exc = 0;
+  DevBuf hi, lo, ot, exc_pos, exc_byte, rec_start, rec_name_off, rec_name_len, rec_names;
+  bool loaded = false;
+  GenomeView view() const {
+    GenomeView g;
+    g.hi = hi.as<uint32_t>();
+    g.lo = lo.as<uint32_t>();
+    g.ot = ot.as<uint32_t>();
+    g.exc_pos = exc_pos.as<uint64_t>();
+    g.exc_byte = exc_byte.as<uint8_t>();
+    g.n_exc = n_exc;
+    g.n = n;
+    g.rec_start = rec_start.as<uint64_t>();
+    g.rec_name_off = rec_name_off.as<uint32_t>();
+    g.rec_name_len = rec_name_len.as<uint32_t>();
+    g.rec_names = rec_names.as<char>();
+    g.n_rec = n_rec;
+    return g;
+  }
+};
+
+struct KernelStat {
+  uint64_t launches = 0;
+  double ms = 0;
+  double units = 0;
+};
+
+}  // namespace
+
+struct cof_handle {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  Job job;
+  bool has_job = false;
+  bool job_on_device = false;
+  int nw = 1;
+  std::vector<uint32_t> nonN;  // non-N positions per variant
+  DevBuf vmask, vfmt, sfmt, pool;
+  FinderPattern fpat{};
+
+  DevGenome genome, scratch;
+
+  DevBuf queue, qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small;
+  HostPinned host_text;
+  std::string summary_text;
+  std::map<std::string, unsigned long long> summary;
+  bool summary_on = false;
+  uint64_t last_hits = 0, last_rows = 0;
+
+  bool profiling = false;
+  std::map<std::string, KernelStat> stats;
+};
+
+namespace {
+
+std::mutex g_open_mu;
+std::string g_open_err;
+
+cof_status fail(cof_handle* h, cof_status st, const std::string& msg) {
+  h->err = msg;
+  return st;
+}
+
+#define COF_CUDA(h, call)                                                                           \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      return fail(h, e_ == cudaErrorMemoryAllocation ? COF_ERR_NOMEM : COF_ERR_CUDA,                \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                              \
+  } while (0)
+
+// Uploads a packed genome into `dg` (copies are stream-ordered on h->stream).
+cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
+                         uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
+                         const std::vector<std::string>& names, const std::vector<uint64_t>& starts) {
+  const uint64_t W = plane_words(n);
+  dg.loaded = false;
+  COF_CUDA(h, dg.hi.ensure(W * 4));
+  COF_CUDA(h, dg.lo.ensure(W * 4));
+  COF_CUDA(h, dg.ot.ensure(W * 4));
+  COF_CUDA(h, cudaMemcpyAsync(dg.hi.p, hi, W * 4, cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(dg.lo.p, lo, W * 4, cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(dg.ot.p, ot, W * 4, cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, dg.exc_pos.ensure(n_exc * 8));
+  COF_CUDA(h, dg.exc_byte.ensure(n_exc));
+  if (n_exc) {
+    COF_CUDA(h, cudaMemcpyAsync(dg.exc_pos.p, exc_pos, n_exc * 8, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(dg.exc_byte.p, exc_byte, n_exc, cudaMemcpyHostToDevice, h->stream));
+  }
+  std::vector<uint32_t> off(names.size()), len(names.size());
+  std::string pool;
+  for (size_t i = 0; i < names.size(); ++i) {
+    off[i] = (uint32_t)pool.size();
+    len[i] = (uint32_t)names[i].size();
+    pool += names[i];
+  }
+  const size_t R = std::min(names.size(), starts.size());
+  COF_CUDA(h, dg.rec_start.ensure(std::max<size_t>(R, 1) * 8));
+  COF_CUDA(h, dg.rec_name_off.ensure(std::max<size_t>(R, 1) * 4));
+  COF_CUDA(h, dg.rec_name_len.ensure(std::max<size_t>(R, 1) * 4));
+  COF_CUDA(h, dg.rec_names.ensure(std::max<size_t>(pool.size(), 1)));
+  if (R) {
+    COF_CUDA(h, cudaMemcpyAsync(dg.rec_start.p, starts.data(), R * 8, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(dg.rec_name_off.p, off.data(), R * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(dg.rec_name_len.p, len.data(), R * 4, cudaMemcpyHostToDevice, h->stream));
+  }
+  if (!pool.empty())
+    COF_CUDA(h, cudaMemcpyAsync(dg.rec_names.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, h->stream));
+  // Host vectors above are freed on return: wait for the copies.
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  dg.n = n;
+  dg.n_exc = n_exc;
+  dg.n_rec = (uint32_t)R;
+  dg.loaded = true;
+  return COF_OK;
+}
+
+cof_status upload_packed(cof_handle* h, DevGenome& dg, const PackedGenome& g) {
+  return upload_genome(h, dg, g.hi.data(), g.lo.data(), g.ot.data(), g.n, g.exc_pos.data(), g.exc_byte.data(),
+                       g.exc_pos.size(), g.names, g.starts);
+}
+
+// PAM-scan pattern from the forward pattern and its reverse complement.
+bool make_finder_pattern(const std::string& fwd, const std::string& rev, FinderPattern& fp) {
+  const size_t L = fwd.size();
+  if (L == 0 || L > (size_t)kMaxL || rev.size() != L) return false;
+  std::memset(&fp, 0, sizeof fp);
+  fp.L = (uint32_t)L;
+  for (size_t k = 0; k < L; ++k) {
+    const uint32_t mf = class_bits_of((unsigned char)fwd[k]);
+    if (mf) {
+      fp.fk[fp.nf] = (uint8_t)k;
+      fp.fm[fp.nf++] = (uint8_t)mf;
+    }
+    const uint32_t mr = class_bits_of((unsigned char)rev[k]);
+    if (mr) {
+      fp.rk[fp.nr] = (uint8_t)k;
+      fp.rm[fp.nr++] = (uint8_t)mr;
+    }
+  }
+  return true;
+}
+
+std::string revcomp(const std::string& s) {
+  std::string r(s.rbegin(), s.rend());
+  for (char& c : r) c = (char)complement_byte((unsigned char)c);
+  return r;
+}
+
+template <int NW>
+void fill_mask(VariantMask<NW>& vm, const std::string& comp, uint32_t thr, uint32_t gid) {
+  std::memset(&vm, 0, sizeof vm);
+  for (size_t k = 0; k < comp.size(); ++k) {
+    const uint32_t m = class_bits_of((unsigned char)comp[k]);
+    const uint32_t bit = 1u << (k & 31);
+    const int w = (int)(k >> 5);
+    if (m & 1) vm.t[w] |= bit;
+    if (m & 2) vm.c[w] |= bit;
+    if (m & 4) vm.a[w] |= bit;
+    if (m & 8) vm.g[w] |= bit;
+    if (m & 16) vm.o[w] |= bit;
+  }
+  vm.thr = thr;
+  vm.gid = gid;
+}
+
+// Uploads the variant masks and formatting tables of the current job.
+cof_status upload_job(cof_handle* h) {
+  if (h->job_on_device) return COF_OK;
+  const Job& job = h->job;
+  const size_t L = job.pattern.size();
+  if (L > (size_t)kMaxL)
+    return fail(h, COF_ERR_UNSUPPORTED, "pattern length " + std::to_string(L) + " exceeds " + std::to_string(kMaxL));
+  if (job.variants.size() >= (1u << 20)) return fail(h, COF_ERR_UNSUPPORTED, "more than 2^20 compare variants");
+  h->nw = L <= 32 ? 1 : 2;
+  make_finder_pattern(job.pattern, revcomp(job.pattern), h->fpat);
+  const size_t V = job.variants.size();
+  h->nonN.assign(V, 0);
+  std::vector<unsigned char> masks;
+  const size_t msz = h->nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>);
+  masks.resize(std::max<size_t>(V, 1) * msz);
+  std::string pool;
+  std::vector<VariantFmt> vf(V);
+  std::vector<ShapeFmt> sf;
+  auto put = [&](const std::string& s) {
+    const uint32_t o = (uint32_t)pool.size();
+    pool += s;
+    return o;
+  };
+  for (size_t v = 0; v < V; ++v) {
+    const Variant& var = job.variants[v];
+    for (char c : var.key) h->nonN[v] += c != 'N';
+    if (h->nw == 1) fill_mask<1>(((VariantMask<1>*)masks.data())[v], var.key, var.threshold, (uint32_t)v);
+    else fill_mask<2>(((VariantMask<2>*)masks.data())[v], var.key, var.threshold, (uint32_t)v);
+    vf[v].comp_off = put(var.key);
+    vf[v].L = (uint32_t)L;
+    for (int s = 0; s < 2; ++s) {
+      vf[v].shape_begin[s] = (uint32_t)sf.size();
+      for (const RowShape& r : job.shapes[s][v]) {
+        ShapeFmt f;
+        f.head_off = put(r.head);
+        f.head_len = (uint32_t)r.head.size();
+        f.dna_off = put(r.dna);
+        f.dna_len = (uint32_t)r.dna.size();
+        f.tail_off = put(r.tail);
+        f.tail_len = (uint32_t)r.tail.size();
+        f.offset = r.offset;
+        f.dir = s ? '-' : '+';
+        sf.push_back(f);
+      }
+      vf[v].shape_end[s] = (uint32_t)sf.size();
+    }
+  }
+  COF_CUDA(h, h->vmask.ensure(masks.size()));
+  COF_CUDA(h, h->vfmt.ensure(std::max<size_t>(V, 1) * sizeof(VariantFmt)));
+  COF_CUDA(h, h->sfmt.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
+  COF_CUDA(h, h->pool.ensure(std::max<size_t>(pool.size(), 1)));
+  COF_CUDA(h, cudaMemcpyAsync(h->vmask.p, masks.data(), masks.size(), cudaMemcpyHostToDevice, h->stream));
+  if (V) COF_CUDA(h, cudaMemcpyAsync(h->vfmt.p, vf.data(), V * sizeof(VariantFmt), cudaMemcpyHostToDevice, h->stream));
+  if (!sf.empty())
+    COF_CUDA(h, cudaMemcpyAsync(h->sfmt.p, sf.data(), sf.size() * sizeof(ShapeFmt), cudaMemcpyHostToDevice, h->stream));
+  if (!pool.empty()) COF_CUDA(h, cudaMemcpyAsync(h->pool.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->job_on_device = true;
+  return COF_OK;
+}
+
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  std::string name;
+  double units = 0;
+};
+
+cof_status record_start(cof_handle* h, std::vector<EventPair>& evs, const char* name, double units) {
+  if (!h->profiling) return COF_OK;
+  EventPair p;
+  p.name = name;
+  p.units = units;
+  COF_CUDA(h, cudaEventCreate(&p.a));
+  COF_CUDA(h, cudaEventCreate(&p.b));
+  COF_CUDA(h, cudaEventRecord(p.a, h->stream));
+  evs.push_back(p);
+  return COF_OK;
+}
+cof_status record_stop(cof_handle* h, std::vector<EventPair>& evs) {
+  if (!h->profiling) return COF_OK;
+  COF_CUDA(h, cudaEventRecord(evs.back().b, h->stream));
+  return COF_OK;
+}
+void collect(cof_handle* h, std::vector<EventPair>& evs) {
+  for (EventPair& p : evs) {
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+      KernelStat& s = h->stats[p.name];
+      s.launches += 1;
+      s.ms += ms;
+      s.units += p.units;
+    }
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  evs.clear();
+}
+
+// Finder + comparer over the whole genome; leaves the hit count in h->hit_count.
+cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& evs, uint64_t* seg_count) {
+  const DevGenome& dg = h->genome;
+  const GenomeView gv = dg.view();
+  const uint64_t L = h->job.pattern.size();
+  const uint64_t npos = dg.n >= L ? dg.n - L + 1 : 0;
+  const uint64_t total_words = (npos + 31) / 32;
+  const uint64_t nseg = (total_words + kSegWords - 1) / kSegWords;
+  *seg_count = nseg;
+  COF_CUDA(h, h->qcounts.ensure(std::max<uint64_t>(nseg, 1) * 4));
+  COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<uint64_t>(nseg, 1) * 4, h->stream));
+  COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
+  for (uint64_t s = 0; s < nseg; ++s) {
+    const uint64_t w0 = s * kSegWords, w1 = std::min(total_words, w0 + kSegWords);
+    uint32_t* qc = h->qcounts.as<uint32_t>() + s;
+    cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32);
+    if (st) return st;
+    launch_finder(gv, w0, w1, h->fpat, h->queue.as<uint32_t>(), qc, h->stream);
+    if ((st = record_stop(h, evs))) return st;
+    if ((st = record_start(h, evs, "comparer", 0))) return st;
+    launch_comparer(gv, h->queue.as<uint32_t>(), qc, w0 * 32, h->vmask.p, (uint32_t)h->job.variants.size(), h->nw,
+                    (uint32_t)L, h->hits.as<uint64_t>(), h->hit_count.as<unsigned long long>(), hit_cap,
+                    h->sm_count, h->stream);
+    if ((st = record_stop(h, evs))) return st;
+  }
+  COF_CUDA(h, cudaGetLastError());
+  return COF_OK;
+}
+
+cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
+  if (!h->has_job) return fail(h, COF_ERR_STATE, "no input file has been read");
+  if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
+  cof_status st = upload_job(h);
+  if (st) return st;
+  *rows = nullptr;
+  *rows_len = 0;
+  h->last_hits = h->last_rows = 0;
+  const uint64_t V = h->job.variants.size();
+  const uint64_t L = h->job.pattern.size();
+  if (V == 0 || h->genome.n < L) {
+    *rows = "";
+    return COF_OK;
+  }
+  COF_CUDA(h, h->queue.ensure(2 * kSegPositions * 4));
+  COF_CUDA(h, h->hit_count.ensure(8));
+  uint64_t cap = std::max<uint64_t>(h->hits.cap / 8, 1u << 20);
+  COF_CUDA(h, h->hits.ensure(cap * 8));
+  std::vector<EventPair> evs;
+  uint64_t nseg = 0, nhits = 0;
+  for (;;) {
+    if ((st = run_passes(h, cap, evs, &nseg))) return st;
+    COF_CUDA(h, cudaMemcpyAsync(&nhits, h->hit_count.p, 8, cudaMemcpyDeviceToHost, h->stream));
+    COF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (nhits <= cap) break;
+    collect(h, evs);  // the overflowing pass counts as work done
+    cap = nhits + nhits / 8;
+    COF_CUDA(h, h->hits.ensure(cap * 8));
+  }
+  if (h->profiling) {
+    // Comparer units: base comparisons = oriented candidates x non-N variant positions.
+    std::vector<uint32_t> qc(nseg);
+    COF_CUDA(h, cudaMemcpy(qc.data(), h->qcounts.p, nseg * 4, cudaMemcpyDeviceToHost));
+    double nonN = 0;
+    for (uint32_t x : h->nonN) nonN += x;
+    size_t si = 0;
+    for (EventPair& p : evs)
+      if (p.name == "comparer" && si < nseg) p.units = (double)qc[si++] * nonN;
+    collect(h, evs);
+  }
+  h->last_hits = nhits;
+  if (nhits == 0) {
+    *rows = "";
+    return COF_OK;
+  }
+  // Sort hit keys into output order.
+  COF_CUDA(h, h->hits_sorted.ensure(nhits * 8));
+  COF_CUDA(h, h->row_bytes.ensure(nhits * 8));
+  COF_CUDA(h, h->row_offsets.ensure(nhits * 8));
+  COF_CUDA(h, h->row_count.ensure(nhits * 4));
+  COF_CUDA(h, h->small.ensure(64));
+  size_t tmp = 0;
+  COF_CUDA(h, cub::DeviceRadixSort::SortKeys(nullptr, tmp, h->hits.as<uint64_t>(), h->hits_sorted.as<uint64_t>(),
+                                             (int64_t)nhits, 0, 64, h->stream));
+  size_t tmp2 = 0;
+  COF_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, tmp2, h->row_bytes.as<uint64_t>(), h->row_offsets.as<uint64_t>(),
+                                            (int64_t)nhits, h->stream));
+  size_t tmp3 = 0;
+  COF_CUDA(h, cub::DeviceReduce::Sum(nullptr, tmp3, h->row_count.as<uint32_t>(), h->small.as<uint64_t>(),
+                                     (int64_t)nhits, h->stream));
+  COF_CUDA(h, h->sort_tmp.ensure(std::max(tmp, std::max(tmp2, tmp3))));
+  tmp = h->sort_tmp.cap;
+  COF_CUDA(h, cub::DeviceRadixSort::SortKeys(h->sort_tmp.p, tmp, h->hits.as<uint64_t>(), h->hits_sorted.as<uint64_t>(),
+                                             (int64_t)nhits, 0, 64, h->stream));
+  // Row sizes, offsets, then the rows themselves.
+  const GenomeView gv = h->genome.view();
+  FormatTables ft{h->vfmt.as<VariantFmt>(), h->sfmt.as<ShapeFmt>(), h->pool.as<char>()};
+  if ((st = record_start(h, evs, "format", (double)nhits))) return st;
+  launch_row_lengths(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_bytes.as<uint64_t>(),
+                     h->row_count.as<uint32_t>(), h->stream);
+  tmp = h->sort_tmp.cap;
+  COF_CUDA(h, cub::DeviceScan::ExclusiveSum(h->sort_tmp.p, tmp, h->row_bytes.as<uint64_t>(),
+                                            h->row_offsets.as<uint64_t>(), (int64_t)nhits, h->stream));
+  tmp = h->sort_tmp.cap;
+  COF_CUDA(h, cub::DeviceReduce::Sum(h->sort_tmp.p, tmp, h->row_count.as<uint32_t>(), h->small.as<uint64_t>(),
+                                     (int64_t)nhits, h->stream));
+  uint64_t tail[3] = {0, 0, 0};
+  COF_CUDA(h, cudaMemcpyAsync(&tail[0], h->row_offsets.as<uint64_t>() + nhits - 1, 8, cudaMemcpyDeviceToHost,
+                              h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(&tail[1], h->row_bytes.as<uint64_t>() + nhits - 1, 8, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(&tail[2], h->small.p, 8, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  const uint64_t bytes = tail[0] + tail[1];
+  COF_CUDA(h, h->text.ensure(bytes + 1));
+  launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), h->text.as<char>(),
+                    h->stream);
+  if ((st = record_stop(h, evs))) return st;
+  COF_CUDA(h, cudaGetLastError());
+  COF_CUDA(h, h->host_text.ensure(bytes + 1));
+  COF_CUDA(h, cudaMemcpyAsync(h->host_text.p, h->text.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  ((char*)h->host_text.p)[bytes] = 0;
+  collect(h, evs);
+  h->last_rows = tail[2];
+  if (h->summary_on) {
+    std::vector<uint64_t> keys(nhits);
+    COF_CUDA(h, cudaMemcpy(keys.data(), h->hits_sorted.p, nhits * 8, cudaMemcpyDeviceToHost));
+    for (uint64_t k : keys) {
+      const uint32_t gid = (uint32_t)(k >> 44), strand = (uint32_t)((k >> 7) & 1), mm = (uint32_t)(k & 0x7F);
+      const Variant& var = h->job.variants[gid];
+      for (const RowShape& r : h->job.shapes[strand][gid]) {
+        char key[10000];
+        snprintf(key, sizeof key, "%s,%s,%d,%d", var.id.c_str(), r.type.c_str(), (int)r.bulge_size, (int)mm);
+        ++h->summary[key];
+      }
+    }
+  }
+  *rows = (const char*)h->host_text.p;
+  *rows_len = bytes;
+  return COF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cof_open_error(void) {
+  std::lock_guard<std::mutex> g(g_open_mu);
+  return g_open_err.c_str();
+}
+
+cof_status cof_open(int device, cof_handle** out) {
+  if (!out) return COF_ERR_ARG;
+  *out = nullptr;
+  auto set_err = [](const std::string& m) {
+    std::lock_guard<std::mutex> g(g_open_mu);
+    g_open_err = m;
+  };
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    set_err(std::string("no CUDA device: ") + cudaGetErrorString(e));
+    return COF_ERR_CUDA;
+  }
+  if (device < 0 || device >= count) {
+    set_err("device ordinal out of range");
+    return COF_ERR_ARG;
+  }
+  if ((e = cudaSetDevice(device)) != cudaSuccess) {
+    set_err(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    return COF_ERR_CUDA;
+  }
+  cof_handle* h = new cof_handle();
+  h->device = device;
+  cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+    set_err(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
+    delete h;
+    return COF_ERR_CUDA;
+  }
+  *out = h;
+  return COF_OK;
+}
+
+void cof_close(cof_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  cudaStream_t s = h->stream;
+  delete h;  // frees device buffers
+  if (s) cudaStreamDestroy(s);
+}
+
+const char* cof_last_error(const cof_handle* h) { return h ? h->err.c_str() : "null handle"; }
+
+cof_status cof_read_input(cof_handle* h, const char* text, size_t len) {
+  if (!h || (!text && len)) return COF_ERR_ARG;
+  h->err.clear();
+  Job job;
+  std::string err;
+  if (!parse_job(text ? text : "", len, job, err)) return fail(h, COF_ERR_INPUT, err);
+  if (!build_shapes(job, err)) return fail(h, COF_ERR_INPUT, err);
+  h->job = std::move(job);
+  h->has_job = true;
+  h->job_on_device = false;
+  h->summary.clear();
+  return COF_OK;
+}
+
+const char* cof_genome_path(const cof_handle* h) { return (h && h->has_job) ? h->job.genome_path.c_str() : ""; }
+
+cof_status cof_input_info(const cof_handle* h, uint32_t* pattern_len, uint32_t* n_variants, uint32_t* n_bulge_records) {
+  if (!h) return COF_ERR_ARG;
+  if (!h->has_job) return COF_ERR_STATE;
+  if (pattern_len) *pattern_len = (uint32_t)h->job.pattern.size();
+  if (n_variants) *n_variants = (uint32_t)h->job.variants.size();
+  if (n_bulge_records) {
+    uint32_t n = 0;
+    for (const Variant& v : h->job.variants) n += (uint32_t)v.bulges.size();
+    *n_bulge_records = n;
+  }
+  return COF_OK;
+}
+
+cof_status cof_genome_load_file(cof_handle* h, const char* path) {
+  if (!h || !path) return COF_ERR_ARG;
+  h->err.clear();
+  cudaSetDevice(h->device);
+  PackedGenome g;
+  if (load_fasta(path, g) != 0) {
+    g = PackedGenome();
+    if (load_twobit(path, g) != 0) return fail(h, COF_ERR_NOT_GENOME, std::string("Skipping non-acceptable file ") + path);
+  }
+  return upload_packed(h, h->genome, g);
+}
+
+cof_status cof_genome_load_text(cof_handle* h, const char* seq, uint64_t n, const char* const* names,
+                                const uint64_t* starts, uint32_t n_records) {
+  if (!h || (!seq && n) || (n_records && (!names || !starts))) return COF_ERR_ARG;
+  h->err.clear();
+  cudaSetDevice(h->device);
+  PackedGenome g;
+  g.n = n;
+  const uint64_t W = plane_words(n);
+  g.hi.assign(W, 0);
+  g.lo.assign(W, 0);
+  g.ot.assign(W, 0);
+  pack_text(seq, n, g.hi.data(), g.lo.data(), g.ot.data(), &g.exc_pos, &g.exc_byte);
+  for (uint32_t i = 0; i < n_records; ++i) {
+    g.names.push_back(names[i] ? names[i] : "");
+    g.starts.push_back(starts[i]);
+  }
+  return upload_packed(h, h->genome, g);
+}
+
+cof_status cof_genome_load_planes(cof_handle* h, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
+                                  uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
+                                  const char* const* names, const uint64_t* starts, uint32_t n_records) {
+  if (!h || !hi || !lo || !ot || (n_exc && (!exc_pos || !exc_byte)) || (n_records && (!names || !starts)))
+    return COF_ERR_ARG;
+  h->err.clear();
+  cudaSetDevice(h->device);
+  std::vector<std::string> nm;
+  std::vector<uint64_t> st;
+  for (uint32_t i = 0; i < n_records; ++i) {
+    nm.push_back(names[i] ? names[i] : "");
+    st.push_back(starts[i]);
+  }
+  return upload_genome(h, h->genome, hi, lo, ot, n, exc_pos, exc_byte, n_exc, nm, st);
+}
+
+cof_status cof_genome_info(const cof_handle* h, uint64_t* n, uint32_t* n_records) {
+  if (!h) return COF_ERR_ARG;
+  if (!h->genome.loaded) return COF_ERR_STATE;
+  if (n) *n = h->genome.n;
+  if (n_records) *n_records = h->genome.n_rec;
+  return COF_OK;
+}
+
+cof_status cof_search(cof_handle* h, const char** rows, size_t* rows_len) {
+  if (!h || !rows || !rows_len) return COF_ERR_ARG;
+  h->err.clear();
+  cudaSetDevice(h->device);
+  return do_search(h, rows, rows_len);
+}
+
+cof_status cof_last_hit_count(const cof_handle* h, uint64_t* n_hits, uint64_t* n_rows) {
+  if (!h) return COF_ERR_ARG;
+  if (n_hits) *n_hits = h->last_hits;
+  if (n_rows) *n_rows = h->last_rows;
+  return COF_OK;
+}
+
+cof_status cof_set_summary(cof_handle* h, int enable) {
+  if (!h) return COF_ERR_ARG;
+  h->summary_on = enable != 0;
+  return COF_OK;
+}
+
+cof_status cof_summary_text(cof_handle* h, const char** text, size_t* len) {
+  if (!h || !text || !len) return COF_ERR_ARG;
+  static const char* kHead[4] = {"Id", "Bulge Type", "Bulge Size", "Mismatches"};
+  std::string out;
+  for (const auto& kv : h->summary) {
+    std::string key = kv.first;
+    out += "##";
+    size_t cut;
+    int col = 0;
+    while ((cut = key.find(',')) != std::string::npos && col < 3) {
+      out += std::string(kHead[col++]) + "=" + key.substr(0, cut) + ";";
+      key.erase(0, cut + 1);
+    }
+    out += std::string(kHead[col]) + "=" + key + ";";
+    out += "Number of Found Targets=" + std::to_string(kv.second) + "\n";
+  }
+  h->summary_text = out;
+  *text = h->summary_text.c_str();
+  *len = h->summary_text.size();
+  return COF_OK;
+}
+
+const char* cof_header_text(void) {
+  return "##Generated by Cas-OFFinder 3.0.0\n"
+         "#Id\tBulge Type\tcrRNA\tDNA\tChromosome\tLocation\tDirection\tMismatches\tBulge Size\n";
+}
+
+cof_status cof_finder_chunk(cof_handle* h, const char* chr, uint64_t worksize, const char* pat, uint32_t patternlen,
+                            uint32_t* loci, uint8_t* flag, uint32_t* entrycount) {
+  if (!h || !chr || !pat || !loci || !flag || !entrycount || patternlen == 0) return COF_ERR_ARG;
+  if (patternlen > (uint32_t)kMaxL) return fail(h, COF_ERR_UNSUPPORTED, "pattern too long");
+  if (worksize >= (1ull << 31)) return fail(h, COF_ERR_ARG, "worksize must be below 2^31");
+  h->err.clear();
+  cudaSetDevice(h->device);
+  *entrycount = 0;
+  if (worksize == 0) return COF_OK;
+  const uint64_t n = worksize + patternlen - 1;
+  PackedGenome g;
+  g.n = n;
+  g.hi.assign(plane_words(n), 0);
+  g.lo.assign(plane_words(n), 0);
+  g.ot.assign(plane_words(n), 0);
+  pack_text(chr, n, g.hi.data(), g.lo.data(), g.ot.data(), &g.exc_pos, &g.exc_byte);
+  cof_status st = upload_packed(h, h->scratch, g);
+  if (st) return st;
+  FinderPattern fp;
+  make_finder_pattern(std::string(pat, patternlen), std::string(pat + patternlen, patternlen), fp);
+  const uint64_t words = (worksize + 31) / 32;
+  DevBuf q, qc;
+  COF_CUDA(h, q.ensure(words * 64 * 4));
+  COF_CUDA(h, qc.ensure(4));
+  COF_CUDA(h, cudaMemsetAsync(qc.p, 0, 4, h->stream));
+  launch_finder(h->scratch.view(), 0, words, fp, q.as<uint32_t>(), qc.as<uint32_t>(), h->stream);
+  COF_CUDA(h, cudaGetLastError());
+  uint32_t cnt = 0;
+  COF_CUDA(h, cudaMemcpyAsync(&cnt, qc.p, 4, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<uint32_t> e(cnt);
+  if (cnt) COF_CUDA(h, cudaMemcpy(e.data(), q.p, (size_t)cnt * 4, cudaMemcpyDeviceToHost));
+  std::sort(e.begin(), e.end());
+  uint32_t out = 0;
+  for (size_t i = 0; i < e.size();) {
+    const uint32_t pos = e[i] >> 1;
+    bool f = false, r = false;
+    while (i < e.size() && (e[i] >> 1) == pos) {
+      if (e[i] & 1) r = true;
+      else f = true;
+      ++i;
+    }
+    if (pos >= worksize) continue;
+    loci[out] = pos;
+    flag[out] = (f && r) ? 0 : (f ? 1 : 2);
+    ++out;
+  }
+  *entrycount = out;
+  return COF_OK;
+}
+
+cof_status cof_comparer_chunk(cof_handle* h, const char* chr, uint64_t chrlen, const uint32_t* loci,
+                              const uint8_t* flag, uint32_t locicnt, const char* comp, uint32_t patternlen,
+                              uint16_t threshold, uint32_t* mm_loci, uint16_t* mm_count, char* direction,
+                              uint32_t* entrycount) {
+  if (!h || !chr || (locicnt && (!loci || !flag)) || !comp || !mm_loci || !mm_count || !direction || !entrycount ||
+      patternlen == 0)
+    return COF_ERR_ARG;
+  if (patternlen > (uint32_t)kMaxL) return fail(h, COF_ERR_UNSUPPORTED, "pattern too long");
+  if (chrlen >= (1ull << 31)) return fail(h, COF_ERR_ARG, "chunk must be below 2^31 bytes");
+  h->err.clear();
+  cudaSetDevice(h->device);
+  *entrycount = 0;
+  std::vector<uint32_t> entries;
+  for (uint32_t i = 0; i < locicnt; ++i) {
+    if ((uint64_t)loci[i] + patternlen > chrlen) return fail(h, COF_ERR_ARG, "candidate window beyond the chunk");
+    if (flag[i] == 0 || flag[i] == 1) entries.push_back(loci[i] << 1);
+    if (flag[i] == 0 || flag[i] == 2) entries.push_back((loci[i] << 1) | 1u);
+  }
+  if (entries.empty()) return COF_OK;
+  PackedGenome g;
+  g.n = chrlen;
+  g.hi.assign(plane_words(chrlen), 0);
+  g.lo.assign(plane_words(chrlen), 0);
+  g.ot.assign(plane_words(chrlen), 0);
+  pack_text(chr, chrlen, g.hi.data(), g.lo.data(), g.ot.data(), &g.exc_pos, &g.exc_byte);
+  cof_status st = upload_packed(h, h->scratch, g);
+  if (st) return st;
+  const int nw = patternlen <= 32 ? 1 : 2;
+  std::vector<unsigned char> vm(nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>));
+  const std::string cs(comp, patternlen);
+  if (nw == 1) fill_mask<1>(*(VariantMask<1>*)vm.data(), cs, threshold, 0);
+  else fill_mask<2>(*(VariantMask<2>*)vm.data(), cs, threshold, 0);
+  DevBuf q, qc, vmd, hb, hc;
+  const uint64_t cap = entries.size();
+  COF_CUDA(h, q.ensure(entries.size() * 4));
+  COF_CUDA(h, qc.ensure(4));
+  COF_CUDA(h, vmd.ensure(vm.size()));
+  COF_CUDA(h, hb.ensure(cap * 8));
+  COF_CUDA(h, hc.ensure(8));
+  const uint32_t ne = (uint32_t)entries.size();
+  COF_CUDA(h, cudaMemcpyAsync(q.p, entries.data(), entries.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(qc.p, &ne, 4, cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(vmd.p, vm.data(), vm.size(), cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, cudaMemsetAsync(hc.p, 0, 8, h->stream));
+  launch_comparer(h->scratch.view(), q.as<uint32_t>(), qc.as<uint32_t>(), 0, vmd.p, 1, nw, patternlen,
+                  hb.as<uint64_t>(), hc.as<unsigned long long>(), cap, h->sm_count, h->stream);
+  COF_CUDA(h, cudaGetLastError());
+  uint64_t nh = 0;
+  COF_CUDA(h, cudaMemcpyAsync(&nh, hc.p, 8, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  std::vector<uint64_t> keys(nh);
+  if (nh) COF_CUDA(h, cudaMemcpy(keys.data(), hb.p, nh * 8, cudaMemcpyDeviceToHost));
+  std::sort(keys.begin(), keys.end());
+  for (uint64_t i = 0; i < nh; ++i) {
+    mm_loci[i] = (uint32_t)((keys[i] >> kHitPosShift) & kHitPosMask);
+    mm_count[i] = (uint16_t)(keys[i] & 0x7F);
+    direction[i] = ((keys[i] >> 7) & 1) ? '-' : '+';
+  }
+  *entrycount = (uint32_t)nh;
+  return COF_OK;
+}
+
+uint64_t cof_plane_words(uint64_t n) { return plane_words(n); }
+
+uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, uint32_t* ot, uint64_t* exc_pos,
+                       uint8_t* exc_byte) {
+  std::vector<uint64_t> ep;
+  std::vector<uint8_t> eb;
+  if (hi && lo && ot) {
+    pack_text(seq, n, hi, lo, ot, &ep, &eb);
+  } else {
+    std::vector<uint32_t> a(plane_words(n)), b(plane_words(n)), c(plane_words(n));
+    pack_text(seq, n, a.data(), b.data(), c.data(), &ep, &eb);
+  }
+  if (exc_pos && exc_byte) {
+    std::copy(ep.begin(), ep.end(), exc_pos);
+    std::copy(eb.begin(), eb.end(), exc_byte);
+  }
+  return ep.size();
+}
+
+cof_status cof_set_profiling(cof_handle* h, int enable) {
+  if (!h) return COF_ERR_ARG;
+  h->profiling = enable != 0;
+  return COF_OK;
+}
+
+cof_status cof_kernel_stats(const cof_handle* h, const char* name, uint64_t* launches, double* total_ms,
+                            double* units) {
+  if (!h || !name) return COF_ERR_ARG;
+  auto it = h->stats.find(name);
+  KernelStat s = it == h->stats.end() ? KernelStat() : it->second;
+  if (launches) *launches = s.launches;
+  if (total_ms) *total_ms = s.ms;
+  if (units) *units = s.units;
+  return COF_OK;
+}
+
+cof_status cof_reset_stats(cof_handle* h) {
+  if (!h) return COF_ERR_ARG;
+  h->stats.clear();
+  return COF_OK;
+}
+
+cof_status cof_synchronize(cof_handle* h) {
+  if (!h) return COF_ERR_ARG;
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return COF_OK;
+}
+
+}  // extern "C"

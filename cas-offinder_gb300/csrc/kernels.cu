@@ -1,0 +1,387 @@
+// GB300 kernels of the Cas-OFFinder search path.
+//
+//   finder_kernel      replaces finder/finder_cpu (cas-offinder.cl:6-72,
+//                      :157-213): PAM scan of 32 start positions per thread,
+//                      bit-parallel over the planes, warp-aggregated append of
+//                      strand-oriented candidates.
+//   comparer_kernel    replaces comparer/comparer_cpu (cas-offinder.cl:73-155,
+//                      :214-286): a tile of oriented candidate windows in
+//                      shared memory against all compare variants of the
+//                      pattern at once (one variant per thread, held in
+//                      registers), mismatches counted by popcount.
+//   row_len_kernel /   replace compareAll's host-side row formatting
+//   write_rows_kernel  (cas-offinder.cpp:394-455): rows are written on the GPU
+//                      from per-(variant, bulge, strand) row shapes.
+//
+// Mismatch rule (cas-offinder.cl:30-43) in plane form: for window bits
+// (h, l, o) and a pattern byte with class masks (T, C, A, G, O),
+//   mismatch = o ? O : (h ? (l ? G : A) : (l ? C : T)),
+// evaluated for 32 positions per 32-bit word.  A '-' strand candidate is the
+// reverse complement of the window (bit-reverse, flip hi) tested against the
+// forward compare string; the IUPAC rule is complement-symmetric, so this
+// counts the same mismatches as the reference's test of the reverse-complement
+// compare string against the forward genome.
+#include "kernels.cuh"
+
+namespace cof {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+
+__device__ __forceinline__ uint32_t mux(uint32_t s, uint32_t a, uint32_t b) { return (s & a) | (~s & b); }
+
+__device__ __forceinline__ uint32_t mismatch_word(uint32_t h, uint32_t l, uint32_t o, uint32_t mt, uint32_t mc,
+                                                  uint32_t ma, uint32_t mg, uint32_t mo) {
+  return mux(o, mo, mux(h, mux(l, mg, ma), mux(l, mc, mt)));
+}
+
+// 32 consecutive bits starting at bit k (0 <= k < 64) of the 96-bit value w0|w1|w2.
+__device__ __forceinline__ uint32_t bits_at(uint32_t w0, uint32_t w1, uint32_t w2, unsigned k) {
+  const unsigned r = k & 31;
+  return (k & 32) ? __funnelshift_r(w1, w2, r) : __funnelshift_r(w0, w1, r);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- finder
+__global__ void __launch_bounds__(256) finder_kernel(const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo,
+                                                     const uint32_t* __restrict__ ot, uint64_t w_begin, uint64_t w_end,
+                                                     const __grid_constant__ FinderPattern pat,
+                                                     uint32_t* __restrict__ queue, uint32_t* __restrict__ qcount) {
+  const unsigned lane = threadIdx.x & 31;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t wb = w_begin + (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wb < w_end; wb += stride) {
+    const uint64_t w = wb + lane;
+    uint32_t fwd = 0, rev = 0;
+    if (w < w_end) {
+      const uint32_t h0 = hi[w], h1 = hi[w + 1], h2 = hi[w + 2];
+      const uint32_t l0 = lo[w], l1 = lo[w + 1], l2 = lo[w + 2];
+      const uint32_t o0 = ot[w], o1 = ot[w + 1], o2 = ot[w + 2];
+      uint32_t badf = 0, badr = 0;
+      for (uint32_t j = 0; j < pat.nf; ++j) {
+        const unsigned k = pat.fk[j];
+        const uint32_t m = pat.fm[j];
+        badf |= mismatch_word(bits_at(h0, h1, h2, k), bits_at(l0, l1, l2, k), bits_at(o0, o1, o2, k), 0u - (m & 1),
+                              0u - ((m >> 1) & 1), 0u - ((m >> 2) & 1), 0u - ((m >> 3) & 1), 0u - ((m >> 4) & 1));
+      }
+      for (uint32_t j = 0; j < pat.nr; ++j) {
+        const unsigned k = pat.rk[j];
+        const uint32_t m = pat.rm[j];
+        badr |= mismatch_word(bits_at(h0, h1, h2, k), bits_at(l0, l1, l2, k), bits_at(o0, o1, o2, k), 0u - (m & 1),
+                              0u - ((m >> 1) & 1), 0u - ((m >> 2) & 1), 0u - ((m >> 3) & 1), 0u - ((m >> 4) & 1));
+      }
+      fwd = ~badf;
+      rev = ~badr;
+      if (fwd | rev) {
+        // Drop windows holding a record separator (cas-offinder.cl:64-67).
+        const uint32_t s0 = o0 & l0 & ~h0, s1 = o1 & l1 & ~h1, s2 = o2 & l2 & ~h2;
+        if (s0 | s1 | s2) {
+          uint32_t near = 0;
+          for (unsigned k = 0; k < pat.L; ++k) near |= bits_at(s0, s1, s2, k);
+          fwd &= ~near;
+          rev &= ~near;
+        }
+      }
+    }
+    const uint32_t cnt = __popc(fwd) + __popc(rev);
+    uint32_t incl = cnt;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(kFull, incl, d);
+      if (lane >= (unsigned)d) incl += t;
+    }
+    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    uint32_t base = 0;
+    if (lane == 31 && total) base = atomicAdd(qcount, total);
+    base = __shfl_sync(kFull, base, 31);
+    uint32_t at = base + incl - cnt;
+    const uint32_t rel = (uint32_t)((w - w_begin) << 5);
+    while (fwd) {
+      const unsigned b = __ffs(fwd) - 1;
+      fwd &= fwd - 1;
+      queue[at++] = (rel + b) << 1;
+    }
+    while (rev) {
+      const unsigned b = __ffs(rev) - 1;
+      rev &= rev - 1;
+      queue[at++] = ((rel + b) << 1) | 1u;
+    }
+  }
+}
+
+void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const FinderPattern& pat, uint32_t* queue,
+                   uint32_t* qcount, cudaStream_t stream) {
+  const uint64_t words = w_end - w_begin;
+  const unsigned threads = 256;
+  uint64_t blocks = (words + threads - 1) / threads;
+  if (blocks > 65535ull * 8) blocks = 65535ull * 8;
+  if (blocks == 0) return;
+  finder_kernel<<<(unsigned)blocks, threads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, pat, queue, qcount);
+}
+
+// ---------------------------------------------------------------- comparer
+template <int NW>
+struct CandWindow {
+  uint32_t h[NW], l[NW], o[NW];
+  uint32_t entry;
+};
+
+template <int NW>
+__global__ void __launch_bounds__(256) comparer_kernel(const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo,
+                                                       const uint32_t* __restrict__ ot,
+                                                       const uint32_t* __restrict__ queue,
+                                                       const uint32_t* __restrict__ qcount, uint64_t seg_pos0,
+                                                       const VariantMask<NW>* __restrict__ vars, uint32_t nvar,
+                                                       uint32_t L, uint64_t* __restrict__ hits,
+                                                       unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+  __shared__ CandWindow<NW> tile[256];
+  const uint32_t n = *qcount;
+  const uint32_t ntiles = (n + 255) / 256;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    // Stage one oriented window per thread.
+    const uint32_t idx = t * 256 + threadIdx.x;
+    if (idx < n) {
+      const uint32_t e = queue[idx];
+      const uint64_t pos = seg_pos0 + (e >> 1);
+      const uint64_t w = pos >> 5;
+      const unsigned r = (unsigned)(pos & 31);
+      CandWindow<NW> cw;
+      cw.entry = e;
+      uint32_t hw[NW], lw[NW], ow[NW];
+#pragma unroll
+      for (int i = 0; i < NW; ++i) {
+        hw[i] = __funnelshift_r(hi[w + i], hi[w + i + 1], r);
+        lw[i] = __funnelshift_r(lo[w + i], lo[w + i + 1], r);
+        ow[i] = __funnelshift_r(ot[w + i], ot[w + i + 1], r);
+      }
+      if (e & 1) {
+        // Reverse complement of the L-position window: reverse the bit order,
+        // then complement the bases (flip hi; non-base bytes keep o = 1).
+        if (NW == 1) {
+          const unsigned sh = 32 - L;
+          cw.h[0] = ~(__brev(hw[0]) >> sh) & (0xFFFFFFFFu >> sh);
+          cw.l[0] = __brev(lw[0]) >> sh;
+          cw.o[0] = __brev(ow[0]) >> sh;
+        } else {
+          const unsigned sh = 64 - L;
+          const uint64_t mask = ~0ull >> sh;
+          const uint64_t H = ~(__brevll(((uint64_t)hw[NW - 1] << 32) | hw[0]) >> sh) & mask;
+          const uint64_t Lw = __brevll(((uint64_t)lw[NW - 1] << 32) | lw[0]) >> sh;
+          const uint64_t O = __brevll(((uint64_t)ow[NW - 1] << 32) | ow[0]) >> sh;
+          cw.h[0] = (uint32_t)H;
+          cw.h[NW - 1] = (uint32_t)(H >> 32);
+          cw.l[0] = (uint32_t)Lw;
+          cw.l[NW - 1] = (uint32_t)(Lw >> 32);
+          cw.o[0] = (uint32_t)O;
+          cw.o[NW - 1] = (uint32_t)(O >> 32);
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < NW; ++i) {
+          cw.h[i] = hw[i];
+          cw.l[i] = lw[i];
+          cw.o[i] = ow[i];
+        }
+      }
+      tile[threadIdx.x] = cw;
+    }
+    __syncthreads();
+    const uint32_t m = min(256u, n - t * 256);
+    for (uint32_t v = threadIdx.x; v < nvar; v += blockDim.x) {
+      const VariantMask<NW> vm = vars[v];
+      for (uint32_t c = 0; c < m; ++c) {
+        const CandWindow<NW>& cw = tile[c];
+        uint32_t mm = 0;
+#pragma unroll
+        for (int i = 0; i < NW; ++i)
+          mm += __popc(mismatch_word(cw.h[i], cw.l[i], cw.o[i], vm.t[i], vm.c[i], vm.a[i], vm.g[i], vm.o[i]));
+        if (mm <= vm.thr) {
+          const unsigned long long at = atomicAdd(hit_count, 1ull);
+          if (at < hit_cap) hits[at] = make_hit(vm.gid, seg_pos0 + (cw.entry >> 1), cw.entry & 1, mm);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
+                     const void* vars, uint32_t nvar, int nw, uint32_t L, uint64_t* hits,
+                     unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
+  if (nvar == 0) return;
+  const unsigned blocks = (unsigned)sm_count * 8;
+  if (nw == 1)
+    comparer_kernel<1><<<blocks, 256, 0, stream>>>(g.hi, g.lo, g.ot, queue, qcount, seg_pos0,
+                                                   (const VariantMask<1>*)vars, nvar, L, hits, hit_count, hit_cap);
+  else
+    comparer_kernel<2><<<blocks, 256, 0, stream>>>(g.hi, g.lo, g.ot, queue, qcount, seg_pos0,
+                                                   (const VariantMask<2>*)vars, nvar, L, hits, hit_count, hit_cap);
+}
+
+// ---------------------------------------------------------------- formatting
+namespace {
+
+__device__ bool dev_mismatch(unsigned char p, unsigned char g) {
+  unsigned gb;
+  switch (g) {
+    case 'T': gb = 0; break;
+    case 'C': gb = 1; break;
+    case 'A': gb = 2; break;
+    case 'G': gb = 3; break;
+    default: gb = 4; break;
+  }
+  return (class_bits_of(p) >> gb) & 1u;
+}
+
+__device__ unsigned char dev_complement(unsigned char c) {
+  switch (c) {
+    case 'A': return 'T';
+    case 'T': return 'A';
+    case 'G': return 'C';
+    case 'C': return 'G';
+    case 'R': return 'Y';
+    case 'Y': return 'R';
+    case 'M': return 'K';
+    case 'K': return 'M';
+    case 'H': return 'D';
+    case 'D': return 'H';
+    case 'B': return 'V';
+    case 'V': return 'B';
+    default: return c;
+  }
+}
+
+__device__ unsigned char genome_byte(const GenomeView& g, uint64_t p) {
+  const uint64_t w = p >> 5;
+  const unsigned b = (unsigned)(p & 31);
+  const unsigned h = (g.hi[w] >> b) & 1, l = (g.lo[w] >> b) & 1, o = (g.ot[w] >> b) & 1;
+  if (!o) return (unsigned char)"TCAG"[h * 2 + l];
+  if (!h) return l ? ';' : 'N';
+  uint64_t a = 0, z = g.n_exc;  // first exception position >= p
+  while (a < z) {
+    const uint64_t mid = (a + z) >> 1;
+    if (g.exc_pos[mid] < p) a = mid + 1;
+    else z = mid;
+  }
+  return (a < g.n_exc && g.exc_pos[a] == p) ? g.exc_byte[a] : (unsigned char)'N';
+}
+
+__device__ uint32_t record_of(const GenomeView& g, uint64_t p) {
+  uint32_t a = 0, z = g.n_rec;  // first start > p
+  while (a < z) {
+    const uint32_t mid = (a + z) >> 1;
+    if (g.rec_start[mid] <= p) a = mid + 1;
+    else z = mid;
+  }
+  return a ? a - 1 : 0;
+}
+
+__device__ __forceinline__ uint32_t decimal_len(uint64_t v) {
+  uint32_t d = 1;
+  while (v >= 10) {
+    v /= 10;
+    ++d;
+  }
+  return d;
+}
+
+__device__ __forceinline__ char* put_decimal(char* o, uint64_t v) {
+  char tmp[20];
+  int k = 0;
+  do {
+    tmp[k++] = (char)('0' + v % 10);
+    v /= 10;
+  } while (v);
+  while (k) *o++ = tmp[--k];
+  return o;
+}
+
+struct HitView {
+  uint32_t gid, strand, mm;
+  uint64_t pos;
+};
+__device__ __forceinline__ HitView decode(uint64_t key) {
+  HitView h;
+  h.gid = (uint32_t)(key >> 44);
+  h.pos = (key >> kHitPosShift) & kHitPosMask;
+  h.strand = (uint32_t)((key >> 7) & 1);
+  h.mm = (uint32_t)(key & 0x7F);
+  return h;
+}
+
+}  // namespace
+
+__global__ void row_len_kernel(GenomeView g, FormatTables ft, const uint64_t* __restrict__ hits, uint64_t n_hits,
+                               uint64_t* __restrict__ row_bytes, uint32_t* __restrict__ row_count) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_hits) return;
+  const HitView h = decode(hits[i]);
+  const VariantFmt vf = ft.var[h.gid];
+  const uint32_t rec = record_of(g, h.pos);
+  const uint64_t rel = h.pos - g.rec_start[rec];
+  const uint32_t fixed_sep = 5;  // tabs around chromosome, location, direction, mismatches
+  uint64_t bytes = 0;
+  for (uint32_t s = vf.shape_begin[h.strand]; s < vf.shape_end[h.strand]; ++s) {
+    const ShapeFmt sh = ft.shape[s];
+    bytes += sh.head_len + sh.dna_len + g.rec_name_len[rec] + decimal_len(rel + (uint64_t)sh.offset) + 1 +
+             decimal_len(h.mm) + sh.tail_len + fixed_sep;
+  }
+  row_bytes[i] = bytes;
+  row_count[i] = vf.shape_end[h.strand] - vf.shape_begin[h.strand];
+}
+
+__global__ void write_rows_kernel(GenomeView g, FormatTables ft, const uint64_t* __restrict__ hits, uint64_t n_hits,
+                                  const uint64_t* __restrict__ offsets, char* __restrict__ out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_hits) return;
+  const HitView h = decode(hits[i]);
+  const VariantFmt vf = ft.var[h.gid];
+  const uint32_t L = vf.L;
+  const char* comp = ft.pool + vf.comp_off;
+  // Oriented window with mismatches lower-cased (indicate_mismatches,
+  // cas-offinder.cpp:299-317: byte += 32).
+  unsigned char win[kMaxL];
+  for (uint32_t k = 0; k < L; ++k) {
+    unsigned char c = h.strand ? dev_complement(genome_byte(g, h.pos + (L - 1 - k))) : genome_byte(g, h.pos + k);
+    if (dev_mismatch((unsigned char)comp[k], c)) c = (unsigned char)(c + 32);
+    win[k] = c;
+  }
+  const uint32_t rec = record_of(g, h.pos);
+  const uint64_t rel = h.pos - g.rec_start[rec];
+  const char* name = g.rec_names + g.rec_name_off[rec];
+  const uint32_t name_len = g.rec_name_len[rec];
+  char* o = out + offsets[i];
+  for (uint32_t s = vf.shape_begin[h.strand]; s < vf.shape_end[h.strand]; ++s) {
+    const ShapeFmt sh = ft.shape[s];
+    for (uint32_t k = 0; k < sh.head_len; ++k) *o++ = ft.pool[sh.head_off + k];
+    for (uint32_t k = 0; k < sh.dna_len; ++k) {
+      const unsigned char c = (unsigned char)ft.pool[sh.dna_off + k];
+      *o++ = (char)(c >= 0x80 ? win[c - 0x80] : c);
+    }
+    *o++ = '\t';
+    for (uint32_t k = 0; k < name_len; ++k) *o++ = name[k];
+    *o++ = '\t';
+    o = put_decimal(o, rel + (uint64_t)sh.offset);
+    *o++ = '\t';
+    *o++ = sh.dir;
+    *o++ = '\t';
+    o = put_decimal(o, h.mm);
+    *o++ = '\t';
+    for (uint32_t k = 0; k < sh.tail_len; ++k) *o++ = ft.pool[sh.tail_off + k];
+  }
+}
+
+void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
+                        uint64_t* row_bytes, uint32_t* row_count, cudaStream_t stream) {
+  if (!n_hits) return;
+  row_len_kernel<<<(unsigned)((n_hits + 255) / 256), 256, 0, stream>>>(g, ft, hits, n_hits, row_bytes, row_count);
+}
+
+void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
+                       const uint64_t* offsets, char* out, cudaStream_t stream) {
+  if (!n_hits) return;
+  write_rows_kernel<<<(unsigned)((n_hits + 127) / 128), 128, 0, stream>>>(g, ft, hits, n_hits, offsets, out);
+}
+
+}  // namespace cof

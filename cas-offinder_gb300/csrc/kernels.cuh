@@ -1,0 +1,115 @@
+// Device data layouts and kernel launchers of the GB300 search path.
+//
+// Genome: three bit planes (hi, lo, ot), one bit per position, 32 positions
+// per uint32 word (layout and code in cof_internal.h).  The planes are read
+// in place by every kernel; nothing else of the genome is resident.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace cof {
+
+constexpr int kMaxL = 64;  // longest pattern: two 32-bit words per window
+
+// Per-position mismatch classes of one pattern/compare byte: bit 0 mismatches
+// a genome T, bit 1 C, bit 2 A, bit 3 G, bit 4 any non-base byte.
+__host__ __device__ inline uint32_t class_bits_of(unsigned char p) {
+  switch (p) {
+    case 'A': return 0x1Bu;  // T C G other
+    case 'C': return 0x1Du;  // T A G other
+    case 'G': return 0x17u;  // T C A other
+    case 'T': return 0x1Eu;  // C A G other
+    case 'R': return 0x03u;  // A/G: T C
+    case 'Y': return 0x0Cu;  // C/T: A G
+    case 'K': return 0x06u;  // G/T: C A
+    case 'M': return 0x09u;  // A/C: T G
+    case 'W': return 0x0Au;  // A/T: C G
+    case 'S': return 0x05u;  // C/G: T A
+    case 'H': return 0x08u;  // A/C/T: G
+    case 'B': return 0x04u;  // C/G/T: A
+    case 'V': return 0x01u;  // A/C/G: T
+    case 'D': return 0x02u;  // A/G/T: C
+    default: return 0u;      // N and every other byte never mismatch
+  }
+}
+
+// PAM scan pattern: the positions of the pattern (forward) and of its reverse
+// complement that can mismatch, with their class bits.
+struct FinderPattern {
+  uint32_t L;
+  uint32_t nf, nr;
+  uint8_t fk[kMaxL], fm[kMaxL];
+  uint8_t rk[kMaxL], rm[kMaxL];
+};
+
+// One compare variant as NW-word class masks (bit k = window position k).
+template <int NW>
+struct VariantMask {
+  uint32_t t[NW], c[NW], a[NW], g[NW], o[NW];
+  uint32_t thr;  // mismatch limit
+  uint32_t gid;  // global variant index (row order rank)
+};
+
+// Hit key, sortable into output order:
+//   [63:44] global variant index  [43:8] genome position
+//   [7] strand (1 = '-')          [6:0] mismatches
+constexpr int kHitPosShift = 8;
+constexpr uint64_t kHitPosMask = (1ull << 36) - 1;
+__host__ __device__ inline uint64_t make_hit(uint32_t gid, uint64_t pos, uint32_t strand, uint32_t mm) {
+  return ((uint64_t)gid << 44) | (pos << kHitPosShift) | ((uint64_t)strand << 7) | (uint64_t)mm;
+}
+
+// Formatting tables (all offsets into one byte pool).
+struct VariantFmt {
+  uint32_t comp_off;            // compare string (L bytes)
+  uint32_t L;
+  uint32_t shape_begin[2], shape_end[2];  // rows per strand
+};
+struct ShapeFmt {
+  uint32_t head_off, head_len, dna_off, dna_len, tail_off, tail_len;
+  int64_t offset;
+  char dir;
+};
+
+struct GenomeView {
+  const uint32_t* hi;
+  const uint32_t* lo;
+  const uint32_t* ot;
+  const uint64_t* exc_pos;
+  const uint8_t* exc_byte;
+  uint64_t n_exc;
+  uint64_t n;
+  const uint64_t* rec_start;
+  const uint32_t* rec_name_off;
+  const uint32_t* rec_name_len;
+  const char* rec_names;
+  uint32_t n_rec;
+};
+
+struct FormatTables {
+  const VariantFmt* var;
+  const ShapeFmt* shape;
+  const char* pool;
+};
+
+// ---- launchers (kernels.cu).  All run on `stream`, none synchronizes.
+// Scans start positions [32*w_begin, 32*w_end) and appends oriented candidate
+// entries (position - 32*w_begin) << 1 | strand to `queue`.
+void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const FinderPattern& pat, uint32_t* queue,
+                   uint32_t* qcount, cudaStream_t stream);
+// Tests every entry of `queue` (count read on the device) against `nvar`
+// variants; appends hit keys to `hits` (count in *hit_count; entries past
+// hit_cap are counted, not written).
+void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
+                     const void* vars, uint32_t nvar, int nw, uint32_t L, uint64_t* hits,
+                     unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
+// Row byte counts per sorted hit (and rows per hit).
+void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
+                        uint64_t* row_bytes, uint32_t* row_count, cudaStream_t stream);
+// Writes the rows of every hit at `offsets` (exclusive scan of row_bytes).
+void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
+                       const uint64_t* offsets, char* out, cudaStream_t stream);
+
+}  // namespace cof

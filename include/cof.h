@@ -1,0 +1,161 @@
+/*
+ * cof.h - C ABI of the GB300 Cas-OFFinder search engine (libcasoff.so).
+ *
+ * The reference (Cas-OFFinder 3.0.0) has no plugin API: its search path sits
+ * behind the C++ class Cas_OFFinder (cas-offinder.h:24-107) and the OpenCL
+ * kernels finder/comparer (cas-offinder.cl:6-155).  This header is the C ABI
+ * that replaces that OpenCL device path.  Every entry point below names the
+ * reference interface it stands in for.  All calls return a cof_status
+ * (COF_OK = 0) instead of exit(1) (oclfunctions.cpp:5-296), take plain
+ * pointers and sizes, and never call exit().  A handle is used by one host
+ * thread at a time, like the reference's in-order queues
+ * (cas-offinder.cpp:123).
+ *
+ * Typical use (what the cas-offinder CLI does, mirroring main.cpp:72-157):
+ *   cof_open(0, &h);
+ *   cof_read_input(h, text, len);                 // readInputFile
+ *   cof_genome_load_file(h, path);                // read_fasta / read_twobit
+ *   cof_search(h, &rows, &nrows_bytes);           // loadNextChunk..compareAll
+ *   fwrite(rows, 1, nrows_bytes, out);
+ *   cof_close(h);
+ */
+#ifndef COF_H
+#define COF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int cof_status;
+enum {
+  COF_OK = 0,
+  COF_ERR_CUDA = 1,        /* a CUDA runtime call failed (message in cof_last_error) */
+  COF_ERR_ARG = 2,         /* a bad argument (null pointer, size out of range) */
+  COF_ERR_NOMEM = 3,       /* device or host allocation failed */
+  COF_ERR_INPUT = 4,       /* malformed input file; message = the reference's text */
+  COF_ERR_IO = 5,          /* a file could not be read */
+  COF_ERR_STATE = 6,       /* call out of order (no input or no genome loaded) */
+  COF_ERR_UNSUPPORTED = 7, /* pattern longer than COF_MAX_PATTERN */
+  COF_ERR_NOT_GENOME = 8,  /* file is neither FASTA nor 2BIT ("Skipping non-acceptable file") */
+  COF_ERR_DEVICE = 9       /* a kernel reported an internal inconsistency */
+};
+
+/* Longest pattern (PAM + spacer + DNA-bulge padding) the kernels accept. */
+#define COF_MAX_PATTERN 64
+
+typedef struct cof_handle cof_handle;
+
+/* ---- engine lifetime: Cas_OFFinder::Cas_OFFinder / ~Cas_OFFinder
+ *      (cas-offinder.cpp:131-173).  `device` is the CUDA ordinal (the CLI's
+ *      G0 selects device 0). */
+cof_status cof_open(int device, cof_handle** out);
+void cof_close(cof_handle* h);
+/* Text of the last error on this handle ("" if none).  Valid until the next call. */
+const char* cof_last_error(const cof_handle* h);
+/* Same for errors of cof_open itself (no handle exists yet). */
+const char* cof_open_error(void);
+
+/* ---- input file: Cas_OFFinder::readInputFile / parseInput
+ *      (cas-offinder.cpp:590-751).  `text` holds the whole input file.  On a
+ *      malformed file the status is COF_ERR_INPUT and cof_last_error() holds
+ *      the reference's message ("Malformed input file." ...). */
+cof_status cof_read_input(cof_handle* h, const char* text, size_t len);
+/* Line 1 of the input file: genome file or directory (Cas_OFFinder::m_chrdir). */
+const char* cof_genome_path(const cof_handle* h);
+/* Pattern length L (m_patternlen), number of compare variants (m_compares.size()). */
+cof_status cof_input_info(const cof_handle* h, uint32_t* pattern_len, uint32_t* n_variants,
+                          uint32_t* n_bulge_records);
+
+/* ---- genome: read_fasta (read_fasta.cpp:11-58) / read_twobit
+ *      (read_twobit.cpp:44-131) + Cas_OFFinder::setChrData
+ *      (cas-offinder.cpp:175-208).  The genome is packed to 2-bit planes plus
+ *      an exception bitmap and stays resident in HBM until replaced.
+ *      FASTA is tried first, then 2BIT, as run_cas_offinder does
+ *      (main.cpp:49-53); COF_ERR_NOT_GENOME if neither parses. */
+cof_status cof_genome_load_file(cof_handle* h, const char* path);
+/* The reference's in-memory genome: records joined by ';' (`seq`, n bytes),
+ * record names and record start offsets (Cas_OFFinder::m_chrdata, m_chrnames,
+ * m_chrpos; cas-offinder.h:86-89). */
+cof_status cof_genome_load_text(cof_handle* h, const char* seq, uint64_t n, const char* const* names,
+                                const uint64_t* starts, uint32_t n_records);
+/* Pre-packed genome (what cof_pack_text produces, e.g. from pinned memory).
+ * Plane word w bit b describes position 32*w+b; each plane has
+ * cof_plane_words(n) words.  `exc_pos`/`exc_byte` list, in ascending position
+ * order, the bytes that are not A/C/G/T/N/';' (n_exc entries). */
+cof_status cof_genome_load_planes(cof_handle* h, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
+                                  uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
+                                  const char* const* names, const uint64_t* starts, uint32_t n_records);
+/* Genome length in bytes (separators included) and record count. */
+cof_status cof_genome_info(const cof_handle* h, uint64_t* n, uint32_t* n_records);
+
+/* ---- search: loadNextChunk + findPattern + compareAll + releaseLociinfo
+ *      (cas-offinder.cpp:210-469, 502-519).  Searches the resident genome
+ *      with the current input and formats every output row (the TSV body, no
+ *      header lines) on the GPU.  Row order: compare variants in the
+ *      reference's std::map key order, hits of a variant by position with '+'
+ *      before '-', bulge records of a hit in insertion order - the order the
+ *      reference emits for a single chunk with work-items run in order.
+ *      `*rows` points into a buffer owned by the handle, valid until the next
+ *      search or cof_close. */
+cof_status cof_search(cof_handle* h, const char** rows, size_t* rows_len);
+/* Hit count of the last search (hits = (variant, position, strand) triples
+ * with mismatches <= threshold, before expansion into bulge rows). */
+cof_status cof_last_hit_count(const cof_handle* h, uint64_t* n_hits, uint64_t* n_rows);
+/* Count rows into the summary table during searches (off by default; the CLI
+ * turns it on for --summary, main.cpp:90-97). */
+cof_status cof_set_summary(cof_handle* h, int enable);
+/* Summary table of all searches since cof_read_input, as the reference writes
+ * it with --summary (Cas_OFFinder::writeSummaryTable, cas-offinder.cpp:471-500). */
+cof_status cof_summary_text(cof_handle* h, const char** text, size_t* len);
+
+/* ---- header lines: Cas_OFFinder::writeHeaders (cas-offinder.cpp:319-328). */
+const char* cof_header_text(void);
+
+/* ---- kernel-level entry points with the OpenCL kernels' argument contracts.
+ * cof_finder_chunk replaces finder/finder_cpu (cas-offinder.cl:6-72,
+ * :157-213): `chr` is the chunk (worksize + L - 1 bytes), `pat` the pattern
+ * and its reverse complement (2L bytes, as readInputFile builds it,
+ * cas-offinder.cpp:708-714).  Outputs candidate start offsets and flags
+ * (0 both strands, 1 forward only, 2 reverse only) in ascending offset order;
+ * *entrycount receives the count (capacity: worksize entries). */
+cof_status cof_finder_chunk(cof_handle* h, const char* chr, uint64_t worksize, const char* pat,
+                            uint32_t patternlen, uint32_t* loci, uint8_t* flag, uint32_t* entrycount);
+/* cof_comparer_chunk replaces comparer/comparer_cpu (cas-offinder.cl:73-155,
+ * :214-286): one compare string `comp` (L bytes; its reverse complement is
+ * formed internally) with `threshold`, over `locicnt` candidates.  Hits are
+ * written ordered by candidate then '+' before '-' (capacity 2*locicnt). */
+cof_status cof_comparer_chunk(cof_handle* h, const char* chr, uint64_t chrlen, const uint32_t* loci,
+                              const uint8_t* flag, uint32_t locicnt, const char* comp, uint32_t patternlen,
+                              uint16_t threshold, uint32_t* mm_loci, uint16_t* mm_count, char* direction,
+                              uint32_t* entrycount);
+
+/* ---- packing helpers (host side). */
+/* Words per plane for a genome of n bytes (includes the tail padding). */
+uint64_t cof_plane_words(uint64_t n);
+/* Pack the reference's genome string into planes; returns the number of
+ * exception bytes, written to exc_pos/exc_byte when those are non-null
+ * (call once with nulls to size them). */
+uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, uint32_t* ot, uint64_t* exc_pos,
+                       uint8_t* exc_byte);
+
+/* ---- instrumentation: per-kernel CUDA-event timing on the engine's stream. */
+cof_status cof_set_profiling(cof_handle* h, int enable);
+/* Totals since profiling was enabled for kernel `name` ("finder", "comparer",
+ * "format"): launches, summed device milliseconds and algorithmic units
+ * (finder: genome positions scanned; comparer: base comparisons, i.e. the
+ * non-N positions of each compare variant times the strand-oriented
+ * candidates it was tested against, counted without early exit). */
+cof_status cof_kernel_stats(const cof_handle* h, const char* name, uint64_t* launches, double* total_ms,
+                            double* units);
+cof_status cof_reset_stats(cof_handle* h);
+/* Wait for all work of the handle's stream. */
+cof_status cof_synchronize(cof_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COF_H */

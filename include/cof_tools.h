@@ -1,0 +1,31 @@
+/*
+ * cof_tools.h - helpers of libcasoff.so that are not part of the reference's
+ * interface: a deterministic synthetic genome generator used to make
+ * benchmark and test genomes of a stated shape without any download.
+ */
+#ifndef COF_TOOLS_H
+#define COF_TOOLS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Writes `len` bytes of one synthetic record (A, C, G, T, N) to `out`.
+ * Bases are drawn i.i.d. with P(G) = P(C) = gc_w / 2 and P(A) = P(T) =
+ * (1 - gc_w) / 2, where gc_w = gc + gc_drift * U(-1, 1), redrawn for every
+ * window of `drift_window` bases (gc_drift = 0: one GC fraction throughout).
+ * Then round(n_frac * len / mean_run) runs of N are placed at uniform starts
+ * with lengths uniform in [n_run_min, n_run_max] (runs may overlap).  The
+ * output depends only on (seed, record, the parameters): it is the same on
+ * every platform and thread count.  Returns the number of N bytes written. */
+uint64_t cofx_synth_record(uint64_t seed, uint32_t record, uint64_t len, double gc, double gc_drift,
+                           uint32_t drift_window, double n_frac, uint32_t n_run_min, uint32_t n_run_max,
+                           char* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COF_TOOLS_H */
