@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""Benchmark: guide-Gbp/s of the plain Cas-OFFinder search on one GB300.
+
+Workload (the full-scale plain configuration): a synthetic 3.1 Gbp genome of 24
+records (lengths log-uniform in 47-249 Mbp, rescaled to 3.1 Gbp), 41% GC with
+a +-10% GC drift per 100 kbp window and 5% N in runs of 1-100 kbp; pattern
+NNNNNNNNNNNNNNNNNNNNNRG with DNA bulge 2 and RNA bulge 1; 4 random 20-nt
+guides + NNN with at most 5 mismatches.  All inputs are seeded.
+
+One step = one full search of the genome (PAM scan, compare, sort, row
+formatting on the GPU, rows copied to host memory).
+  value : steps with the packed genome already resident in HBM.
+  e2e   : steps through the C ABI from host buffers: each step copies the
+          genome planes from pinned host memory (cof_genome_load_planes),
+          searches, and copies the rows back (cof_search).
+The genome planes (1.16 GB) are larger than L2, so no flush is needed between
+steps.  Timing: CUDA events on the engine's stream (cof_timer_start/stop),
+after warm-up steps, max over ranks.  Under torchrun each rank runs an
+independent replica on its own GPU (weak scaling; the search has no
+cross-GPU exchange).
+
+--impl reference times the reference algorithm on the host CPU cores instead:
+the reference binary built from its sources when it runs here, else the
+oracle's CPU restatement, on a bounded prefix of the same genome.
+"""
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+PATTERN = "N" * 21 + "RG"
+DNA, RNA, MM, N_GUIDES = 2, 1, 5, 4
+GENOME_SEED = 2
+GUIDE_SEED = 3
+METRIC = "guide-Gbp/s (bit-exact hits) plain vs batched-served; p50/p99 request latency"
+
+
+def pkg():
+    from pkgload import pkg as _p
+    return _p()
+
+
+def make_guides(seed=GUIDE_SEED, n=N_GUIDES):
+    import random
+    rng = random.Random(seed)
+    return ["".join(rng.choice("ACGT") for _ in range(20)) + "NNN" for _ in range(n)]
+
+
+def input_text(genome_path, guides):
+    return f"{genome_path}\n{PATTERN} {DNA} {RNA}\n" + "".join(f"{g} {MM}\n" for g in guides)
+
+
+def build_genome(P, total_bp, n_records=24, seed=GENOME_SEED):
+    """The synthetic genome as the reference's string (records joined by ';')."""
+    import ctypes
+    lens = P.record_lengths(seed, n_records, int(total_bp))
+    n = sum(lens) + n_records - 1
+    buf = bytearray(n)
+    base = ctypes.addressof((ctypes.c_char * n).from_buffer(buf))
+    starts, pos = [], 0
+    for r, ln in enumerate(lens):
+        if r:
+            buf[pos] = ord(";")
+            pos += 1
+        starts.append(pos)
+        P.lib().cofx_synth_record(seed, r, ln, 0.41, 0.10, 100000, 0.05, 1000, 100000, base + pos)
+        pos += ln
+    names = [f"chr{r + 1}" for r in range(n_records)]
+    return buf, names, starts, lens
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    def __init__(self, index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.index = index
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        try:
+            rows = [l.split(", ") for l in open(self.path).read().strip().splitlines() if l.strip()]
+        except OSError:
+            rows = []
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and "Active" in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_sample_run(binary, genome_buf, names, starts, sample_bp, guides, threads, workdir):
+    """Runs the CPU implementation on the first `sample_bp` positions of the
+    genome (as FASTA); returns (seconds, rows)."""
+    fa = os.path.join(workdir, "sample.fa")
+    if not os.path.exists(fa):
+        end = min(len(genome_buf), sample_bp)
+        P = pkg()
+        recs, nm = [], []
+        for i, s in enumerate(starts):
+            e = (starts[i + 1] - 1) if i + 1 < len(starts) else len(genome_buf)
+            if s >= end:
+                break
+            recs.append(bytes(genome_buf[s:min(e, end)]))
+            nm.append(names[i])
+        P.write_fasta(fa, nm, recs)
+    inp = os.path.join(workdir, "sample_input.txt")
+    with open(inp, "w") as f:
+        f.write(input_text(fa, guides))
+    out = os.path.join(workdir, "sample_out.tsv")
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    t0 = time.perf_counter()
+    r = subprocess.run([binary, inp, "C", out], env=env, capture_output=True)
+    dt = time.perf_counter() - t0
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr.decode()[-2000:])
+    rows = sum(1 for l in open(out, "rb") if not l.startswith(b"#"))
+    return dt, rows
+
+
+def cpu_binary():
+    """(path, kind): the reference built from its sources if it runs here, else the oracle port."""
+    import build_oracle
+    port, _ = build_oracle.build(with_reference=False)
+    ref_path = os.path.join(ROOT, "oracle", "_ref", "cas-offinder-ref")  # prebuilt by build(), if at all
+    for cand, kind in ((ref_path, "reference"), (port, "port")):
+        if cand and os.path.exists(cand):
+            try:
+                r = subprocess.run([cand], capture_output=True, timeout=30)
+                if r.returncode == 0:
+                    return cand, kind
+            except OSError:
+                continue
+    raise RuntimeError("no CPU implementation available")
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    P = pkg()
+    P.build()
+    binary, kind = cpu_binary()
+    guides = make_guides()
+    sample_bp = int(args.sample_mbp * 1e6)
+    buf, names, starts, _ = build_genome(P, max(sample_bp * 1.05, 1e6), n_records=1)
+    threads = os.cpu_count() or 1
+    times = []
+    with tempfile.TemporaryDirectory() as tmp:
+        for i in range(args.warmup + args.steps):
+            dt, rows = cpu_sample_run(binary, buf, names, starts, sample_bp, guides, threads, tmp)
+            if i >= args.warmup:
+                times.append(dt)
+    total = sum(times)
+    gbp = min(len(buf), sample_bp) / 1e9
+    value = N_GUIDES * gbp * len(times) / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "guide-Gbp/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "plain NRG dna2 rna1, 4 guides mm5, genome prefix sample",
+                   "sample_bp": min(len(buf), sample_bp)},
+        "cpu_baseline": {"value": value, "unit": "guide-Gbp/s", "cores": threads, "kind": kind,
+                         "sample": f"first {min(len(buf), sample_bp)} bp of the seeded synthetic genome, "
+                                   f"same pattern and guides, {rows} rows"},
+        "e2e": {"value": value, "unit": "guide-Gbp/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--genome-gbp", type=float, default=3.1)
+    ap.add_argument("--sample-mbp", type=float, default=20.0, help="CPU baseline sample (Mbp)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+
+    import numpy as np
+    import torch
+    P = pkg()
+    P.build()
+    torch.cuda.set_device(local)
+    guides = make_guides()
+    total_bp = args.genome_gbp * 1e9
+    t0 = time.time()
+    buf, names, starts, lens = build_genome(P, total_bp)
+    n = len(buf)
+    W = P.plane_words(n)
+    # Planes packed straight into pinned host memory (the e2e source buffers).
+    pinned = torch.empty(3 * W, dtype=torch.int32, pin_memory=True)
+    planes = pinned.numpy().view(np.uint32)
+    hi, lo, ot = planes[:W], planes[W:2 * W], planes[2 * W:]
+    _, _, _, exc_pos, _ = P.pack_text(buf, out=(hi, lo, ot))
+    assert exc_pos.size == 0  # the synthetic genome holds only A/C/G/T/N and ';'
+    gen_s = time.time() - t0
+
+    eng = P.CasOFFinder(local)
+    eng.readInputFile(input_text("synthetic", guides))
+    info = eng.input_info()
+    eng.load_genome_planes(hi, lo, ot, n, None, None, names, starts)
+    h2d_bytes = 3 * W * 4 + sum(len(x) for x in names) + 8 * len(starts)
+
+    # Warm-up (also sizes every device buffer).
+    rows_len = 0
+    for _ in range(args.warmup):
+        addr, rows_len = eng.search_view()
+    nh, nrows = eng.last_hit_count()
+
+    # ---- value: genome resident in HBM
+    dist_barrier(world)
+    eng.synchronize()
+    eng.reset_stats()
+    eng.set_profiling(True)
+    with ClockSampler(local) as clk:
+        eng.timer_start()
+        for _ in range(args.steps):
+            eng.search_view()
+        ms = eng.timer_stop()
+    eng.set_profiling(False)
+    stats = {k: eng.kernel_stats(k) for k in ("finder", "comparer", "format")}
+    tests_stat = eng.kernel_stats("comparer.tests")
+    ms_step = dist_max(ms / args.steps, world)
+    gbp = sum(lens) / 1e9
+    value = world * N_GUIDES * gbp / (ms_step / 1e3)
+
+    # ---- e2e: host planes -> device, search, rows -> host, every step
+    for _ in range(1):
+        eng.load_genome_planes(hi, lo, ot, n, None, None, names, starts)
+        eng.search_view()
+    dist_barrier(world)
+    eng.synchronize()
+    eng.timer_start()
+    for _ in range(args.steps):
+        eng.load_genome_planes(hi, lo, ot, n, None, None, names, starts)
+        _, rows_len = eng.search_view()
+    e2e_ms = dist_max(eng.timer_stop() / args.steps, world)
+    e2e_value = world * N_GUIDES * gbp / (e2e_ms / 1e3)
+
+    # ---- roofline of the dominant kernel (comparer: integer pipes)
+    rates = P.pipe_rates(local)
+    cmp = stats["comparer"]
+    nw = 1 if info["pattern_len"] <= 32 else 2
+    achieved = cmp["units"] / (cmp["ms"] * 1e-3) / 1e9 if cmp["ms"] else 0.0  # G base comparisons / s
+    tests = tests_stat["units"]
+    mean_nonN = cmp["units"] / tests if tests else 0.0  # base comparisons per variant test
+    tests_per_s = min(rates["lop3"] / (4 * nw), rates["popc"] / nw)
+    peak = tests_per_s * mean_nonN / 1e9
+    traffic = committed_traffic("comparer")
+    fnd = stats["finder"]
+    finder_gbs = (fnd["units"] * 0.375) / (fnd["ms"] * 1e-3) / 1e9 if fnd["ms"] else 0.0
+    peaks = load_peaks()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            binary, kind = cpu_binary()
+            with tempfile.TemporaryDirectory() as tmp:
+                sample_bp = int(args.sample_mbp * 1e6)
+                threads = os.cpu_count() or 1
+                dt, srows = cpu_sample_run(binary, buf, names, starts, sample_bp, guides, threads, tmp)
+                cpu = {"value": N_GUIDES * (sample_bp / 1e9) / dt, "unit": "guide-Gbp/s", "cores": threads,
+                       "kind": kind, "sample": f"first {sample_bp} bp of the same genome and input "
+                                               f"({srows} rows, {dt:.2f} s)"}
+        except Exception as e:  # the baseline is reported, never required
+            cpu = {"value": None, "unit": "guide-Gbp/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {e}"[:300]}
+
+    launches = int(stats["finder"]["launches"] + stats["comparer"]["launches"] + 2 * stats["format"]["launches"])
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "guide-Gbp/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": "plain: 3.1 Gbp synthetic genome (24 records, 41% GC +-10% drift, 5% N), "
+                                   "NNNNNNNNNNNNNNNNNNNNNRG dna 2 rna 1, 4 random 20-nt guides + NNN, mm 5",
+                       "genome_bp": n, "variants": info["variants"], "pattern_len": info["pattern_len"],
+                       "hits": nh, "rows": nrows, "l2": "no flush: inputs (1.16 GB planes) exceed L2",
+                       "genome_gen_s": round(gen_s, 1)},
+            "e2e": {"value": e2e_value, "unit": "guide-Gbp/s", "h2d_bytes_per_step": h2d_bytes,
+                    "d2h_bytes_per_step": rows_len + 16, "ms_per_step": e2e_ms},
+            "roofline": {"bound": "int-pipe", "kernel": "comparer", "achieved": achieved, "peak": peak,
+                         "unit": "G base-comparisons/s", "frac": achieved / peak if peak else None,
+                         "traffic": traffic,
+                         "peak_basis": f"measured LOP3 {rates['lop3'] / 1e12:.2f} T/s, POPC "
+                                       f"{rates['popc'] / 1e12:.2f} T/s; encoding {4 * nw} LOP3 + {nw} POPC "
+                                       f"per test, {mean_nonN:.2f} base comparisons per test"},
+            "roofline_finder": {"bound": "hbm", "achieved": finder_gbs, "peak": peaks.get("hbm_gbs"),
+                                "unit": "GB/s", "frac": finder_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs")
+                                else None, "basis": "0.375 B per genome position (3 bit planes)"},
+            "kernel_ms_per_step": {k: v["ms"] / max(1, args.steps) for k, v in stats.items()},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
+def committed_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        return json.load(open(path)).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+if __name__ == "__main__":
+    main()

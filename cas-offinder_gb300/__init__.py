@@ -35,8 +35,8 @@ EXPORTS = [
     "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes",
     "cof_genome_info", "cof_search", "cof_last_hit_count", "cof_set_summary", "cof_summary_text",
     "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
-    "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_synchronize",
-    "cofx_synth_record",
+    "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
+    "cof_synchronize", "cofx_synth_record", "cofx_pipe_rates",
 ]
 
 _lib = None
@@ -89,12 +89,16 @@ def lib():
             "cof_comparer_chunk": (c.c_int, [vp, c.c_char_p, u64, vp, vp, u32, c.c_char_p, u32, c.c_uint16,
                                              vp, vp, vp, c.POINTER(u32)]),
             "cof_plane_words": (u64, [u64]),
-            "cof_pack_text": (u64, [c.c_char_p, u64, vp, vp, vp, vp, vp]),
+            "cof_pack_text": (u64, [vp, u64, vp, vp, vp, vp, vp]),
             "cof_set_profiling": (c.c_int, [vp, c.c_int]),
             "cof_kernel_stats": (c.c_int, [vp, c.c_char_p, c.POINTER(u64), c.POINTER(c.c_double),
                                            c.POINTER(c.c_double)]),
             "cof_reset_stats": (c.c_int, [vp]),
             "cof_synchronize": (c.c_int, [vp]),
+            "cof_timer_start": (c.c_int, [vp]),
+            "cof_timer_stop": (c.c_int, [vp, c.POINTER(c.c_double)]),
+            "cofx_pipe_rates": (c.c_int, [c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double),
+                                          c.POINTER(c.c_double)]),
             "cofx_synth_record": (u64, [u64, u32, u64, c.c_double, c.c_double, u32, c.c_double, u32, u32, vp]),
         }
         for name, (res, args) in sig.items():
@@ -114,18 +118,31 @@ def plane_words(n):
     return int(lib().cof_plane_words(n))
 
 
-def pack_text(seq: bytes):
-    """Pack a reference-style genome string into (hi, lo, ot, exc_pos, exc_byte) numpy arrays."""
+def _addr(seq):
+    """Address of a bytes/bytearray buffer (bytes are copied once)."""
+    if isinstance(seq, bytearray):
+        return ctypes.addressof((ctypes.c_char * max(1, len(seq))).from_buffer(seq)) if len(seq) else None, seq
+    keep = ctypes.create_string_buffer(bytes(seq), max(1, len(seq)))
+    return ctypes.addressof(keep), keep
+
+
+def pack_text(seq, out=None):
+    """Pack a reference-style genome string into (hi, lo, ot, exc_pos, exc_byte)
+    numpy arrays.  `out` = optional preallocated (hi, lo, ot) arrays."""
     L = lib()
     n = len(seq)
     W = plane_words(n)
-    hi = np.zeros(W, np.uint32)
-    lo = np.zeros(W, np.uint32)
-    ot = np.zeros(W, np.uint32)
-    ne = int(L.cof_pack_text(seq, n, None, None, None, None, None))
+    addr, keep = _addr(seq)
+    if out is None:
+        hi, lo, ot = np.zeros(W, np.uint32), np.zeros(W, np.uint32), np.zeros(W, np.uint32)
+    else:
+        hi, lo, ot = out
+    ne = int(L.cof_pack_text(addr, n, _ptr(hi), _ptr(lo), _ptr(ot), None, None))
     ep = np.zeros(ne, np.uint64)
     eb = np.zeros(ne, np.uint8)
-    L.cof_pack_text(seq, n, _ptr(hi), _ptr(lo), _ptr(ot), _ptr(ep), _ptr(eb))
+    if ne:
+        L.cof_pack_text(addr, n, _ptr(hi), _ptr(lo), _ptr(ot), _ptr(ep), _ptr(eb))
+    del keep
     return hi, lo, ot, ep, eb
 
 
@@ -266,6 +283,22 @@ class CasOFFinder:
 
     def synchronize(self):
         self._check(self._L.cof_synchronize(self._h))
+
+    def timer_start(self):
+        self._check(self._L.cof_timer_start(self._h))
+
+    def timer_stop(self):
+        ms = ctypes.c_double()
+        self._check(self._L.cof_timer_stop(self._h, ctypes.byref(ms)))
+        return ms.value
+
+
+def pipe_rates(device=0):
+    """Measured integer-pipe throughput (lane-ops/s): {'lop3', 'popc', 'iadd'}."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    if lib().cofx_pipe_rates(device, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)) != 0:
+        raise RuntimeError("cofx_pipe_rates failed")
+    return {"lop3": a.value, "popc": b.value, "iadd": c.value}
 
 
 # ---------------------------------------------------------------- synthetic genomes

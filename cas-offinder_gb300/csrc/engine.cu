@@ -124,6 +124,7 @@ struct cof_handle {
 
   bool profiling = false;
   std::map<std::string, KernelStat> stats;
+  cudaEvent_t timer_a = nullptr, timer_b = nullptr;
 };
 
 namespace {
@@ -150,6 +151,13 @@ cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const
                          const std::vector<std::string>& names, const std::vector<uint64_t>& starts) {
   const uint64_t W = plane_words(n);
   dg.loaded = false;
+  // The record table must describe the genome like the reference's m_chrpos:
+  // first start 0, non-decreasing, inside the genome.
+  if (n >= (1ull << 36)) return fail(h, COF_ERR_UNSUPPORTED, "genome longer than 2^36 positions");
+  if (names.size() != starts.size()) return fail(h, COF_ERR_ARG, "record names and starts differ in count");
+  if (n > 0 && (starts.empty() || starts[0] != 0)) return fail(h, COF_ERR_ARG, "first record must start at 0");
+  for (size_t i = 1; i < starts.size(); ++i)
+    if (starts[i] < starts[i - 1] || starts[i] > n) return fail(h, COF_ERR_ARG, "record starts must be sorted");
   COF_CUDA(h, dg.hi.ensure(W * 4));
   COF_CUDA(h, dg.lo.ensure(W * 4));
   COF_CUDA(h, dg.ot.ensure(W * 4));
@@ -404,6 +412,10 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
     size_t si = 0;
     for (EventPair& p : evs)
       if (p.name == "comparer" && si < nseg) p.units = (double)qc[si++] * nonN;
+    // Variant tests (oriented candidate x variant) under "comparer.tests".
+    double cands = 0;
+    for (uint32_t x : qc) cands += x;
+    h->stats["comparer.tests"].units += cands * (double)h->job.variants.size();
     collect(h, evs);
   }
   h->last_hits = nhits;
@@ -525,6 +537,8 @@ void cof_close(cof_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   cudaStream_t s = h->stream;
+  if (h->timer_a) cudaEventDestroy(h->timer_a);
+  if (h->timer_b) cudaEventDestroy(h->timer_b);
   delete h;  // frees device buffers
   if (s) cudaStreamDestroy(s);
 }
@@ -678,6 +692,8 @@ cof_status cof_finder_chunk(cof_handle* h, const char* chr, uint64_t worksize, c
   g.lo.assign(plane_words(n), 0);
   g.ot.assign(plane_words(n), 0);
   pack_text(chr, n, g.hi.data(), g.lo.data(), g.ot.data(), &g.exc_pos, &g.exc_byte);
+  g.names.push_back("chunk");
+  g.starts.push_back(0);
   cof_status st = upload_packed(h, h->scratch, g);
   if (st) return st;
   FinderPattern fp;
@@ -738,6 +754,8 @@ cof_status cof_comparer_chunk(cof_handle* h, const char* chr, uint64_t chrlen, c
   g.lo.assign(plane_words(chrlen), 0);
   g.ot.assign(plane_words(chrlen), 0);
   pack_text(chr, chrlen, g.hi.data(), g.lo.data(), g.ot.data(), &g.exc_pos, &g.exc_byte);
+  g.names.push_back("chunk");
+  g.starts.push_back(0);
   cof_status st = upload_packed(h, h->scratch, g);
   if (st) return st;
   const int nw = patternlen <= 32 ? 1 : 2;
@@ -814,6 +832,25 @@ cof_status cof_kernel_stats(const cof_handle* h, const char* name, uint64_t* lau
 cof_status cof_reset_stats(cof_handle* h) {
   if (!h) return COF_ERR_ARG;
   h->stats.clear();
+  return COF_OK;
+}
+
+cof_status cof_timer_start(cof_handle* h) {
+  if (!h) return COF_ERR_ARG;
+  cudaSetDevice(h->device);
+  if (!h->timer_a) COF_CUDA(h, cudaEventCreate(&h->timer_a));
+  if (!h->timer_b) COF_CUDA(h, cudaEventCreate(&h->timer_b));
+  COF_CUDA(h, cudaEventRecord(h->timer_a, h->stream));
+  return COF_OK;
+}
+
+cof_status cof_timer_stop(cof_handle* h, double* ms) {
+  if (!h || !ms || !h->timer_a) return COF_ERR_ARG;
+  COF_CUDA(h, cudaEventRecord(h->timer_b, h->stream));
+  COF_CUDA(h, cudaEventSynchronize(h->timer_b));
+  float f = 0;
+  COF_CUDA(h, cudaEventElapsedTime(&f, h->timer_a, h->timer_b));
+  *ms = f;
   return COF_OK;
 }
 

@@ -1,0 +1,105 @@
+// Integer-pipe throughput probe (cofx_pipe_rates, include/cof_tools.h).
+//
+// The comparer's roofline is set by the integer pipes, not by HBM or the tensor
+// cores, so its denominator is measured here on the running GPU: sustained
+// lane-operations per second of LOP3, POPC and IADD3, each from a kernel of
+// many independent dependency chains (enough warps and chains to saturate the
+// pipe), timed with CUDA events.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/cof_tools.h"
+
+namespace {
+
+constexpr int kChains = 8;
+constexpr int kIters = 4096;
+constexpr int kUnroll = 8;
+
+__global__ void lop3_loop(uint32_t* sink, uint32_t seed) {
+  uint32_t a[kChains];
+  const uint32_t b = seed ^ threadIdx.x, c = seed * 3u + blockIdx.x;
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) a[i] = seed + i * 0x9E3779B9u + threadIdx.x;
+  for (int it = 0; it < kIters; ++it) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int i = 0; i < kChains; ++i) asm volatile("lop3.b32 %0, %0, %1, %2, 0x96;" : "+r"(a[i]) : "r"(b), "r"(c));
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) x ^= a[i];
+  if (x == 0x12345678u) sink[0] = x;
+}
+
+__global__ void popc_loop(uint32_t* sink, uint32_t seed) {
+  uint32_t a[kChains];
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) a[i] = seed + i * 0x9E3779B9u + threadIdx.x;
+  for (int it = 0; it < kIters; ++it) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int i = 0; i < kChains; ++i) asm volatile("popc.b32 %0, %0;" : "+r"(a[i]));
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) x ^= a[i];
+  if (x == 0x12345678u) sink[0] = x;
+}
+
+__global__ void iadd3_loop(uint32_t* sink, uint32_t seed) {
+  uint32_t a[kChains];
+  const uint32_t b = seed ^ threadIdx.x, c = seed * 3u + blockIdx.x;
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) a[i] = seed + i * 0x9E3779B9u + threadIdx.x;
+  for (int it = 0; it < kIters; ++it) {
+#pragma unroll
+    for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+      for (int i = 0; i < kChains; ++i) asm volatile("add.u32 %0, %0, %1;\n\tadd.u32 %0, %0, %2;" : "+r"(a[i]) : "r"(b), "r"(c));
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int i = 0; i < kChains; ++i) x ^= a[i];
+  if (x == 0x12345678u) sink[0] = x;
+}
+
+template <typename K>
+double rate(K kernel, int blocks, int threads, double ops_per_thread, uint32_t* sink) {
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  kernel<<<blocks, threads>>>(sink, 1u);  // warm-up
+  cudaEventRecord(a);
+  kernel<<<blocks, threads>>>(sink, 2u);
+  cudaEventRecord(b);
+  cudaEventSynchronize(b);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (cudaGetLastError() != cudaSuccess || ms <= 0) return 0;
+  return (double)blocks * threads * ops_per_thread / (ms * 1e-3);
+}
+
+}  // namespace
+
+extern "C" int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd) {
+  if (cudaSetDevice(device) != cudaSuccess) return 1;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  uint32_t* sink = nullptr;
+  if (cudaMalloc(&sink, 4) != cudaSuccess) return 1;
+  const int threads = 256, blocks = sms * 8;
+  const double per = (double)kIters * kUnroll * kChains;
+  if (lop3) *lop3 = rate(lop3_loop, blocks, threads, per, sink);
+  if (popc) *popc = rate(popc_loop, blocks, threads, per, sink);
+  // iadd3_loop issues two dependent add.u32 per chain step; ptxas may fuse them
+  // into one IADD3, so count one operation per pair (a lower bound on adds).
+  if (iadd) *iadd = rate(iadd3_loop, blocks, threads, per, sink);
+  cudaFree(sink);
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}

@@ -144,13 +144,18 @@ uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, 
 /* ---- instrumentation: per-kernel CUDA-event timing on the engine's stream. */
 cof_status cof_set_profiling(cof_handle* h, int enable);
 /* Totals since profiling was enabled for kernel `name` ("finder", "comparer",
- * "format"): launches, summed device milliseconds and algorithmic units
+ * "format"; "comparer.tests" counts variant tests in `units`): launches,
+ * summed device milliseconds and algorithmic units
  * (finder: genome positions scanned; comparer: base comparisons, i.e. the
  * non-N positions of each compare variant times the strand-oriented
  * candidates it was tested against, counted without early exit). */
 cof_status cof_kernel_stats(const cof_handle* h, const char* name, uint64_t* launches, double* total_ms,
                             double* units);
 cof_status cof_reset_stats(cof_handle* h);
+/* Device-side step timer: records a CUDA event on the handle's stream at
+ * start and stop; stop waits for the stream and returns the elapsed ms. */
+cof_status cof_timer_start(cof_handle* h);
+cof_status cof_timer_stop(cof_handle* h, double* ms);
 /* Wait for all work of the handle's stream. */
 cof_status cof_synchronize(cof_handle* h);
 

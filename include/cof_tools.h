@@ -24,6 +24,12 @@ uint64_t cofx_synth_record(uint64_t seed, uint32_t record, uint64_t len, double 
                            uint32_t drift_window, double n_frac, uint32_t n_run_min, uint32_t n_run_max,
                            char* out);
 
+/* Measures sustained integer-pipe throughput on CUDA device `device`, in
+ * lane-operations per second: LOP3 (3-input logic), POPC (population count)
+ * and IADD (32-bit add).  These are the denominators of the comparer's
+ * roofline.  Takes about a second.  Returns 0 on success. */
+int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd);
+
 #ifdef __cplusplus
 }
 #endif

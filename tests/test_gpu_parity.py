@@ -1,0 +1,146 @@
+"""Parity of the GB300 path with the reference (golden fixtures) and the oracle.
+
+All comparisons are byte-exact: the engine emits rows in the order the
+reference emits them for one chunk with work-items in order, which is also
+the oracle's order."""
+import os
+
+import numpy as np
+import pytest
+
+import cases
+from conftest import GOLDEN, golden_cases, golden_input
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_cli_matches_reference_golden(case, P, built, tmp_path):
+    d = os.path.join(GOLDEN, case)
+    inp = golden_input(case, tmp_path)
+    out = str(tmp_path / "out.tsv")
+    summ = str(tmp_path / "summary.txt") if os.path.exists(os.path.join(d, "expected_summary.txt")) else None
+    r = cases.run_cli(P.CLI_PATH, inp, out, device="G0", summary=summ)
+    if os.path.exists(os.path.join(d, "expected_error.txt")):
+        code, msg = open(os.path.join(d, "expected_error.txt")).read().split("\n")[:2]
+        assert r.returncode == int(code)
+        assert msg in r.stderr.decode()
+        return
+    assert r.returncode == 0, r.stderr.decode()
+    got, want = open(out, "rb").read(), open(os.path.join(d, "expected.tsv"), "rb").read()
+    if got != want:
+        g, w = cases.rows_of(got), cases.rows_of(want)
+        extra = sorted(set(g) - set(w))[:5]
+        missing = sorted(set(w) - set(g))[:5]
+        pytest.fail(f"{len(g)} rows vs {len(w)} expected; extra {extra}; missing {missing}")
+    if summ:
+        assert open(summ, "rb").read() == open(os.path.join(d, "expected_summary.txt"), "rb").read()
+
+
+RANDOM_CASES = [
+    dict(seed=201, lens=[120000, 80000], pattern="N" * 21 + "GG", mm=5, per_guide=40),
+    dict(seed=202, lens=[100000, 50000, 7], fmt="2bit", pattern="N" * 21 + "RG", dna=2, rna=1, mm=5, per_guide=40,
+         n_frac=0.05, gc_drift=0.1),
+    dict(seed=203, lens=[90000], pattern="TTTV" + "N" * 23, dna=1, rna=1, mm=4, per_guide=40),
+    dict(seed=204, lens=[60000, 40000], pattern="N" * 21 + "NNGRRT", dna=1, rna=1, mm=[3, 6], iupac_frac=0.1,
+         sprinkle_chars="RYKMWSBDHVnacgtX*-", with_ids=True),
+    dict(seed=205, lens=[70000], pattern="N" * 24 + "NNNNGMTT", dna=1, rna=1, mm=5, per_guide=40),
+    dict(seed=206, lens=[50000, 50000], pattern="N" * 20 + "NNAGAAW", dna=1, rna=1, mm=4, per_guide=40),
+    dict(seed=207, lens=[30000], pattern="N" * 40 + "NGG", dna=2, rna=2, mm=8, per_guide=40),
+]
+
+
+@pytest.mark.parametrize("spec", RANDOM_CASES, ids=[str(c["seed"]) for c in RANDOM_CASES])
+def test_cli_matches_oracle_random(spec, P, built, oracle, tmp_path):
+    inp, _ = cases.make_case(str(tmp_path), **spec)
+    a, b = str(tmp_path / "ora.tsv"), str(tmp_path / "gpu.tsv")
+    ra = cases.run_cli(oracle, inp, a, threads=4)
+    rb = cases.run_cli(P.CLI_PATH, inp, b, device="G0")
+    assert ra.returncode == 0, ra.stderr.decode()
+    assert rb.returncode == 0, rb.stderr.decode()
+    ta, tb = open(a, "rb").read(), open(b, "rb").read()
+    assert len(cases.rows_of(ta)) > 0
+    assert ta == tb
+
+
+def test_abi_search_matches_golden_and_repeats(P, built, tmp_path):
+    """Through the C ABI: same rows twice in a row, and after reloading."""
+    case = "nrg_bulge_2bit"
+    d = os.path.join(GOLDEN, case)
+    inp = golden_input(case, tmp_path)
+    want = open(os.path.join(d, "expected.tsv"), "rb").read()
+    with P.CasOFFinder(0) as eng:
+        eng.read_input_path(inp)
+        eng.load_genome_file(eng.chrdir)
+        first = eng.search()
+        second = eng.search()
+        assert P.HEADER.encode() + first == want
+        assert first == second
+        nh, nr = eng.last_hit_count()
+        assert nr == len(cases.rows_of(want))
+
+
+def test_abi_text_and_planes_loaders_agree(P, built, tmp_path):
+    """load_genome_text / load_genome_planes give the same rows as the file loader."""
+    case = "iupac_nngrrt"
+    inp = golden_input(case, tmp_path)
+    want = open(os.path.join(GOLDEN, case, "expected.tsv"), "rb").read()
+    names, seqs = read_fasta(os.path.join(GOLDEN, case, "genome.fa"))
+    text, starts = P.reference_text(seqs)
+    with P.CasOFFinder(0) as eng:
+        eng.read_input_path(inp)
+        eng.load_genome_text(text, names, starts)
+        assert P.HEADER.encode() + eng.search() == want
+        hi, lo, ot, ep, eb = P.pack_text(text)
+        eng.load_genome_planes(hi, lo, ot, len(text), ep, eb, names, starts)
+        assert P.HEADER.encode() + eng.search() == want
+
+
+def read_fasta(path):
+    names, seqs = [], []
+    for line in open(path, "rb").read().split(b"\n"):
+        line = line.rstrip(b"\r")
+        if line.startswith(b">"):
+            names.append(line[1:])
+            seqs.append(bytearray())
+        elif line:
+            seqs[-1] += line
+    return names, seqs
+
+
+def test_kernel_level_chunk_abi(P, built, tmp_path):
+    """cof_finder_chunk / cof_comparer_chunk (the OpenCL kernels' contracts)
+    against a direct restatement of finder_cpu/comparer_cpu on a small chunk."""
+    names, seqs = read_fasta(os.path.join(GOLDEN, "ngg_fasta", "genome.fa"))
+    text, _ = P.reference_text(seqs)
+    text = text[:30000]
+    pattern = b"N" * 21 + b"GG"
+    L = len(pattern)
+    rc = bytes(pattern[::-1].translate(bytes.maketrans(b"ACGTRYKMHDBV", b"TGCAYRMKDHVB")))
+    worksize = len(text) - L + 1
+    with P.CasOFFinder(0) as eng:
+        loci, flag = eng.finder_chunk(text, worksize, pattern + rc, L)
+        # finder_cpu: GG at +21 on '+', CC at +0 on '-'; windows with ';' dropped
+        exp = []
+        for i in range(worksize):
+            win = text[i:i + L]
+            f = win[21:23] == b"GG"
+            r = win[0:2] == b"CC"
+            if (f or r) and b";" not in win:
+                exp.append((i, 0 if (f and r) else (1 if f else 2)))
+        assert list(zip(loci.tolist(), flag.tolist())) == exp
+        comp = b"GGCCGACCTGTCGCTGACGCNNN"
+        mm_loci, mm_count, direction = eng.comparer_chunk(text, loci, flag, comp, 9)
+        rcomp = comp[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA"))
+        exp_hits = []
+        for i, fl in zip(loci.tolist(), flag.tolist()):
+            win = text[i:i + L]
+            for s, c in ((b"+", comp), (b"-", rcomp)):
+                if (s == b"+" and fl == 2) or (s == b"-" and fl == 1):
+                    continue
+                m = sum(1 for k in range(L) if c[k:k + 1] != b"N" and win[k] != c[k])
+                if m <= 9:
+                    exp_hits.append((i, m, s))
+        got = list(zip(mm_loci.tolist(), mm_count.tolist(), [bytes([x]) for x in direction]))
+        assert got == exp_hits
+        assert len(got) > 0

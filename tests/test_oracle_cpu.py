@@ -1,0 +1,75 @@
+"""The oracle (CPU restatement) against the reference's own outputs.
+
+Golden fixtures hold outputs of the reference itself (tests/golden/
+make_golden.py); the oracle must reproduce each byte for byte when run with
+one thread.  When the reference checkout is present, seeded random cases are
+also run through both programs here."""
+import os
+import subprocess
+
+import pytest
+
+import cases
+from conftest import GOLDEN, golden_cases, golden_input
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_oracle_matches_reference_golden(case, oracle, tmp_path):
+    d = os.path.join(GOLDEN, case)
+    inp = golden_input(case, tmp_path)
+    out = str(tmp_path / "out.tsv")
+    summ = str(tmp_path / "summary.txt") if os.path.exists(os.path.join(d, "expected_summary.txt")) else None
+    r = cases.run_cli(oracle, inp, out, threads=1, summary=summ)
+    if os.path.exists(os.path.join(d, "expected_error.txt")):
+        code, msg = open(os.path.join(d, "expected_error.txt")).read().split("\n")[:2]
+        assert r.returncode == int(code)
+        assert msg in r.stderr.decode()
+        return
+    assert r.returncode == 0, r.stderr.decode()
+    assert open(out, "rb").read() == open(os.path.join(d, "expected.tsv"), "rb").read()
+    if summ:
+        assert open(summ, "rb").read() == open(os.path.join(d, "expected_summary.txt"), "rb").read()
+
+
+def test_oracle_threads_same_order(oracle, tmp_path):
+    inp = golden_input("nrg_bulge_2bit", tmp_path)
+    a, b = str(tmp_path / "a.tsv"), str(tmp_path / "b.tsv")
+    assert cases.run_cli(oracle, inp, a, threads=1).returncode == 0
+    assert cases.run_cli(oracle, inp, b, threads=4).returncode == 0
+    assert open(a, "rb").read() == open(b, "rb").read()
+
+
+RANDOM_CASES = [
+    dict(seed=101, lens=[20000, 15000], pattern="N" * 21 + "GG", mm=4),
+    dict(seed=102, lens=[30000], fmt="2bit", pattern="N" * 21 + "RG", dna=2, rna=1, mm=5),
+    dict(seed=103, lens=[25000, 5000], pattern="TTTN" + "N" * 20, dna=2, rna=2, mm=3),
+    dict(seed=104, lens=[20000], pattern="N" * 19 + "NNGRRT", dna=1, rna=0, mm=[2, 6], iupac_frac=0.15,
+         sprinkle_chars="RYSWnX"),
+    dict(seed=105, lens=[8000, 8000], pattern="N" * 30 + "NGG", dna=1, rna=1, mm=6),
+]
+
+
+@pytest.mark.parametrize("spec", RANDOM_CASES, ids=[str(c["seed"]) for c in RANDOM_CASES])
+def test_oracle_matches_reference_random(spec, oracle, reference, tmp_path):
+    if reference is None:
+        pytest.skip("reference checkout not present")
+    inp, _ = cases.make_case(str(tmp_path), **spec)
+    a, b = str(tmp_path / "ref.tsv"), str(tmp_path / "ora.tsv")
+    ra = cases.run_cli(reference, inp, a, threads=1)
+    rb = cases.run_cli(oracle, inp, b, threads=1)
+    assert ra.returncode == 0 and rb.returncode == 0
+    ta, tb = open(a, "rb").read(), open(b, "rb").read()
+    assert ta == tb
+    assert len(cases.rows_of(ta)) > 0
+
+
+def test_reference_gpu_kernels_agree(reference, tmp_path):
+    """The reference's work-group kernels (finder/comparer, device G) give the
+    same rows as its CPU kernels (multiset; atomics reorder them)."""
+    if reference is None:
+        pytest.skip("reference checkout not present")
+    inp = golden_input("nrg_bulge_2bit", tmp_path)
+    a, b = str(tmp_path / "c.tsv"), str(tmp_path / "g.tsv")
+    assert cases.run_cli(reference, inp, a, threads=2, device="C").returncode == 0
+    assert cases.run_cli(reference, inp, b, threads=2, device="G").returncode == 0
+    assert cases.canonical(open(a, "rb").read()) == cases.canonical(open(b, "rb").read())
