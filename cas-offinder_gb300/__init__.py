@@ -36,7 +36,7 @@ EXPORTS = [
     "cof_genome_info", "cof_search", "cof_last_hit_count", "cof_set_summary", "cof_summary_text",
     "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
     "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
-    "cof_synchronize", "cofx_synth_record", "cofx_pipe_rates",
+    "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cofx_synth_record", "cofx_pipe_rates",
 ]
 
 _lib = None
@@ -96,6 +96,8 @@ def lib():
             "cof_reset_stats": (c.c_int, [vp]),
             "cof_synchronize": (c.c_int, [vp]),
             "cof_timer_start": (c.c_int, [vp]),
+            "cof_set_comparer": (c.c_int, [vp, c.c_int]),
+            "cof_comparer_info": (c.c_int, [vp, c.POINTER(c.c_int), c.POINTER(c.c_int)]),
             "cof_timer_stop": (c.c_int, [vp, c.POINTER(c.c_double)]),
             "cofx_pipe_rates": (c.c_int, [c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double),
                                           c.POINTER(c.c_double)]),
@@ -267,6 +269,15 @@ class CasOFFinder:
                                                _ptr(mm_count), _ptr(direction), ctypes.byref(cnt)))
         k = cnt.value
         return mm_loci[:k].copy(), mm_count[:k].copy(), direction[:k].tobytes()
+
+    def set_comparer(self, kind):
+        """0 auto (bit-sliced when it fits), 1 popcount, 2 bit-sliced."""
+        self._check(self._L.cof_set_comparer(self._h, kind))
+
+    def comparer_info(self):
+        k, sl = ctypes.c_int(), ctypes.c_int()
+        self._check(self._L.cof_comparer_info(self._h, ctypes.byref(k), ctypes.byref(sl)))
+        return {"kind": {1: "popcount", 2: "bit-sliced"}[k.value], "slots": sl.value}
 
     # instrumentation
     def set_profiling(self, on=True):

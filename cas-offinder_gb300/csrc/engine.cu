@@ -102,7 +102,9 @@ struct KernelStat {
 struct cof_handle {
   int device = 0;
   int sm_count = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;   // comparer, formatting, copies
+  cudaStream_t stream2 = nullptr;  // finder passes, one segment ahead of the comparer
+  cudaEvent_t ev_start = nullptr, ev_found[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
   std::string err;
 
   Job job;
@@ -111,11 +113,14 @@ struct cof_handle {
   int nw = 1;
   std::vector<uint32_t> nonN;  // non-N positions per variant
   DevBuf vmask, vfmt, sfmt, pool;
+  DevBuf bs_off, bs_thr, bs_gid;  // bit-sliced comparer tables
+  int bs_slots = 0;               // 0: use the popcount comparer
+  bool force_popc = false;
   FinderPattern fpat{};
 
   DevGenome genome, scratch;
 
-  DevBuf queue, qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small;
+  DevBuf queue[2], qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small;
   HostPinned host_text;
   std::string summary_text;
   std::map<std::string, unsigned long long> summary;
@@ -294,6 +299,40 @@ cof_status upload_job(cof_handle* h) {
       vf[v].shape_end[s] = (uint32_t)sf.size();
     }
   }
+  // Bit-sliced comparer tables: per variant, the positions that can mismatch
+  // as offsets of their class word in the shared-memory table.
+  int maxpos = 0;
+  for (const Variant& var : job.variants) {
+    int c = 0;
+    for (char ch : var.key) c += bs_class_of((unsigned char)ch) != 0;
+    maxpos = std::max(maxpos, c);
+  }
+  h->bs_slots = h->force_popc ? 0 : bs_slots_for(maxpos);
+  if (h->bs_slots) {
+    const int S = h->bs_slots;
+    const uint32_t row = (uint32_t)bs_row_for((uint32_t)L);
+    std::vector<uint32_t> off(std::max<size_t>(V, 1) * (S / 2), 0), thr(std::max<size_t>(V, 1), 0),
+        gid(std::max<size_t>(V, 1), 0);
+    for (size_t v = 0; v < V; ++v) {
+      const std::string& key = job.variants[v].key;
+      int s = 0;
+      for (size_t k = 0; k < key.size(); ++k) {
+        const uint32_t c = bs_class_of((unsigned char)key[k]);
+        if (!c) continue;
+        const uint32_t byte_off = (c * row + (uint32_t)k) * 8;  // uint2 table element (two groups)
+        off[v * (S / 2) + s / 2] |= byte_off << (16 * (s & 1));
+        ++s;
+      }
+      thr[v] = job.variants[v].threshold;
+      gid[v] = (uint32_t)v;
+    }
+    COF_CUDA(h, h->bs_off.ensure(off.size() * 4));
+    COF_CUDA(h, h->bs_thr.ensure(thr.size() * 4));
+    COF_CUDA(h, h->bs_gid.ensure(gid.size() * 4));
+    COF_CUDA(h, cudaMemcpyAsync(h->bs_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(h->bs_thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(h->bs_gid.p, gid.data(), gid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  }
   COF_CUDA(h, h->vmask.ensure(masks.size()));
   COF_CUDA(h, h->vfmt.ensure(std::max<size_t>(V, 1) * sizeof(VariantFmt)));
   COF_CUDA(h, h->sfmt.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
@@ -314,20 +353,21 @@ struct EventPair {
   double units = 0;
 };
 
-cof_status record_start(cof_handle* h, std::vector<EventPair>& evs, const char* name, double units) {
+cof_status record_start(cof_handle* h, std::vector<EventPair>& evs, const char* name, double units,
+                        cudaStream_t st) {
   if (!h->profiling) return COF_OK;
   EventPair p;
   p.name = name;
   p.units = units;
   COF_CUDA(h, cudaEventCreate(&p.a));
   COF_CUDA(h, cudaEventCreate(&p.b));
-  COF_CUDA(h, cudaEventRecord(p.a, h->stream));
+  COF_CUDA(h, cudaEventRecord(p.a, st));
   evs.push_back(p);
   return COF_OK;
 }
-cof_status record_stop(cof_handle* h, std::vector<EventPair>& evs) {
+cof_status record_stop(cof_handle* h, std::vector<EventPair>& evs, cudaStream_t st) {
   if (!h->profiling) return COF_OK;
-  COF_CUDA(h, cudaEventRecord(evs.back().b, h->stream));
+  COF_CUDA(h, cudaEventRecord(evs.back().b, st));
   return COF_OK;
 }
 void collect(cof_handle* h, std::vector<EventPair>& evs) {
@@ -346,6 +386,8 @@ void collect(cof_handle* h, std::vector<EventPair>& evs) {
 }
 
 // Finder + comparer over the whole genome; leaves the hit count in h->hit_count.
+// Segment s is scanned on stream2 into queue[s % 2] while the comparer works
+// on segment s - 1 on the main stream; events order the two.
 cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& evs, uint64_t* seg_count) {
   const DevGenome& dg = h->genome;
   const GenomeView gv = dg.view();
@@ -357,18 +399,30 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   COF_CUDA(h, h->qcounts.ensure(std::max<uint64_t>(nseg, 1) * 4));
   COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<uint64_t>(nseg, 1) * 4, h->stream));
   COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
+  COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
+  COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
+  const uint32_t V = (uint32_t)h->job.variants.size();
   for (uint64_t s = 0; s < nseg; ++s) {
+    const int b = (int)(s & 1);
     const uint64_t w0 = s * kSegWords, w1 = std::min(total_words, w0 + kSegWords);
     uint32_t* qc = h->qcounts.as<uint32_t>() + s;
-    cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32);
+    uint32_t* q = h->queue[b].as<uint32_t>();
+    if (s >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
+    cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32, h->stream2);
     if (st) return st;
-    launch_finder(gv, w0, w1, h->fpat, h->queue.as<uint32_t>(), qc, h->stream);
-    if ((st = record_stop(h, evs))) return st;
-    if ((st = record_start(h, evs, "comparer", 0))) return st;
-    launch_comparer(gv, h->queue.as<uint32_t>(), qc, w0 * 32, h->vmask.p, (uint32_t)h->job.variants.size(), h->nw,
-                    (uint32_t)L, h->hits.as<uint64_t>(), h->hit_count.as<unsigned long long>(), hit_cap,
-                    h->sm_count, h->stream);
-    if ((st = record_stop(h, evs))) return st;
+    launch_finder(gv, w0, w1, h->fpat, q, qc, h->stream2);
+    if ((st = record_stop(h, evs, h->stream2))) return st;
+    COF_CUDA(h, cudaEventRecord(h->ev_found[b], h->stream2));
+    COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_found[b], 0));
+    if ((st = record_start(h, evs, "comparer", 0, h->stream))) return st;
+    if (!h->bs_slots ||
+        !launch_comparer_bs(gv, q, qc, w0 * 32, h->bs_off.as<uint32_t>(), h->bs_thr.as<uint32_t>(),
+                            h->bs_gid.as<uint32_t>(), V, h->bs_slots, (uint32_t)L, h->hits.as<uint64_t>(),
+                            h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream))
+      launch_comparer(gv, q, qc, w0 * 32, h->vmask.p, V, h->nw, (uint32_t)L, h->hits.as<uint64_t>(),
+                      h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream);
+    if ((st = record_stop(h, evs, h->stream))) return st;
+    COF_CUDA(h, cudaEventRecord(h->ev_used[b], h->stream));
   }
   COF_CUDA(h, cudaGetLastError());
   return COF_OK;
@@ -388,7 +442,8 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
     *rows = "";
     return COF_OK;
   }
-  COF_CUDA(h, h->queue.ensure(2 * kSegPositions * 4));
+  COF_CUDA(h, h->queue[0].ensure(2 * kSegPositions * 4));
+  COF_CUDA(h, h->queue[1].ensure(2 * kSegPositions * 4));
   COF_CUDA(h, h->hit_count.ensure(8));
   uint64_t cap = std::max<uint64_t>(h->hits.cap / 8, 1u << 20);
   COF_CUDA(h, h->hits.ensure(cap * 8));
@@ -445,7 +500,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   // Row sizes, offsets, then the rows themselves.
   const GenomeView gv = h->genome.view();
   FormatTables ft{h->vfmt.as<VariantFmt>(), h->sfmt.as<ShapeFmt>(), h->pool.as<char>()};
-  if ((st = record_start(h, evs, "format", (double)nhits))) return st;
+  if ((st = record_start(h, evs, "format", (double)nhits, h->stream))) return st;
   launch_row_lengths(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_bytes.as<uint64_t>(),
                      h->row_count.as<uint32_t>(), h->stream);
   tmp = h->sort_tmp.cap;
@@ -464,7 +519,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   COF_CUDA(h, h->text.ensure(bytes + 1));
   launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), h->text.as<char>(),
                     h->stream);
-  if ((st = record_stop(h, evs))) return st;
+  if ((st = record_stop(h, evs, h->stream))) return st;
   COF_CUDA(h, cudaGetLastError());
   COF_CUDA(h, h->host_text.ensure(bytes + 1));
   COF_CUDA(h, cudaMemcpyAsync(h->host_text.p, h->text.p, bytes, cudaMemcpyDeviceToHost, h->stream));
@@ -523,9 +578,16 @@ cof_status cof_open(int device, cof_handle** out) {
   cof_handle* h = new cof_handle();
   h->device = device;
   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device);
-  if ((e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking)) != cudaSuccess) {
-    set_err(std::string("cudaStreamCreate: ") + cudaGetErrorString(e));
-    delete h;
+  e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    e = cudaEventCreateWithFlags(&h->ev_found[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_used[i], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    set_err(std::string("stream/event creation: ") + cudaGetErrorString(e));
+    cof_close(h);
     return COF_ERR_CUDA;
   }
   *out = h;
@@ -536,11 +598,15 @@ void cof_close(cof_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  cudaStream_t s = h->stream;
-  if (h->timer_a) cudaEventDestroy(h->timer_a);
-  if (h->timer_b) cudaEventDestroy(h->timer_b);
+  if (h->stream2) cudaStreamSynchronize(h->stream2);
+  cudaStream_t s = h->stream, s2 = h->stream2;
+  cudaEvent_t evs[7] = {h->timer_a, h->timer_b, h->ev_start, h->ev_found[0], h->ev_found[1], h->ev_used[0],
+                        h->ev_used[1]};
   delete h;  // frees device buffers
+  for (cudaEvent_t ev : evs)
+    if (ev) cudaEventDestroy(ev);
   if (s) cudaStreamDestroy(s);
+  if (s2) cudaStreamDestroy(s2);
 }
 
 const char* cof_last_error(const cof_handle* h) { return h ? h->err.c_str() : "null handle"; }
@@ -810,6 +876,20 @@ uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, 
     std::copy(eb.begin(), eb.end(), exc_byte);
   }
   return ep.size();
+}
+
+cof_status cof_set_comparer(cof_handle* h, int kind) {
+  if (!h || kind < 0 || kind > 2) return COF_ERR_ARG;
+  h->force_popc = kind == 1;
+  h->job_on_device = false;  // rebuild the comparer tables on the next search
+  return COF_OK;
+}
+
+cof_status cof_comparer_info(const cof_handle* h, int* kind, int* slots) {
+  if (!h) return COF_ERR_ARG;
+  if (kind) *kind = h->bs_slots ? 2 : 1;
+  if (slots) *slots = h->bs_slots;
+  return COF_OK;
 }
 
 cof_status cof_set_profiling(cof_handle* h, int enable) {

@@ -45,11 +45,19 @@ __device__ __forceinline__ uint32_t bits_at(uint32_t w0, uint32_t w1, uint32_t w
 }  // namespace
 
 // ---------------------------------------------------------------- finder
-__global__ void __launch_bounds__(256) finder_kernel(const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo,
-                                                     const uint32_t* __restrict__ ot, uint64_t w_begin, uint64_t w_end,
-                                                     const __grid_constant__ FinderPattern pat,
-                                                     uint32_t* __restrict__ queue, uint32_t* __restrict__ qcount) {
+// One thread = 32 consecutive start positions (one plane word).  A warp's
+// candidates are staged in shared memory in scan order, then written to the
+// queue with one atomic reservation and coalesced stores.
+constexpr int kFinderThreads = 128;
+constexpr int kFinderStage = 32 * 64;  // a warp emits at most 32 words x 32 starts x 2 strands
+
+__global__ void __launch_bounds__(kFinderThreads) finder_kernel(
+    const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
+    uint64_t w_begin, uint64_t w_end, const __grid_constant__ FinderPattern pat, uint32_t* __restrict__ queue,
+    uint32_t* __restrict__ qcount) {
+  __shared__ uint32_t stage[kFinderThreads / 32][kFinderStage];
   const unsigned lane = threadIdx.x & 31;
+  uint32_t* my = stage[threadIdx.x >> 5];
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t wb = w_begin + (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wb < w_end; wb += stride) {
     const uint64_t w = wb + lane;
@@ -92,32 +100,36 @@ __global__ void __launch_bounds__(256) finder_kernel(const uint32_t* __restrict_
       if (lane >= (unsigned)d) incl += t;
     }
     const uint32_t total = __shfl_sync(kFull, incl, 31);
-    uint32_t base = 0;
-    if (lane == 31 && total) base = atomicAdd(qcount, total);
-    base = __shfl_sync(kFull, base, 31);
-    uint32_t at = base + incl - cnt;
+    if (total == 0) continue;  // warp-uniform
+    uint32_t at = incl - cnt;
     const uint32_t rel = (uint32_t)((w - w_begin) << 5);
     while (fwd) {
       const unsigned b = __ffs(fwd) - 1;
       fwd &= fwd - 1;
-      queue[at++] = (rel + b) << 1;
+      my[at++] = (rel + b) << 1;
     }
     while (rev) {
       const unsigned b = __ffs(rev) - 1;
       rev &= rev - 1;
-      queue[at++] = ((rel + b) << 1) | 1u;
+      my[at++] = ((rel + b) << 1) | 1u;
     }
+    __syncwarp();
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(qcount, total);
+    base = __shfl_sync(kFull, base, 0);
+    for (uint32_t i = lane; i < total; i += 32) queue[base + i] = my[i];
+    __syncwarp();
   }
 }
 
 void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const FinderPattern& pat, uint32_t* queue,
                    uint32_t* qcount, cudaStream_t stream) {
   const uint64_t words = w_end - w_begin;
-  const unsigned threads = 256;
-  uint64_t blocks = (words + threads - 1) / threads;
+  uint64_t blocks = (words + kFinderThreads - 1) / kFinderThreads;
   if (blocks > 65535ull * 8) blocks = 65535ull * 8;
   if (blocks == 0) return;
-  finder_kernel<<<(unsigned)blocks, threads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, pat, queue, qcount);
+  finder_kernel<<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, pat, queue,
+                                                                  qcount);
 }
 
 // ---------------------------------------------------------------- comparer

@@ -105,6 +105,19 @@ void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const 
 void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                      const void* vars, uint32_t nvar, int nw, uint32_t L, uint64_t* hits,
                      unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
+// Bit-sliced comparer (comparer_bs.cu) for variants with at most 32 positions
+// that can mismatch.  `voff` holds, per variant, `slots` u16 shared-memory
+// byte offsets ((class * row + k) * 8, 0 = padding), packed two per word;
+// `vthr` the thresholds; `vgid` the global variant indices.  Returns false if
+// no kernel instance fits (then use launch_comparer).
+bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
+                        const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, int slots,
+                        uint32_t L, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
+                        cudaStream_t stream);
+int bs_slots_for(int max_positions);  // 0 when more than 32 positions can mismatch
+int bs_row_for(uint32_t L);           // words per class row of the shared table
+uint32_t bs_class_of(unsigned char p);  // class row of a pattern byte (0: never mismatches)
+
 // Row byte counts per sorted hit (and rows per hit).
 void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
                         uint64_t* row_bytes, uint32_t* row_count, cudaStream_t stream);

@@ -141,6 +141,15 @@ uint64_t cof_plane_words(uint64_t n);
 uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, uint32_t* ot, uint64_t* exc_pos,
                        uint8_t* exc_byte);
 
+/* ---- comparer selection.  0 (default): the bit-sliced comparer when every
+ * compare variant has at most 32 positions that can mismatch, else the
+ * popcount comparer; 1: always the popcount comparer; 2: bit-sliced where
+ * possible (same as 0).  Both give identical hits. */
+cof_status cof_set_comparer(cof_handle* h, int kind);
+/* Comparer used by the last search: *kind 1 popcount, 2 bit-sliced; *slots =
+ * the bit-sliced slot count (mismatchable positions per variant, padded). */
+cof_status cof_comparer_info(const cof_handle* h, int* kind, int* slots);
+
 /* ---- instrumentation: per-kernel CUDA-event timing on the engine's stream. */
 cof_status cof_set_profiling(cof_handle* h, int enable);
 /* Totals since profiling was enabled for kernel `name` ("finder", "comparer",

@@ -144,3 +144,18 @@ def test_kernel_level_chunk_abi(P, built, tmp_path):
         got = list(zip(mm_loci.tolist(), mm_count.tolist(), [bytes([x]) for x in direction]))
         assert got == exp_hits
         assert len(got) > 0
+
+
+@pytest.mark.parametrize("spec", RANDOM_CASES[:5], ids=[str(c["seed"]) for c in RANDOM_CASES[:5]])
+def test_both_comparers_identical(spec, P, built, oracle, tmp_path):
+    """The popcount and the bit-sliced comparer give the same rows as the oracle."""
+    inp, _ = cases.make_case(str(tmp_path), **spec)
+    a = str(tmp_path / "ora.tsv")
+    assert cases.run_cli(oracle, inp, a, threads=4).returncode == 0
+    want = open(a, "rb").read()
+    with P.CasOFFinder(0) as eng:
+        eng.read_input_path(inp)
+        eng.load_genome_file(eng.chrdir)
+        for kind in (1, 2, 0):
+            eng.set_comparer(kind)
+            assert P.HEADER.encode() + eng.search() == want, f"comparer {kind}"
