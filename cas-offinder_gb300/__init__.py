@@ -25,7 +25,7 @@ CLI_PATH = os.path.join(PKG_DIR, "bin", "cas-offinder")
 
 COF_OK = 0
 STATUS_NAMES = {0: "OK", 1: "CUDA", 2: "ARG", 3: "NOMEM", 4: "INPUT", 5: "IO", 6: "STATE",
-                7: "UNSUPPORTED", 8: "NOT_GENOME", 9: "DEVICE"}
+                7: "UNSUPPORTED", 8: "NOT_GENOME", 9: "DEVICE", 10: "TOO_LARGE"}
 HEADER = ("##Generated by Cas-OFFinder 3.0.0\n"
           "#Id\tBulge Type\tcrRNA\tDNA\tChromosome\tLocation\tDirection\tMismatches\tBulge Size\n")
 
@@ -36,7 +36,8 @@ EXPORTS = [
     "cof_genome_info", "cof_search", "cof_last_hit_count", "cof_set_summary", "cof_summary_text",
     "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
     "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
-    "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cofx_synth_record", "cofx_pipe_rates",
+    "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cof_search_chunk_static",
+    "cofx_synth_record", "cofx_pipe_rates",
 ]
 
 _lib = None
@@ -98,6 +99,8 @@ def lib():
             "cof_timer_start": (c.c_int, [vp]),
             "cof_set_comparer": (c.c_int, [vp, c.c_int]),
             "cof_comparer_info": (c.c_int, [vp, c.POINTER(c.c_int), c.POINTER(c.c_int)]),
+            "cof_search_chunk_static": (c.c_int, [vp, vp, vp, u64, c.c_char_p, c.c_char_p, u32, c.c_uint16, vp,
+                                                  u64, vp, vp]),
             "cof_timer_stop": (c.c_int, [vp, c.POINTER(c.c_double)]),
             "cofx_pipe_rates": (c.c_int, [c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double),
                                           c.POINTER(c.c_double)]),

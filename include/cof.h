@@ -40,7 +40,8 @@ enum {
   COF_ERR_STATE = 6,       /* call out of order (no input or no genome loaded) */
   COF_ERR_UNSUPPORTED = 7, /* pattern longer than COF_MAX_PATTERN */
   COF_ERR_NOT_GENOME = 8,  /* file is neither FASTA nor 2BIT ("Skipping non-acceptable file") */
-  COF_ERR_DEVICE = 9       /* a kernel reported an internal inconsistency */
+  COF_ERR_DEVICE = 9,      /* a kernel reported an internal inconsistency */
+  COF_ERR_TOO_LARGE = 10   /* input larger than a fixed limit of the entry point */
 };
 
 /* Longest pattern (PAM + spacer + DNA-bulge padding) the kernels accept. */
@@ -131,6 +132,30 @@ cof_status cof_comparer_chunk(cof_handle* h, const char* chr, uint64_t chrlen, c
                               const uint8_t* flag, uint32_t locicnt, const char* comp, uint32_t patternlen,
                               uint16_t threshold, uint32_t* mm_loci, uint16_t* mm_count, char* direction,
                               uint32_t* entrycount);
+
+/* ---- allocation-free chunk search.  No counterpart in the reference: it is
+ * for callers that may not allocate device memory when they search (a host
+ * application that reserved all its GPU memory in its own pool, or a caller
+ * that cannot afford the device-wide synchronization of cudaMalloc/cudaFree).
+ * The caller passes device memory for everything it owns: the chunk's genome
+ * planes (`d_hi`/`d_lo`/`d_ot`, cof_plane_words(n) words each, packed as
+ * cof_pack_text packs, so positions past n read as separators), the hit keys
+ * `d_hits` (hit_cap u64: bits 43..8 start position, bit 7 strand ('-' = 1),
+ * bits 6..0 mismatches) and the hit counter `d_hit_count` (set to the number
+ * of hits; hits past hit_cap are counted, not written).  `pattern` and `comp`
+ * are host strings of patternlen bytes (the padded pattern and one compare
+ * string; reverse complements are formed internally), `stream` a
+ * cudaStream_t (0 = default stream).  Work is queued on `stream`; the results
+ * are valid once it completes.  The candidate queue is a fixed 16 MiB device
+ * array inside the library (held by every GPU that loads it), so n is limited
+ * to 2^21 positions: larger chunks return COF_ERR_TOO_LARGE.  The first call
+ * on a device looks up that array's device address; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race, so
+ * order them (e.g. one stream).  Nothing is allocated or freed. */
+cof_status cof_search_chunk_static(const uint32_t* d_hi, const uint32_t* d_lo, const uint32_t* d_ot, uint64_t n,
+                                   const char* pattern, const char* comp, uint32_t patternlen, uint16_t threshold,
+                                   uint64_t* d_hits, uint64_t hit_cap, unsigned long long* d_hit_count,
+                                   void* stream);
 
 /* ---- packing helpers (host side). */
 /* Words per plane for a genome of n bytes (includes the tail padding). */
