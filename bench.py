@@ -55,6 +55,25 @@ def make_guides(seed=GUIDE_SEED, n=N_GUIDES):
     return ["".join(rng.choice("ACGT") for _ in range(20)) + "NNN" for _ in range(n)]
 
 
+def batched_jobs(seed=5, n=1024, genome_path="synthetic"):
+    """The 1,024-guide mixed workload: one input file per guide, spacer 20-24
+    random bases with 2% IUPAC degenerate codes, PAM NGG or NRG (50/50), max
+    mismatches 3-6, DNA bulge 0-2, RNA bulge 0-1 (all uniform)."""
+    import random
+    rng = random.Random(seed)
+    texts = []
+    for _ in range(n):
+        spacer = rng.randint(20, 24)
+        pam = rng.choice(["NGG", "NRG"])
+        mm, dna, rna = rng.randint(3, 6), rng.randint(0, 2), rng.randint(0, 1)
+        guide = "".join(rng.choice("ACGT") if rng.random() >= 0.02 else rng.choice("RYKMWSBDHV")
+                        for _ in range(spacer)) + "NNN"
+        pattern = "N" * spacer + pam
+        line2 = pattern + (f" {dna} {rna}" if (dna or rna) else "")
+        texts.append(f"{genome_path}\n{line2}\n{guide} {mm}\n")
+    return texts
+
+
 def input_text(genome_path, guides):
     return f"{genome_path}\n{PATTERN} {DNA} {RNA}\n" + "".join(f"{g} {MM}\n" for g in guides)
 

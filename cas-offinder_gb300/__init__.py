@@ -37,7 +37,8 @@ EXPORTS = [
     "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
     "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
     "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cof_search_chunk_static",
-    "cofx_synth_record", "cofx_pipe_rates",
+    "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
+    "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table",
 ]
 
 _lib = None
@@ -99,11 +100,17 @@ def lib():
             "cof_timer_start": (c.c_int, [vp]),
             "cof_set_comparer": (c.c_int, [vp, c.c_int]),
             "cof_comparer_info": (c.c_int, [vp, c.POINTER(c.c_int), c.POINTER(c.c_int)]),
+            "cof_batch_clear": (c.c_int, [vp]),
+            "cof_batch_add_input": (c.c_int, [vp, c.c_char_p, sz, c.POINTER(u32)]),
+            "cof_batch_size": (c.c_int, [vp, c.POINTER(u32)]),
+            "cof_job_rows": (c.c_int, [vp, u32, c.POINTER(c.c_void_p), c.POINTER(sz)]),
+            "cof_job_summary_text": (c.c_int, [vp, u32, c.POINTER(c.c_void_p), c.POINTER(sz)]),
             "cof_search_chunk_static": (c.c_int, [vp, vp, vp, u64, c.c_char_p, c.c_char_p, u32, c.c_uint16, vp,
                                                   u64, vp, vp]),
             "cof_timer_stop": (c.c_int, [vp, c.POINTER(c.c_double)]),
             "cofx_pipe_rates": (c.c_int, [c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double),
                                           c.POINTER(c.c_double)]),
+            "cofx_mismatch_table": (None, [vp]),
             "cofx_synth_record": (u64, [u64, u32, u64, c.c_double, c.c_double, u32, c.c_double, u32, u32, vp]),
         }
         for name, (res, args) in sig.items():
@@ -119,6 +126,13 @@ def _ptr(a):
 
 
 # ---------------------------------------------------------------- packing
+def mismatch_table():
+    """The engine's mismatch predicate as a 256x256 uint8 array [pattern byte, genome byte]."""
+    out = np.zeros(65536, np.uint8)
+    lib().cofx_mismatch_table(_ptr(out))
+    return out.reshape(256, 256)
+
+
 def plane_words(n):
     return int(lib().cof_plane_words(n))
 
@@ -236,6 +250,32 @@ class CasOFFinder:
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         self._check(self._L.cof_search(self._h, ctypes.byref(p), ctypes.byref(n)))
         return p.value, n.value
+
+    # batched search (several input files over the resident genome)
+    def batch_clear(self):
+        self._check(self._L.cof_batch_clear(self._h))
+
+    def batch_add_input(self, text):
+        if isinstance(text, str):
+            text = text.encode()
+        j = ctypes.c_uint32()
+        self._check(self._L.cof_batch_add_input(self._h, text, len(text), ctypes.byref(j)))
+        return j.value
+
+    def batch_size(self):
+        n = ctypes.c_uint32()
+        self._check(self._L.cof_batch_size(self._h, ctypes.byref(n)))
+        return n.value
+
+    def job_rows(self, job) -> bytes:
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self._L.cof_job_rows(self._h, job, ctypes.byref(p), ctypes.byref(n)))
+        return ctypes.string_at(p.value, n.value) if n.value else b""
+
+    def job_summary(self, job) -> bytes:
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self._L.cof_job_summary_text(self._h, job, ctypes.byref(p), ctypes.byref(n)))
+        return ctypes.string_at(p.value, n.value) if n.value else b""
 
     def last_hit_count(self):
         a, b = ctypes.c_uint64(), ctypes.c_uint64()

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/cof.h"
+#include "../../include/cof_tools.h"
 #include "cof_internal.h"
 #include "kernels.cuh"
 
@@ -97,6 +98,18 @@ struct KernelStat {
   double units = 0;
 };
 
+// Compare variants (of one or more jobs) that share one padded pattern.
+struct PatternGroup {
+  std::string pattern;
+  uint32_t L = 0;
+  FinderPattern fpat{};
+  int nw = 1;                  // 32-bit words per window (popcount comparer)
+  int bs_slots = 0;            // bit-sliced slot count, 0 = popcount comparer
+  std::vector<uint32_t> gids;  // global variant ids, ascending
+  double nonN_sum = 0;         // sum of non-N positions over the group's variants
+  DevBuf vmask, bs_off, bs_thr, bs_gid;
+};
+
 }  // namespace
 
 struct cof_handle {
@@ -107,25 +120,25 @@ struct cof_handle {
   cudaEvent_t ev_start = nullptr, ev_found[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
   std::string err;
 
-  Job job;
-  bool has_job = false;
-  bool job_on_device = false;
-  int nw = 1;
-  std::vector<uint32_t> nonN;  // non-N positions per variant
-  DevBuf vmask, vfmt, sfmt, pool;
-  DevBuf bs_off, bs_thr, bs_gid;  // bit-sliced comparer tables
-  int bs_slots = 0;               // 0: use the popcount comparer
+  // The batch: one or more parsed input files ("jobs").  Variant ids are
+  // global and job-major (job j owns [job_gid0[j], job_gid0[j+1])), so one
+  // sort of the hit keys yields every job's rows contiguously, in job order.
+  std::vector<Job> jobs;
+  std::vector<uint32_t> job_gid0;
+  bool jobs_on_device = false;
   bool force_popc = false;
-  FinderPattern fpat{};
-
+  std::vector<PatternGroup> groups;  // jobs sharing a padded pattern share finder + comparer passes
+  DevBuf vfmt, sfmt, pool;           // row formatting tables over all variants
   DevGenome genome, scratch;
 
-  DevBuf queue[2], qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small;
+  DevBuf queue[2], qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small,
+      job_start, job_bytes;
   HostPinned host_text;
   std::string summary_text;
-  std::map<std::string, unsigned long long> summary;
+  std::vector<std::map<std::string, unsigned long long>> summaries;  // per job
   bool summary_on = false;
   uint64_t last_hits = 0, last_rows = 0;
+  std::vector<uint64_t> job_byte0;  // row text of job j: [job_byte0[j], job_byte0[j+1]) of host_text
 
   bool profiling = false;
   std::map<std::string, KernelStat> stats;
@@ -252,98 +265,138 @@ void fill_mask(VariantMask<NW>& vm, const std::string& comp, uint32_t thr, uint3
   vm.gid = gid;
 }
 
-// Uploads the variant masks and formatting tables of the current job.
-cof_status upload_job(cof_handle* h) {
-  if (h->job_on_device) return COF_OK;
-  const Job& job = h->job;
-  const size_t L = job.pattern.size();
-  if (L > (size_t)kMaxL)
-    return fail(h, COF_ERR_UNSUPPORTED, "pattern length " + std::to_string(L) + " exceeds " + std::to_string(kMaxL));
-  if (job.variants.size() >= (1u << 20)) return fail(h, COF_ERR_UNSUPPORTED, "more than 2^20 compare variants");
-  h->nw = L <= 32 ? 1 : 2;
-  make_finder_pattern(job.pattern, revcomp(job.pattern), h->fpat);
-  const size_t V = job.variants.size();
-  h->nonN.assign(V, 0);
-  std::vector<unsigned char> masks;
-  const size_t msz = h->nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>);
-  masks.resize(std::max<size_t>(V, 1) * msz);
+// Builds the pattern groups and uploads every variant's comparer and
+// formatting tables for the current batch.
+cof_status upload_jobs(cof_handle* h) {
+  if (h->jobs_on_device) return COF_OK;
+  h->groups.clear();
+  h->job_gid0.assign(1, 0);
+  for (const Job& job : h->jobs) {
+    if (job.pattern.size() > (size_t)kMaxL)
+      return fail(h, COF_ERR_UNSUPPORTED,
+                  "pattern length " + std::to_string(job.pattern.size()) + " exceeds " + std::to_string(kMaxL));
+    h->job_gid0.push_back(h->job_gid0.back() + (uint32_t)job.variants.size());
+  }
+  const uint64_t total = h->job_gid0.back();
+  if (total >= (1u << 20)) return fail(h, COF_ERR_UNSUPPORTED, "more than 2^20 compare variants in one batch");
+  std::map<std::string, size_t> group_of;
+  std::vector<const Variant*> var_of(total);
+  std::vector<uint32_t> L_of(total);
+  for (size_t j = 0; j < h->jobs.size(); ++j) {
+    const Job& job = h->jobs[j];
+    auto it = group_of.find(job.pattern);
+    if (it == group_of.end()) {
+      it = group_of.emplace(job.pattern, h->groups.size()).first;
+      h->groups.emplace_back();
+      PatternGroup& g = h->groups.back();
+      g.pattern = job.pattern;
+      g.L = (uint32_t)job.pattern.size();
+      g.nw = g.L <= 32 ? 1 : 2;
+      make_finder_pattern(job.pattern, revcomp(job.pattern), g.fpat);
+    }
+    PatternGroup& g = h->groups[it->second];
+    for (size_t v = 0; v < job.variants.size(); ++v) {
+      const uint32_t gid = h->job_gid0[j] + (uint32_t)v;
+      g.gids.push_back(gid);
+      var_of[gid] = &job.variants[v];
+      L_of[gid] = g.L;
+    }
+  }
+  // Formatting tables over all variants.
   std::string pool;
-  std::vector<VariantFmt> vf(V);
+  std::vector<VariantFmt> vf(total);
   std::vector<ShapeFmt> sf;
-  auto put = [&](const std::string& s) {
+  auto put = [&](const std::string& str) {
     const uint32_t o = (uint32_t)pool.size();
-    pool += s;
+    pool += str;
     return o;
   };
-  for (size_t v = 0; v < V; ++v) {
-    const Variant& var = job.variants[v];
-    for (char c : var.key) h->nonN[v] += c != 'N';
-    if (h->nw == 1) fill_mask<1>(((VariantMask<1>*)masks.data())[v], var.key, var.threshold, (uint32_t)v);
-    else fill_mask<2>(((VariantMask<2>*)masks.data())[v], var.key, var.threshold, (uint32_t)v);
-    vf[v].comp_off = put(var.key);
-    vf[v].L = (uint32_t)L;
-    for (int s = 0; s < 2; ++s) {
-      vf[v].shape_begin[s] = (uint32_t)sf.size();
-      for (const RowShape& r : job.shapes[s][v]) {
-        ShapeFmt f;
-        f.head_off = put(r.head);
-        f.head_len = (uint32_t)r.head.size();
-        f.dna_off = put(r.dna);
-        f.dna_len = (uint32_t)r.dna.size();
-        f.tail_off = put(r.tail);
-        f.tail_len = (uint32_t)r.tail.size();
-        f.offset = r.offset;
-        f.dir = s ? '-' : '+';
-        sf.push_back(f);
+  for (size_t j = 0; j < h->jobs.size(); ++j) {
+    const Job& job = h->jobs[j];
+    for (size_t v = 0; v < job.variants.size(); ++v) {
+      const uint32_t gid = h->job_gid0[j] + (uint32_t)v;
+      vf[gid].comp_off = put(job.variants[v].key);
+      vf[gid].L = (uint32_t)job.pattern.size();
+      for (int st = 0; st < 2; ++st) {
+        vf[gid].shape_begin[st] = (uint32_t)sf.size();
+        for (const RowShape& r : job.shapes[st][v]) {
+          ShapeFmt f;
+          f.head_off = put(r.head);
+          f.head_len = (uint32_t)r.head.size();
+          f.dna_off = put(r.dna);
+          f.dna_len = (uint32_t)r.dna.size();
+          f.tail_off = put(r.tail);
+          f.tail_len = (uint32_t)r.tail.size();
+          f.offset = r.offset;
+          f.dir = st ? '-' : '+';
+          sf.push_back(f);
+        }
+        vf[gid].shape_end[st] = (uint32_t)sf.size();
       }
-      vf[v].shape_end[s] = (uint32_t)sf.size();
     }
   }
-  // Bit-sliced comparer tables: per variant, the positions that can mismatch
-  // as offsets of their class word in the shared-memory table.
-  int maxpos = 0;
-  for (const Variant& var : job.variants) {
-    int c = 0;
-    for (char ch : var.key) c += bs_class_of((unsigned char)ch) != 0;
-    maxpos = std::max(maxpos, c);
-  }
-  h->bs_slots = h->force_popc ? 0 : bs_slots_for(maxpos);
-  if (h->bs_slots) {
-    const int S = h->bs_slots;
-    const uint32_t row = (uint32_t)bs_row_for((uint32_t)L);
-    std::vector<uint32_t> off(std::max<size_t>(V, 1) * (S / 2), 0), thr(std::max<size_t>(V, 1), 0),
-        gid(std::max<size_t>(V, 1), 0);
-    for (size_t v = 0; v < V; ++v) {
-      const std::string& key = job.variants[v].key;
-      int s = 0;
-      for (size_t k = 0; k < key.size(); ++k) {
-        const uint32_t c = bs_class_of((unsigned char)key[k]);
-        if (!c) continue;
-        const uint32_t byte_off = (c * row + (uint32_t)k) * 8;  // uint2 table element (two groups)
-        off[v * (S / 2) + s / 2] |= byte_off << (16 * (s & 1));
-        ++s;
+  if (pool.size() >= (1ull << 32)) return fail(h, COF_ERR_UNSUPPORTED, "row tables exceed 4 GB");
+  // Comparer tables per group.
+  for (PatternGroup& g : h->groups) {
+    const size_t V = g.gids.size();
+    const size_t msz = g.nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>);
+    std::vector<unsigned char> masks(std::max<size_t>(V, 1) * msz, 0);
+    int maxpos = 0;
+    g.nonN_sum = 0;
+    for (size_t i = 0; i < V; ++i) {
+      const Variant& var = *var_of[g.gids[i]];
+      if (g.nw == 1) fill_mask<1>(((VariantMask<1>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
+      else fill_mask<2>(((VariantMask<2>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
+      int c = 0;
+      for (char ch : var.key) {
+        c += bs_class_of((unsigned char)ch) != 0;
+        g.nonN_sum += ch != 'N';
       }
-      thr[v] = job.variants[v].threshold;
-      gid[v] = (uint32_t)v;
+      maxpos = std::max(maxpos, c);
     }
-    COF_CUDA(h, h->bs_off.ensure(off.size() * 4));
-    COF_CUDA(h, h->bs_thr.ensure(thr.size() * 4));
-    COF_CUDA(h, h->bs_gid.ensure(gid.size() * 4));
-    COF_CUDA(h, cudaMemcpyAsync(h->bs_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    COF_CUDA(h, cudaMemcpyAsync(h->bs_thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    COF_CUDA(h, cudaMemcpyAsync(h->bs_gid.p, gid.data(), gid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, g.vmask.ensure(masks.size()));
+    COF_CUDA(h, cudaMemcpyAsync(g.vmask.p, masks.data(), masks.size(), cudaMemcpyHostToDevice, h->stream));
+    g.bs_slots = h->force_popc ? 0 : bs_slots_for(maxpos);
+    if (g.bs_slots) {
+      // Per variant, the positions that can mismatch as byte offsets of their
+      // class word in the comparer's shared-memory table.
+      const int S = g.bs_slots;
+      const uint32_t row = (uint32_t)bs_row_for(g.L);
+      std::vector<uint32_t> off(std::max<size_t>(V, 1) * (S / 2), 0), thr(std::max<size_t>(V, 1), 0),
+          gid(std::max<size_t>(V, 1), 0);
+      for (size_t i = 0; i < V; ++i) {
+        const Variant& var = *var_of[g.gids[i]];
+        int sl = 0;
+        for (size_t k = 0; k < var.key.size(); ++k) {
+          const uint32_t c = bs_class_of((unsigned char)var.key[k]);
+          if (!c) continue;
+          const uint32_t byte_off = (c * row + (uint32_t)k) * 8;  // uint2 table element (two groups)
+          off[i * (S / 2) + sl / 2] |= byte_off << (16 * (sl & 1));
+          ++sl;
+        }
+        thr[i] = var.threshold;
+        gid[i] = g.gids[i];
+      }
+      COF_CUDA(h, g.bs_off.ensure(off.size() * 4));
+      COF_CUDA(h, g.bs_thr.ensure(thr.size() * 4));
+      COF_CUDA(h, g.bs_gid.ensure(gid.size() * 4));
+      COF_CUDA(h, cudaMemcpyAsync(g.bs_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, h->stream));
+      COF_CUDA(h, cudaMemcpyAsync(g.bs_thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, h->stream));
+      COF_CUDA(h, cudaMemcpyAsync(g.bs_gid.p, gid.data(), gid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    }
+    // The host vectors die at the end of this iteration: wait for the copies.
+    COF_CUDA(h, cudaStreamSynchronize(h->stream));
   }
-  COF_CUDA(h, h->vmask.ensure(masks.size()));
-  COF_CUDA(h, h->vfmt.ensure(std::max<size_t>(V, 1) * sizeof(VariantFmt)));
+  COF_CUDA(h, h->vfmt.ensure(std::max<size_t>(total, 1) * sizeof(VariantFmt)));
   COF_CUDA(h, h->sfmt.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
   COF_CUDA(h, h->pool.ensure(std::max<size_t>(pool.size(), 1)));
-  COF_CUDA(h, cudaMemcpyAsync(h->vmask.p, masks.data(), masks.size(), cudaMemcpyHostToDevice, h->stream));
-  if (V) COF_CUDA(h, cudaMemcpyAsync(h->vfmt.p, vf.data(), V * sizeof(VariantFmt), cudaMemcpyHostToDevice, h->stream));
+  if (total)
+    COF_CUDA(h, cudaMemcpyAsync(h->vfmt.p, vf.data(), total * sizeof(VariantFmt), cudaMemcpyHostToDevice, h->stream));
   if (!sf.empty())
     COF_CUDA(h, cudaMemcpyAsync(h->sfmt.p, sf.data(), sf.size() * sizeof(ShapeFmt), cudaMemcpyHostToDevice, h->stream));
   if (!pool.empty()) COF_CUDA(h, cudaMemcpyAsync(h->pool.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, h->stream));
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
-  h->job_on_device = true;
+  h->jobs_on_device = true;
   return COF_OK;
 }
 
@@ -385,63 +438,80 @@ void collect(cof_handle* h, std::vector<EventPair>& evs) {
   evs.clear();
 }
 
-// Finder + comparer over the whole genome; leaves the hit count in h->hit_count.
-// Segment s is scanned on stream2 into queue[s % 2] while the comparer works
-// on segment s - 1 on the main stream; events order the two.
+// Finder + comparer over the whole genome for every pattern group; leaves the
+// hit count in h->hit_count.  Pass i = (segment s, group g) scans on stream2
+// into queue[i % 2] while the comparer works on pass i - 1 on the main
+// stream; events order the two.  qcounts[s * groups + g] keeps each pass's
+// candidate count.
 cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& evs, uint64_t* seg_count) {
   const DevGenome& dg = h->genome;
   const GenomeView gv = dg.view();
-  const uint64_t L = h->job.pattern.size();
-  const uint64_t npos = dg.n >= L ? dg.n - L + 1 : 0;
-  const uint64_t total_words = (npos + 31) / 32;
-  const uint64_t nseg = (total_words + kSegWords - 1) / kSegWords;
+  const size_t G = h->groups.size();
+  uint64_t max_words = 0;
+  for (const PatternGroup& g : h->groups) {
+    const uint64_t npos = dg.n >= g.L ? dg.n - g.L + 1 : 0;
+    max_words = std::max(max_words, (npos + 31) / 32);
+  }
+  const uint64_t nseg = (max_words + kSegWords - 1) / kSegWords;
   *seg_count = nseg;
-  COF_CUDA(h, h->qcounts.ensure(std::max<uint64_t>(nseg, 1) * 4));
-  COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<uint64_t>(nseg, 1) * 4, h->stream));
+  const uint64_t nq = std::max<uint64_t>(nseg * G, 1);
+  COF_CUDA(h, h->qcounts.ensure(nq * 4));
+  COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, nq * 4, h->stream));
   COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
   COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
   COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
-  const uint32_t V = (uint32_t)h->job.variants.size();
+  uint64_t pass = 0;
   for (uint64_t s = 0; s < nseg; ++s) {
-    const int b = (int)(s & 1);
-    const uint64_t w0 = s * kSegWords, w1 = std::min(total_words, w0 + kSegWords);
-    uint32_t* qc = h->qcounts.as<uint32_t>() + s;
-    uint32_t* q = h->queue[b].as<uint32_t>();
-    if (s >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
-    cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32, h->stream2);
-    if (st) return st;
-    launch_finder(gv, w0, w1, h->fpat, q, qc, h->stream2);
-    if ((st = record_stop(h, evs, h->stream2))) return st;
-    COF_CUDA(h, cudaEventRecord(h->ev_found[b], h->stream2));
-    COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_found[b], 0));
-    if ((st = record_start(h, evs, "comparer", 0, h->stream))) return st;
-    if (!h->bs_slots ||
-        !launch_comparer_bs(gv, q, qc, w0 * 32, h->bs_off.as<uint32_t>(), h->bs_thr.as<uint32_t>(),
-                            h->bs_gid.as<uint32_t>(), V, h->bs_slots, (uint32_t)L, h->hits.as<uint64_t>(),
-                            h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream))
-      launch_comparer(gv, q, qc, w0 * 32, h->vmask.p, V, h->nw, (uint32_t)L, h->hits.as<uint64_t>(),
-                      h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream);
-    if ((st = record_stop(h, evs, h->stream))) return st;
-    COF_CUDA(h, cudaEventRecord(h->ev_used[b], h->stream));
+    for (size_t gi = 0; gi < G; ++gi) {
+      const PatternGroup& g = h->groups[gi];
+      const uint64_t npos = dg.n >= g.L ? dg.n - g.L + 1 : 0;
+      const uint64_t words = (npos + 31) / 32;
+      const uint64_t w0 = s * kSegWords, w1 = std::min(words, w0 + kSegWords);
+      if (w0 >= w1 || g.gids.empty()) continue;
+      const int b = (int)(pass & 1);
+      uint32_t* qc = h->qcounts.as<uint32_t>() + s * G + gi;
+      uint32_t* q = h->queue[b].as<uint32_t>();
+      if (pass >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
+      cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32, h->stream2);
+      if (st) return st;
+      launch_finder(gv, w0, w1, g.fpat, q, qc, h->stream2);
+      if ((st = record_stop(h, evs, h->stream2))) return st;
+      COF_CUDA(h, cudaEventRecord(h->ev_found[b], h->stream2));
+      COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_found[b], 0));
+      // Comparer units are filled in from qcounts after the search.
+      if ((st = record_start(h, evs, "comparer", (double)(s * G + gi), h->stream))) return st;
+      const uint32_t V = (uint32_t)g.gids.size();
+      if (!g.bs_slots ||
+          !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_off.as<uint32_t>(), g.bs_thr.as<uint32_t>(),
+                              g.bs_gid.as<uint32_t>(), V, g.bs_slots, g.L, h->hits.as<uint64_t>(),
+                              h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream))
+        launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, h->hits.as<uint64_t>(),
+                        h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream);
+      if ((st = record_stop(h, evs, h->stream))) return st;
+      COF_CUDA(h, cudaEventRecord(h->ev_used[b], h->stream));
+      ++pass;
+    }
   }
+  // Join stream2 into the main stream (it may end with a finder whose
+  // comparer was skipped; normally the last comparer already waited on it).
+  COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream2));
+  COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_start, 0));
   COF_CUDA(h, cudaGetLastError());
   return COF_OK;
 }
 
 cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
-  if (!h->has_job) return fail(h, COF_ERR_STATE, "no input file has been read");
+  if (h->jobs.empty()) return fail(h, COF_ERR_STATE, "no input file has been read");
   if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
-  cof_status st = upload_job(h);
+  cof_status st = upload_jobs(h);
   if (st) return st;
-  *rows = nullptr;
+  const size_t J = h->jobs.size();
+  *rows = "";
   *rows_len = 0;
   h->last_hits = h->last_rows = 0;
-  const uint64_t V = h->job.variants.size();
-  const uint64_t L = h->job.pattern.size();
-  if (V == 0 || h->genome.n < L) {
-    *rows = "";
-    return COF_OK;
-  }
+  h->job_byte0.assign(J + 1, 0);
+  if (h->summaries.size() != J) h->summaries.assign(J, {});
+  if (h->job_gid0.back() == 0) return COF_OK;
   COF_CUDA(h, h->queue[0].ensure(2 * kSegPositions * 4));
   COF_CUDA(h, h->queue[1].ensure(2 * kSegPositions * 4));
   COF_CUDA(h, h->hit_count.ensure(8));
@@ -454,36 +524,39 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
     COF_CUDA(h, cudaMemcpyAsync(&nhits, h->hit_count.p, 8, cudaMemcpyDeviceToHost, h->stream));
     COF_CUDA(h, cudaStreamSynchronize(h->stream));
     if (nhits <= cap) break;
-    collect(h, evs);  // the overflowing pass counts as work done
+    for (EventPair& p : evs) {  // discard the overflowing pass's timings
+      cudaEventDestroy(p.a);
+      cudaEventDestroy(p.b);
+    }
+    evs.clear();
     cap = nhits + nhits / 8;
     COF_CUDA(h, h->hits.ensure(cap * 8));
   }
   if (h->profiling) {
-    // Comparer units: base comparisons = oriented candidates x non-N variant positions.
-    std::vector<uint32_t> qc(nseg);
-    COF_CUDA(h, cudaMemcpy(qc.data(), h->qcounts.p, nseg * 4, cudaMemcpyDeviceToHost));
-    double nonN = 0;
-    for (uint32_t x : h->nonN) nonN += x;
-    size_t si = 0;
+    // Comparer units: base comparisons = oriented candidates x non-N positions
+    // of each variant; variant tests go to "comparer.tests".
+    const size_t G = h->groups.size();
+    std::vector<uint32_t> qc(std::max<uint64_t>(nseg * G, 1), 0);
+    COF_CUDA(h, cudaMemcpy(qc.data(), h->qcounts.p, nseg * G * 4, cudaMemcpyDeviceToHost));
     for (EventPair& p : evs)
-      if (p.name == "comparer" && si < nseg) p.units = (double)qc[si++] * nonN;
-    // Variant tests (oriented candidate x variant) under "comparer.tests".
-    double cands = 0;
-    for (uint32_t x : qc) cands += x;
-    h->stats["comparer.tests"].units += cands * (double)h->job.variants.size();
+      if (p.name == "comparer") {
+        const size_t idx = (size_t)p.units;
+        const PatternGroup& g = h->groups[idx % G];
+        p.units = (double)qc[idx] * g.nonN_sum;
+        h->stats["comparer.tests"].units += (double)qc[idx] * (double)g.gids.size();
+      }
     collect(h, evs);
   }
   h->last_hits = nhits;
-  if (nhits == 0) {
-    *rows = "";
-    return COF_OK;
-  }
+  if (nhits == 0) return COF_OK;
   // Sort hit keys into output order.
   COF_CUDA(h, h->hits_sorted.ensure(nhits * 8));
   COF_CUDA(h, h->row_bytes.ensure(nhits * 8));
   COF_CUDA(h, h->row_offsets.ensure(nhits * 8));
   COF_CUDA(h, h->row_count.ensure(nhits * 4));
   COF_CUDA(h, h->small.ensure(64));
+  COF_CUDA(h, h->job_start.ensure((J + 1) * 4));
+  COF_CUDA(h, h->job_bytes.ensure((J + 1) * 8));
   size_t tmp = 0;
   COF_CUDA(h, cub::DeviceRadixSort::SortKeys(nullptr, tmp, h->hits.as<uint64_t>(), h->hits_sorted.as<uint64_t>(),
                                              (int64_t)nhits, 0, 64, h->stream));
@@ -497,7 +570,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   tmp = h->sort_tmp.cap;
   COF_CUDA(h, cub::DeviceRadixSort::SortKeys(h->sort_tmp.p, tmp, h->hits.as<uint64_t>(), h->hits_sorted.as<uint64_t>(),
                                              (int64_t)nhits, 0, 64, h->stream));
-  // Row sizes, offsets, then the rows themselves.
+  // Row sizes, offsets, per-job byte ranges, then the rows themselves.
   const GenomeView gv = h->genome.view();
   FormatTables ft{h->vfmt.as<VariantFmt>(), h->sfmt.as<ShapeFmt>(), h->pool.as<char>()};
   if ((st = record_start(h, evs, "format", (double)nhits, h->stream))) return st;
@@ -509,13 +582,15 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   tmp = h->sort_tmp.cap;
   COF_CUDA(h, cub::DeviceReduce::Sum(h->sort_tmp.p, tmp, h->row_count.as<uint32_t>(), h->small.as<uint64_t>(),
                                      (int64_t)nhits, h->stream));
-  uint64_t tail[3] = {0, 0, 0};
-  COF_CUDA(h, cudaMemcpyAsync(&tail[0], h->row_offsets.as<uint64_t>() + nhits - 1, 8, cudaMemcpyDeviceToHost,
-                              h->stream));
-  COF_CUDA(h, cudaMemcpyAsync(&tail[1], h->row_bytes.as<uint64_t>() + nhits - 1, 8, cudaMemcpyDeviceToHost, h->stream));
-  COF_CUDA(h, cudaMemcpyAsync(&tail[2], h->small.p, 8, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(h->job_start.p, h->job_gid0.data(), (J + 1) * 4, cudaMemcpyHostToDevice, h->stream));
+  launch_job_bounds(h->hits_sorted.as<uint64_t>(), nhits, h->job_start.as<uint32_t>(), (uint32_t)J,
+                    h->row_offsets.as<uint64_t>(), h->row_bytes.as<uint64_t>(), h->job_bytes.as<uint64_t>(),
+                    h->stream);
+  COF_CUDA(h, cudaMemcpyAsync(h->job_byte0.data(), h->job_bytes.p, (J + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
+  uint64_t nrows = 0;
+  COF_CUDA(h, cudaMemcpyAsync(&nrows, h->small.p, 8, cudaMemcpyDeviceToHost, h->stream));
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
-  const uint64_t bytes = tail[0] + tail[1];
+  const uint64_t bytes = h->job_byte0[J];
   COF_CUDA(h, h->text.ensure(bytes + 1));
   launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), h->text.as<char>(),
                     h->stream);
@@ -526,23 +601,43 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
   ((char*)h->host_text.p)[bytes] = 0;
   collect(h, evs);
-  h->last_rows = tail[2];
+  h->last_rows = nrows;
   if (h->summary_on) {
     std::vector<uint64_t> keys(nhits);
     COF_CUDA(h, cudaMemcpy(keys.data(), h->hits_sorted.p, nhits * 8, cudaMemcpyDeviceToHost));
     for (uint64_t k : keys) {
       const uint32_t gid = (uint32_t)(k >> 44), strand = (uint32_t)((k >> 7) & 1), mm = (uint32_t)(k & 0x7F);
-      const Variant& var = h->job.variants[gid];
-      for (const RowShape& r : h->job.shapes[strand][gid]) {
+      const size_t j = (size_t)(std::upper_bound(h->job_gid0.begin(), h->job_gid0.end(), gid) - h->job_gid0.begin()) - 1;
+      const uint32_t v = gid - h->job_gid0[j];
+      const Variant& var = h->jobs[j].variants[v];
+      for (const RowShape& r : h->jobs[j].shapes[strand][v]) {
         char key[10000];
         snprintf(key, sizeof key, "%s,%s,%d,%d", var.id.c_str(), r.type.c_str(), (int)r.bulge_size, (int)mm);
-        ++h->summary[key];
+        ++h->summaries[j][key];
       }
     }
   }
   *rows = (const char*)h->host_text.p;
   *rows_len = bytes;
   return COF_OK;
+}
+
+std::string summary_of(const std::map<std::string, unsigned long long>& table) {
+  static const char* kHead[4] = {"Id", "Bulge Type", "Bulge Size", "Mismatches"};
+  std::string out;
+  for (const auto& kv : table) {
+    std::string key = kv.first;
+    out += "##";
+    size_t cut;
+    int col = 0;
+    while ((cut = key.find(',')) != std::string::npos && col < 3) {
+      out += std::string(kHead[col++]) + "=" + key.substr(0, cut) + ";";
+      key.erase(0, cut + 1);
+    }
+    out += std::string(kHead[col]) + "=" + key + ";";
+    out += "Number of Found Targets=" + std::to_string(kv.second) + "\n";
+  }
+  return out;
 }
 
 }  // namespace
@@ -618,25 +713,67 @@ cof_status cof_read_input(cof_handle* h, const char* text, size_t len) {
   std::string err;
   if (!parse_job(text ? text : "", len, job, err)) return fail(h, COF_ERR_INPUT, err);
   if (!build_shapes(job, err)) return fail(h, COF_ERR_INPUT, err);
-  h->job = std::move(job);
-  h->has_job = true;
-  h->job_on_device = false;
-  h->summary.clear();
+  h->jobs.clear();
+  h->jobs.push_back(std::move(job));
+  h->jobs_on_device = false;
+  h->summaries.assign(1, {});
+  h->job_byte0.clear();
   return COF_OK;
 }
 
-const char* cof_genome_path(const cof_handle* h) { return (h && h->has_job) ? h->job.genome_path.c_str() : ""; }
+cof_status cof_batch_clear(cof_handle* h) {
+  if (!h) return COF_ERR_ARG;
+  h->jobs.clear();
+  h->summaries.clear();
+  h->job_byte0.clear();
+  h->jobs_on_device = false;
+  return COF_OK;
+}
+
+cof_status cof_batch_add_input(cof_handle* h, const char* text, size_t len, uint32_t* job_index) {
+  if (!h || (!text && len)) return COF_ERR_ARG;
+  h->err.clear();
+  Job job;
+  std::string err;
+  if (!parse_job(text ? text : "", len, job, err)) return fail(h, COF_ERR_INPUT, err);
+  if (!build_shapes(job, err)) return fail(h, COF_ERR_INPUT, err);
+  if (job_index) *job_index = (uint32_t)h->jobs.size();
+  h->jobs.push_back(std::move(job));
+  h->summaries.emplace_back();
+  h->job_byte0.clear();
+  h->jobs_on_device = false;
+  return COF_OK;
+}
+
+cof_status cof_batch_size(const cof_handle* h, uint32_t* n_jobs) {
+  if (!h || !n_jobs) return COF_ERR_ARG;
+  *n_jobs = (uint32_t)h->jobs.size();
+  return COF_OK;
+}
+
+cof_status cof_job_rows(const cof_handle* h, uint32_t job, const char** rows, size_t* rows_len) {
+  if (!h || !rows || !rows_len) return COF_ERR_ARG;
+  if (job >= h->jobs.size() || h->job_byte0.size() != h->jobs.size() + 1) return COF_ERR_STATE;
+  *rows = h->host_text.p ? (const char*)h->host_text.p + h->job_byte0[job] : "";
+  *rows_len = h->job_byte0[job + 1] - h->job_byte0[job];
+  return COF_OK;
+}
+
+const char* cof_genome_path(const cof_handle* h) {
+  return (h && !h->jobs.empty()) ? h->jobs[0].genome_path.c_str() : "";
+}
 
 cof_status cof_input_info(const cof_handle* h, uint32_t* pattern_len, uint32_t* n_variants, uint32_t* n_bulge_records) {
   if (!h) return COF_ERR_ARG;
-  if (!h->has_job) return COF_ERR_STATE;
-  if (pattern_len) *pattern_len = (uint32_t)h->job.pattern.size();
-  if (n_variants) *n_variants = (uint32_t)h->job.variants.size();
-  if (n_bulge_records) {
-    uint32_t n = 0;
-    for (const Variant& v : h->job.variants) n += (uint32_t)v.bulges.size();
-    *n_bulge_records = n;
+  if (h->jobs.empty()) return COF_ERR_STATE;
+  if (pattern_len) *pattern_len = (uint32_t)h->jobs[0].pattern.size();
+  uint32_t nv = 0, nb = 0;
+  for (const Job& j : h->jobs) {
+    nv += (uint32_t)j.variants.size();
+    for (const Variant& v : j.variants) nb += (uint32_t)v.bulges.size();
   }
+  if (n_variants) *n_variants = nv;
+  if (n_bulge_records) *n_bulge_records = nb;
   return COF_OK;
 }
 
@@ -716,22 +853,12 @@ cof_status cof_set_summary(cof_handle* h, int enable) {
 }
 
 cof_status cof_summary_text(cof_handle* h, const char** text, size_t* len) {
+  return cof_job_summary_text(h, 0, text, len);
+}
+
+cof_status cof_job_summary_text(cof_handle* h, uint32_t job, const char** text, size_t* len) {
   if (!h || !text || !len) return COF_ERR_ARG;
-  static const char* kHead[4] = {"Id", "Bulge Type", "Bulge Size", "Mismatches"};
-  std::string out;
-  for (const auto& kv : h->summary) {
-    std::string key = kv.first;
-    out += "##";
-    size_t cut;
-    int col = 0;
-    while ((cut = key.find(',')) != std::string::npos && col < 3) {
-      out += std::string(kHead[col++]) + "=" + key.substr(0, cut) + ";";
-      key.erase(0, cut + 1);
-    }
-    out += std::string(kHead[col]) + "=" + key + ";";
-    out += "Number of Found Targets=" + std::to_string(kv.second) + "\n";
-  }
-  h->summary_text = out;
+  h->summary_text = job < h->summaries.size() ? summary_of(h->summaries[job]) : std::string();
   *text = h->summary_text.c_str();
   *len = h->summary_text.size();
   return COF_OK;
@@ -861,6 +988,15 @@ cof_status cof_comparer_chunk(cof_handle* h, const char* chr, uint64_t chrlen, c
 
 uint64_t cof_plane_words(uint64_t n) { return plane_words(n); }
 
+void cofx_mismatch_table(uint8_t* out) {
+  if (!out) return;
+  for (int p = 0; p < 256; ++p)
+    for (int g = 0; g < 256; ++g) {
+      const int cls = g == 'T' ? 0 : g == 'C' ? 1 : g == 'A' ? 2 : g == 'G' ? 3 : 4;
+      out[p * 256 + g] = (uint8_t)((class_bits_of((unsigned char)p) >> cls) & 1u);
+    }
+}
+
 uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, uint32_t* ot, uint64_t* exc_pos,
                        uint8_t* exc_byte) {
   std::vector<uint64_t> ep;
@@ -881,14 +1017,19 @@ uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, 
 cof_status cof_set_comparer(cof_handle* h, int kind) {
   if (!h || kind < 0 || kind > 2) return COF_ERR_ARG;
   h->force_popc = kind == 1;
-  h->job_on_device = false;  // rebuild the comparer tables on the next search
+  h->jobs_on_device = false;  // rebuild the comparer tables on the next search
   return COF_OK;
 }
 
 cof_status cof_comparer_info(const cof_handle* h, int* kind, int* slots) {
   if (!h) return COF_ERR_ARG;
-  if (kind) *kind = h->bs_slots ? 2 : 1;
-  if (slots) *slots = h->bs_slots;
+  int k = 0, sl = 0;
+  for (const PatternGroup& g : h->groups) {
+    k = std::max(k, g.bs_slots ? 2 : 1);
+    sl = std::max(sl, g.bs_slots);
+  }
+  if (kind) *kind = k ? k : 1;
+  if (slots) *slots = sl;
   return COF_OK;
 }
 

@@ -396,4 +396,31 @@ void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64
   write_rows_kernel<<<(unsigned)((n_hits + 127) / 128), 128, 0, stream>>>(g, ft, hits, n_hits, offsets, out);
 }
 
+// Byte offset of each job's first row: job j's hits start at the first sorted
+// key whose variant id is >= job_gid0[j]; out[J] = total bytes.
+__global__ void job_bounds_kernel(const uint64_t* __restrict__ sorted, uint64_t n, const uint32_t* __restrict__ job_gid0,
+                                  uint32_t njobs, const uint64_t* __restrict__ offsets,
+                                  const uint64_t* __restrict__ row_bytes, uint64_t* __restrict__ out) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > njobs) return;
+  const uint64_t total = n ? offsets[n - 1] + row_bytes[n - 1] : 0;
+  if (j == njobs) {
+    out[j] = total;
+    return;
+  }
+  const uint64_t key = (uint64_t)job_gid0[j] << 44;
+  uint64_t a = 0, z = n;
+  while (a < z) {
+    const uint64_t mid = (a + z) >> 1;
+    if (sorted[mid] < key) a = mid + 1;
+    else z = mid;
+  }
+  out[j] = a < n ? offsets[a] : total;
+}
+
+void launch_job_bounds(const uint64_t* sorted, uint64_t n, const uint32_t* job_gid0, uint32_t njobs,
+                       const uint64_t* offsets, const uint64_t* row_bytes, uint64_t* out, cudaStream_t stream) {
+  job_bounds_kernel<<<(njobs + 1 + 127) / 128, 128, 0, stream>>>(sorted, n, job_gid0, njobs, offsets, row_bytes, out);
+}
+
 }  // namespace cof

@@ -125,4 +125,9 @@ void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint6
 void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
                        const uint64_t* offsets, char* out, cudaStream_t stream);
 
+// Per job (global variant ids job_gid0[j] .. job_gid0[j+1]), the byte offset
+// of its first row in the formatted text; out[njobs] = total bytes.
+void launch_job_bounds(const uint64_t* sorted, uint64_t n, const uint32_t* job_gid0, uint32_t njobs,
+                       const uint64_t* offsets, const uint64_t* row_bytes, uint64_t* out, cudaStream_t stream);
+
 }  // namespace cof

@@ -102,6 +102,19 @@ cof_status cof_genome_info(const cof_handle* h, uint64_t* n, uint32_t* n_records
  *      `*rows` points into a buffer owned by the handle, valid until the next
  *      search or cof_close. */
 cof_status cof_search(cof_handle* h, const char** rows, size_t* rows_len);
+/* ---- batched search: several input files ("jobs") over the resident genome
+ * in one pass.  Jobs whose padded patterns are equal share one PAM scan and
+ * one comparer launch per genome segment; each job keeps its own compare
+ * variants (no key merging across jobs), ids, thresholds and rows, exactly as
+ * if it were searched alone.  cof_read_input replaces the batch by a single
+ * job; cof_batch_add_input appends one (its `genome path` line is ignored:
+ * the batch searches the resident genome).  cof_search then searches every
+ * job and returns the rows of all jobs concatenated in job order;
+ * cof_job_rows gives one job's rows (valid until the next search). */
+cof_status cof_batch_clear(cof_handle* h);
+cof_status cof_batch_add_input(cof_handle* h, const char* text, size_t len, uint32_t* job_index);
+cof_status cof_batch_size(const cof_handle* h, uint32_t* n_jobs);
+cof_status cof_job_rows(const cof_handle* h, uint32_t job, const char** rows, size_t* rows_len);
 /* Hit count of the last search (hits = (variant, position, strand) triples
  * with mismatches <= threshold, before expansion into bulge rows). */
 cof_status cof_last_hit_count(const cof_handle* h, uint64_t* n_hits, uint64_t* n_rows);
@@ -111,6 +124,8 @@ cof_status cof_set_summary(cof_handle* h, int enable);
 /* Summary table of all searches since cof_read_input, as the reference writes
  * it with --summary (Cas_OFFinder::writeSummaryTable, cas-offinder.cpp:471-500). */
 cof_status cof_summary_text(cof_handle* h, const char** text, size_t* len);
+/* The same for one job of a batch (cof_summary_text = job 0). */
+cof_status cof_job_summary_text(cof_handle* h, uint32_t job, const char** text, size_t* len);
 
 /* ---- header lines: Cas_OFFinder::writeHeaders (cas-offinder.cpp:319-328). */
 const char* cof_header_text(void);

@@ -24,6 +24,11 @@ uint64_t cofx_synth_record(uint64_t seed, uint32_t record, uint64_t len, double 
                            uint32_t drift_window, double n_frac, uint32_t n_run_min, uint32_t n_run_max,
                            char* out);
 
+/* Writes the engine's mismatch predicate as 65536 bytes: out[p * 256 + g] = 1
+ * when pattern byte p mismatches genome byte g (the class table every kernel
+ * uses: a genome byte is one of T, C, A, G or "any other byte"). */
+void cofx_mismatch_table(uint8_t* out);
+
 /* Measures sustained integer-pipe throughput on CUDA device `device`, in
  * lane-operations per second: LOP3 (3-input logic), POPC (population count)
  * and IADD (32-bit add).  These are the denominators of the comparer's

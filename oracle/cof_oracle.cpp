@@ -26,6 +26,7 @@
  * only split loops whose results are merged back in sequential order.
  *
  * Usage: cof-oracle [--summary f] {input|-} {C|G|A}[ids] {output|-}
+ *        cof-oracle --mismatch-table out.bin   (the predicate, 256x256 bytes)
  * Environment: OMP_NUM_THREADS sets the thread count.
  */
 #include <dirent.h>
@@ -531,6 +532,13 @@ void search_file(const std::string& path, const Input& in, std::ostream& os, con
 
 int main(int argc, char** argv) {
   init_tables();
+  if (argc == 3 && std::string(argv[1]) == "--mismatch-table") {  // the predicate as 256x256 bytes
+    FILE* f = fopen(argv[2], "wb");
+    if (!f) return 1;
+    for (int p = 0; p < 256; ++p) fwrite(g_mism[p], 1, 256, f);
+    fclose(f);
+    return 0;
+  }
   struct timeval t0, t1;
   gettimeofday(&t0, nullptr);
   std::vector<std::string> pos;

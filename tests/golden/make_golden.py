@@ -7,7 +7,9 @@ Each case directory holds a small seeded genome (FASTA or 2BIT), `input.txt`
 from its own sources by oracle/build_ref.py and run with device C and one
 OpenMP thread (so rows come in the reference's sequential order).  Cases with
 --summary also keep `expected_summary.txt`; cases the reference rejects keep
-`expected_error.txt` (its exit code and message).
+`expected_error.txt` (its exit code and message).  `mismatch_table.bin` is
+the reference kernel's IUPAC mismatch predicate for all 256 x 256 byte pairs
+(oracle/ref_shim/ref_predicate.cpp runs comparer_cpu on every pair).
 
 Run (needs the reference checkout): python tests/golden/make_golden.py
 """
@@ -100,6 +102,10 @@ def main():
             rows = len(cases.rows_of(open(out, "rb").read()))
             manifest[name] = {"rows": rows, "summary": bool(summ)}
             print(f"{name}: {rows} rows")
+    # The reference kernel's mismatch predicate over all 256 x 256 byte pairs.
+    pred = os.path.join(os.path.dirname(ref), "ref-predicate")
+    subprocess.run([pred, os.path.join(HERE, "mismatch_table.bin")], check=True)
+    manifest["mismatch_table.bin"] = {"bytes": 65536, "source": "comparer_cpu of the reference"}
     with open(os.path.join(HERE, "manifest.json"), "w") as f:
         json.dump(manifest, f, indent=1, sort_keys=True)
 

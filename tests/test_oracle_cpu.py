@@ -73,3 +73,17 @@ def test_reference_gpu_kernels_agree(reference, tmp_path):
     assert cases.run_cli(reference, inp, a, threads=2, device="C").returncode == 0
     assert cases.run_cli(reference, inp, b, threads=2, device="G").returncode == 0
     assert cases.canonical(open(a, "rb").read()) == cases.canonical(open(b, "rb").read())
+
+
+def test_mismatch_predicate_exhaustive(P, built, oracle, tmp_path):
+    """All 256 x 256 (pattern byte, genome byte) pairs: the reference kernel's
+    predicate (golden table), the oracle's and the engine's class table agree."""
+    import numpy as np
+    golden = np.fromfile(os.path.join(GOLDEN, "mismatch_table.bin"), np.uint8).reshape(256, 256)
+    out = str(tmp_path / "oracle_table.bin")
+    assert subprocess.run([oracle, "--mismatch-table", out]).returncode == 0
+    ora = np.fromfile(out, np.uint8).reshape(256, 256)
+    eng = P.mismatch_table()
+    assert (ora == golden).all()
+    assert (eng == golden).all()
+    assert golden.sum() == 1036  # 4 concrete bases x 255 + 6 two-base codes x 2 + 4 three-base codes x 1
