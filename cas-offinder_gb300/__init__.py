@@ -125,6 +125,11 @@ def _ptr(a):
     return ctypes.c_void_p(a.ctypes.data) if a is not None and a.size else None
 
 
+def _bytes_at(addr, n):
+    """Copy n bytes at addr (ctypes.string_at takes a C int size: < 2 GiB only)."""
+    return bytes((ctypes.c_char * n).from_address(addr)) if n else b""
+
+
 # ---------------------------------------------------------------- packing
 def mismatch_table():
     """The engine's mismatch predicate as a 256x256 uint8 array [pattern byte, genome byte]."""
@@ -243,7 +248,7 @@ class CasOFFinder:
     def search(self) -> bytes:
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         self._check(self._L.cof_search(self._h, ctypes.byref(p), ctypes.byref(n)))
-        return ctypes.string_at(p.value, n.value) if n.value else b""
+        return _bytes_at(p.value, n.value)
 
     def search_view(self):
         """(address, length) of the rows in the engine's pinned buffer, without a copy."""
@@ -270,7 +275,7 @@ class CasOFFinder:
     def job_rows(self, job) -> bytes:
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         self._check(self._L.cof_job_rows(self._h, job, ctypes.byref(p), ctypes.byref(n)))
-        return ctypes.string_at(p.value, n.value) if n.value else b""
+        return _bytes_at(p.value, n.value)
 
     def job_summary(self, job) -> bytes:
         p, n = ctypes.c_void_p(), ctypes.c_size_t()

@@ -591,6 +591,13 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   COF_CUDA(h, cudaMemcpyAsync(&nrows, h->small.p, 8, cudaMemcpyDeviceToHost, h->stream));
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
   const uint64_t bytes = h->job_byte0[J];
+  // Rows are short; a size out of proportion means corrupted tables or keys.
+  for (size_t j = 0; j < J; ++j)
+    if (h->job_byte0[j] > h->job_byte0[j + 1])
+      return fail(h, COF_ERR_DEVICE, "job row ranges out of order at job " + std::to_string(j));
+  if (bytes > (nrows + 1) * (uint64_t)(1 << 20))
+    return fail(h, COF_ERR_DEVICE, "row text of " + std::to_string(bytes) + " bytes for " + std::to_string(nrows) +
+                                       " rows (" + std::to_string(nhits) + " hits)");
   COF_CUDA(h, h->text.ensure(bytes + 1));
   launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), h->text.as<char>(),
                     h->stream);

@@ -74,3 +74,42 @@ def test_batch_matches_single_job_oracle(P, built, oracle, tmp_path):
         # Single-job API after a batch: replaces the batch.
         eng.readInputFile(texts[2])
         assert P.HEADER.encode() + eng.search() == want[2]
+
+
+def test_batch_mixed_jobs_and_large_group(P, built, oracle, tmp_path):
+    """48 jobs of the 1,024-guide mixed workload's shape (spacer 20-24, NGG/NRG,
+    2% IUPAC codes, mm 3-6, DNA bulge 0-2, RNA bulge 0-1) plus one job whose
+    pattern group has more than 256 compare variants, each checked against the
+    oracle run on that input alone."""
+    import bench
+    rng = random.Random(91)
+    seqs = [P.synth_record(411, r, n, n_frac=0.01, n_run_min=50, n_run_max=500)
+            for r, n in enumerate([400000, 250000])]
+    genome = str(tmp_path / "genome.fa")
+    texts = bench.batched_jobs(seed=17, n=48, genome_path=genome)
+    big = [f"{''.join(rng.choice('ACGT') for _ in range(20))}NNN 5" for _ in range(6)]
+    texts.append(f"{genome}\n{'N' * 21}GG 2 1\n" + "\n".join(big) + "\n")  # 6 x ~57 variants in one group
+    for t in texts:
+        lines = t.strip().split("\n")
+        pat = lines[1].split()
+        dna = int(pat[1]) if len(pat) == 3 else 0
+        rna = int(pat[2]) if len(pat) == 3 else 0
+        cases.plant_sites(rng, seqs, pat[0], [l.split()[0] for l in lines[2:]], 6, 5, dna, rna)
+    P.write_fasta(genome, ["chr1", "chr2"], seqs)
+    want = []
+    for j, t in enumerate(texts):
+        path = str(tmp_path / f"job{j}.txt")
+        open(path, "w").write(t)
+        out = str(tmp_path / f"job{j}.tsv")
+        r = cases.run_cli(oracle, path, out, threads=8)
+        assert r.returncode == 0, r.stderr.decode()
+        want.append(open(out, "rb").read())
+    assert sum(len(cases.rows_of(w)) for w in want) > 100
+    with P.CasOFFinder(0) as eng:
+        eng.load_genome_file(genome)
+        for t in texts:
+            eng.batch_add_input(t)
+        assert eng.input_info()["variants"] > 256 + 48
+        eng.search()
+        for j in range(len(texts)):
+            assert P.HEADER.encode() + eng.job_rows(j) == want[j], f"job {j}"
