@@ -25,7 +25,7 @@ CLI_PATH = os.path.join(PKG_DIR, "bin", "cas-offinder")
 
 COF_OK = 0
 STATUS_NAMES = {0: "OK", 1: "CUDA", 2: "ARG", 3: "NOMEM", 4: "INPUT", 5: "IO", 6: "STATE",
-                7: "UNSUPPORTED", 8: "NOT_GENOME", 9: "DEVICE", 10: "TOO_LARGE"}
+                7: "UNSUPPORTED", 8: "NOT_GENOME", 9: "DEVICE", 10: "TOO_LARGE", 11: "TIMEOUT"}
 HEADER = ("##Generated by Cas-OFFinder 3.0.0\n"
           "#Id\tBulge Type\tcrRNA\tDNA\tChromosome\tLocation\tDirection\tMismatches\tBulge Size\n")
 
@@ -38,6 +38,8 @@ EXPORTS = [
     "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
     "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cof_search_chunk_static",
     "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
+    "cof_server_start", "cof_server_submit", "cof_server_wait", "cof_server_release", "cof_server_stats",
+    "cof_server_last_error", "cof_server_stop",
     "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table",
 ]
 
@@ -101,6 +103,14 @@ def lib():
             "cof_set_comparer": (c.c_int, [vp, c.c_int]),
             "cof_comparer_info": (c.c_int, [vp, c.POINTER(c.c_int), c.POINTER(c.c_int)]),
             "cof_batch_clear": (c.c_int, [vp]),
+            "cof_server_start": (c.c_int, [vp, u64, u64, c.POINTER(vp)]),
+            "cof_server_submit": (c.c_int, [vp, c.c_char_p, sz, c.POINTER(u64)]),
+            "cof_server_wait": (c.c_int, [vp, u64, c.c_int, c.POINTER(c.c_void_p), c.POINTER(sz),
+                                          c.POINTER(c.c_double)]),
+            "cof_server_release": (c.c_int, [vp, u64]),
+            "cof_server_stats": (c.c_int, [vp] + [c.POINTER(u64)] * 6),
+            "cof_server_last_error": (c.c_char_p, [vp]),
+            "cof_server_stop": (None, [vp]),
             "cof_batch_add_input": (c.c_int, [vp, c.c_char_p, sz, c.POINTER(u32)]),
             "cof_batch_size": (c.c_int, [vp, c.POINTER(u32)]),
             "cof_job_rows": (c.c_int, [vp, u32, c.POINTER(c.c_void_p), c.POINTER(sz)]),
@@ -350,6 +360,59 @@ class CasOFFinder:
         ms = ctypes.c_double()
         self._check(self._L.cof_timer_stop(self._h, ctypes.byref(ms)))
         return ms.value
+
+
+class Server:
+    """Served mode over an engine's resident genome (see include/cof.h).
+    While it runs, use the engine only through this server."""
+
+    def __init__(self, engine, max_active_variants=0, hit_buffer_bytes=0):
+        self._L = engine._L
+        self._eng = engine
+        s = ctypes.c_void_p()
+        st = self._L.cof_server_start(engine._h, max_active_variants, hit_buffer_bytes, ctypes.byref(s))
+        if st != COF_OK:
+            raise CofError(st, self._L.cof_last_error(engine._h).decode())
+        self._s = s
+
+    def submit(self, text):
+        if isinstance(text, str):
+            text = text.encode()
+        t = ctypes.c_uint64()
+        st = self._L.cof_server_submit(self._s, text, len(text), ctypes.byref(t))
+        if st != COF_OK:
+            raise CofError(st, self._L.cof_server_last_error(self._s).decode())
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1):
+        """(rows bytes, latency ms), or None on timeout."""
+        p, n, lat = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_double()
+        st = self._L.cof_server_wait(self._s, ticket, timeout_ms, ctypes.byref(p), ctypes.byref(n),
+                                     ctypes.byref(lat))
+        if st == 11:
+            return None
+        if st != COF_OK:
+            raise CofError(st, self._L.cof_server_last_error(self._s).decode())
+        rows = _bytes_at(p.value, n.value)
+        self._L.cof_server_release(self._s, ticket)
+        return rows, lat.value
+
+    def stats(self):
+        vals = [ctypes.c_uint64() for _ in range(6)]
+        self._L.cof_server_stats(self._s, *[ctypes.byref(v) for v in vals])
+        keys = ("steps", "admitted", "completed", "pending", "active", "max_active")
+        return dict(zip(keys, (v.value for v in vals)))
+
+    def stop(self):
+        if self._s:
+            self._L.cof_server_stop(self._s)
+            self._s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()
 
 
 def pipe_rates(device=0):

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
               "--expt-relaxed-constexpr", *ARCH]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
-CU_SOURCES = ["kernels.cu", "comparer_bs.cu", "engine.cu", "pipe_rates.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "comparer_bs.cu", "engine.cu", "server.cu", "pipe_rates.cu", "noalloc.cu"]
 CPP_SOURCES = ["input.cpp", "genome_io.cpp", "synth.cpp"]
 
 

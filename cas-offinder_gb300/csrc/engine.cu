@@ -19,149 +19,26 @@
 
 #include "../../include/cof.h"
 #include "../../include/cof_tools.h"
-#include "cof_internal.h"
-#include "kernels.cuh"
+#include "engine_internal.h"
 
-namespace {
-
-using namespace cof;
-
-constexpr uint64_t kSegPositions = 1ull << 26;  // start positions per finder/comparer pass
-constexpr uint64_t kSegWords = kSegPositions / 32;
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
-    if (e == cudaSuccess) cap = bytes;
-    return e;
-  }
-  template <typename T>
-  T* as() const {
-    return (T*)p;
-  }
-};
-
-struct HostPinned {
-  void* p = nullptr;
-  size_t cap = 0;
-  ~HostPinned() {
-    if (p) cudaFreeHost(p);
-  }
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFreeHost(p);
-    p = nullptr;
-    cap = 0;
-    cudaError_t e = cudaMallocHost(&p, bytes ? bytes : 1);
-    if (e == cudaSuccess) cap = bytes;
-    return e;
-  }
-};
-
-// A genome resident on the device.
-struct DevGenome {
-  uint64_t n = 0;
-  uint32_t n_rec = 0;
-  uint64_t n_exc = 0;
-  DevBuf hi, lo, ot, exc_pos, exc_byte, rec_start, rec_name_off, rec_name_len, rec_names;
-  bool loaded = false;
-  GenomeView view() const {
-    GenomeView g;
-    g.hi = hi.as<uint32_t>();
-    g.lo = lo.as<uint32_t>();
-    g.ot = ot.as<uint32_t>();
-    g.exc_pos = exc_pos.as<uint64_t>();
-    g.exc_byte = exc_byte.as<uint8_t>();
-    g.n_exc = n_exc;
-    g.n = n;
-    g.rec_start = rec_start.as<uint64_t>();
-    g.rec_name_off = rec_name_off.as<uint32_t>();
-    g.rec_name_len = rec_name_len.as<uint32_t>();
-    g.rec_names = rec_names.as<char>();
-    g.n_rec = n_rec;
-    return g;
-  }
-};
-
-struct KernelStat {
-  uint64_t launches = 0;
-  double ms = 0;
-  double units = 0;
-};
-
-// Compare variants (of one or more jobs) that share one padded pattern.
-struct PatternGroup {
-  std::string pattern;
-  uint32_t L = 0;
-  FinderPattern fpat{};
-  int nw = 1;                  // 32-bit words per window (popcount comparer)
-  int bs_slots = 0;            // bit-sliced slot count, 0 = popcount comparer
-  std::vector<uint32_t> gids;  // global variant ids, ascending
-  double nonN_sum = 0;         // sum of non-N positions over the group's variants
-  DevBuf vmask, bs_off, bs_thr, bs_gid;
-};
-
-}  // namespace
-
-struct cof_handle {
-  int device = 0;
-  int sm_count = 0;
-  cudaStream_t stream = nullptr;   // comparer, formatting, copies
-  cudaStream_t stream2 = nullptr;  // finder passes, one segment ahead of the comparer
-  cudaEvent_t ev_start = nullptr, ev_found[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
-  std::string err;
-
-  // The batch: one or more parsed input files ("jobs").  Variant ids are
-  // global and job-major (job j owns [job_gid0[j], job_gid0[j+1])), so one
-  // sort of the hit keys yields every job's rows contiguously, in job order.
-  std::vector<Job> jobs;
-  std::vector<uint32_t> job_gid0;
-  bool jobs_on_device = false;
-  bool force_popc = false;
-  std::vector<PatternGroup> groups;  // jobs sharing a padded pattern share finder + comparer passes
-  DevBuf vfmt, sfmt, pool;           // row formatting tables over all variants
-  DevGenome genome, scratch;
-
-  DevBuf queue[2], qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small,
-      job_start, job_bytes;
-  HostPinned host_text;
-  std::string summary_text;
-  std::vector<std::map<std::string, unsigned long long>> summaries;  // per job
-  bool summary_on = false;
-  uint64_t last_hits = 0, last_rows = 0;
-  std::vector<uint64_t> job_byte0;  // row text of job j: [job_byte0[j], job_byte0[j+1]) of host_text
-
-  bool profiling = false;
-  std::map<std::string, KernelStat> stats;
-  cudaEvent_t timer_a = nullptr, timer_b = nullptr;
-};
-
-namespace {
-
-std::mutex g_open_mu;
-std::string g_open_err;
+namespace cof {
+namespace eng {
 
 cof_status fail(cof_handle* h, cof_status st, const std::string& msg) {
   h->err = msg;
   return st;
 }
 
-#define COF_CUDA(h, call)                                                                           \
-  do {                                                                                              \
-    cudaError_t e_ = (call);                                                                        \
-    if (e_ != cudaSuccess)                                                                          \
-      return fail(h, e_ == cudaErrorMemoryAllocation ? COF_ERR_NOMEM : COF_ERR_CUDA,                \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));                              \
-  } while (0)
+}  // namespace eng
+}  // namespace cof
+
+namespace {
+
+using namespace cof;
+using namespace cof::eng;
+
+std::mutex g_open_mu;
+std::string g_open_err;
 
 // Uploads a packed genome into `dg` (copies are stream-ordered on h->stream).
 cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
@@ -221,7 +98,11 @@ cof_status upload_packed(cof_handle* h, DevGenome& dg, const PackedGenome& g) {
                        g.exc_pos.size(), g.names, g.starts);
 }
 
-// PAM-scan pattern from the forward pattern and its reverse complement.
+}  // namespace
+
+namespace cof {
+namespace eng {
+
 bool make_finder_pattern(const std::string& fwd, const std::string& rev, FinderPattern& fp) {
   const size_t L = fwd.size();
   if (L == 0 || L > (size_t)kMaxL || rev.size() != L) return false;
@@ -265,6 +146,105 @@ void fill_mask(VariantMask<NW>& vm, const std::string& comp, uint32_t thr, uint3
   vm.gid = gid;
 }
 
+void init_group(PatternGroup& g, const std::string& pattern) {
+  g.pattern = pattern;
+  g.L = (uint32_t)pattern.size();
+  g.nw = g.L <= 32 ? 1 : 2;
+  make_finder_pattern(pattern, revcomp(pattern), g.fpat);
+}
+
+cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars) {
+  const size_t V = vars.size();
+  const size_t msz = g.nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>);
+  std::vector<unsigned char> masks(std::max<size_t>(V, 1) * msz, 0);
+  int maxpos = 0;
+  g.nonN_sum = 0;
+  for (size_t i = 0; i < V; ++i) {
+    const Variant& var = *vars[i];
+    if (g.nw == 1) fill_mask<1>(((VariantMask<1>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
+    else fill_mask<2>(((VariantMask<2>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
+    int c = 0;
+    for (char ch : var.key) {
+      c += bs_class_of((unsigned char)ch) != 0;
+      g.nonN_sum += ch != 'N';
+    }
+    maxpos = std::max(maxpos, c);
+  }
+  COF_CUDA(h, g.vmask.ensure(masks.size()));
+  COF_CUDA(h, cudaMemcpyAsync(g.vmask.p, masks.data(), masks.size(), cudaMemcpyHostToDevice, h->stream));
+  g.bs_slots = h->force_popc ? 0 : bs_slots_for(maxpos);
+  std::vector<uint32_t> off, thr, gid;
+  if (g.bs_slots) {
+    // Per variant, the positions that can mismatch as byte offsets of their
+    // class word in the comparer's shared-memory table.
+    const int S = g.bs_slots;
+    const uint32_t row = (uint32_t)bs_row_for(g.L);
+    off.assign(std::max<size_t>(V, 1) * (S / 2), 0);
+    thr.assign(std::max<size_t>(V, 1), 0);
+    gid.assign(std::max<size_t>(V, 1), 0);
+    for (size_t i = 0; i < V; ++i) {
+      const Variant& var = *vars[i];
+      int sl = 0;
+      for (size_t k = 0; k < var.key.size(); ++k) {
+        const uint32_t c = bs_class_of((unsigned char)var.key[k]);
+        if (!c) continue;
+        const uint32_t byte_off = (c * row + (uint32_t)k) * 8;  // uint2 table element (two groups)
+        off[i * (S / 2) + sl / 2] |= byte_off << (16 * (sl & 1));
+        ++sl;
+      }
+      thr[i] = var.threshold;
+      gid[i] = g.gids[i];
+    }
+    COF_CUDA(h, g.bs_off.ensure(off.size() * 4));
+    COF_CUDA(h, g.bs_thr.ensure(thr.size() * 4));
+    COF_CUDA(h, g.bs_gid.ensure(gid.size() * 4));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_gid.p, gid.data(), gid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+  }
+  // The host vectors die on return: wait for the copies.
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  return COF_OK;
+}
+
+void append_format_tables(const Job& job, std::vector<VariantFmt>& vf, std::vector<ShapeFmt>& sf, std::string& pool) {
+  auto put = [&](const std::string& str) {
+    const uint32_t o = (uint32_t)pool.size();
+    pool += str;
+    return o;
+  };
+  for (size_t v = 0; v < job.variants.size(); ++v) {
+    VariantFmt f{};
+    f.comp_off = put(job.variants[v].key);
+    f.L = (uint32_t)job.pattern.size();
+    for (int st = 0; st < 2; ++st) {
+      f.shape_begin[st] = (uint32_t)sf.size();
+      for (const RowShape& r : job.shapes[st][v]) {
+        ShapeFmt x;
+        x.head_off = put(r.head);
+        x.head_len = (uint32_t)r.head.size();
+        x.dna_off = put(r.dna);
+        x.dna_len = (uint32_t)r.dna.size();
+        x.tail_off = put(r.tail);
+        x.tail_len = (uint32_t)r.tail.size();
+        x.offset = r.offset;
+        x.dir = st ? '-' : '+';
+        sf.push_back(x);
+      }
+      f.shape_end[st] = (uint32_t)sf.size();
+    }
+    vf.push_back(f);
+  }
+}
+
+}  // namespace eng
+}  // namespace cof
+
+namespace {
+
+using namespace cof;
+using namespace cof::eng;
+
 // Builds the pattern groups and uploads every variant's comparer and
 // formatting tables for the current batch.
 cof_status upload_jobs(cof_handle* h) {
@@ -280,112 +260,31 @@ cof_status upload_jobs(cof_handle* h) {
   const uint64_t total = h->job_gid0.back();
   if (total >= (1u << 20)) return fail(h, COF_ERR_UNSUPPORTED, "more than 2^20 compare variants in one batch");
   std::map<std::string, size_t> group_of;
-  std::vector<const Variant*> var_of(total);
-  std::vector<uint32_t> L_of(total);
+  std::vector<std::vector<const Variant*>> group_vars;
   for (size_t j = 0; j < h->jobs.size(); ++j) {
     const Job& job = h->jobs[j];
     auto it = group_of.find(job.pattern);
     if (it == group_of.end()) {
       it = group_of.emplace(job.pattern, h->groups.size()).first;
       h->groups.emplace_back();
-      PatternGroup& g = h->groups.back();
-      g.pattern = job.pattern;
-      g.L = (uint32_t)job.pattern.size();
-      g.nw = g.L <= 32 ? 1 : 2;
-      make_finder_pattern(job.pattern, revcomp(job.pattern), g.fpat);
+      init_group(h->groups.back(), job.pattern);
+      group_vars.emplace_back();
     }
-    PatternGroup& g = h->groups[it->second];
     for (size_t v = 0; v < job.variants.size(); ++v) {
-      const uint32_t gid = h->job_gid0[j] + (uint32_t)v;
-      g.gids.push_back(gid);
-      var_of[gid] = &job.variants[v];
-      L_of[gid] = g.L;
+      h->groups[it->second].gids.push_back(h->job_gid0[j] + (uint32_t)v);
+      group_vars[it->second].push_back(&job.variants[v]);
     }
   }
-  // Formatting tables over all variants.
+  // Formatting tables over all variants (ids are job-major, so appending job
+  // by job gives id order).
   std::string pool;
-  std::vector<VariantFmt> vf(total);
+  std::vector<VariantFmt> vf;
   std::vector<ShapeFmt> sf;
-  auto put = [&](const std::string& str) {
-    const uint32_t o = (uint32_t)pool.size();
-    pool += str;
-    return o;
-  };
-  for (size_t j = 0; j < h->jobs.size(); ++j) {
-    const Job& job = h->jobs[j];
-    for (size_t v = 0; v < job.variants.size(); ++v) {
-      const uint32_t gid = h->job_gid0[j] + (uint32_t)v;
-      vf[gid].comp_off = put(job.variants[v].key);
-      vf[gid].L = (uint32_t)job.pattern.size();
-      for (int st = 0; st < 2; ++st) {
-        vf[gid].shape_begin[st] = (uint32_t)sf.size();
-        for (const RowShape& r : job.shapes[st][v]) {
-          ShapeFmt f;
-          f.head_off = put(r.head);
-          f.head_len = (uint32_t)r.head.size();
-          f.dna_off = put(r.dna);
-          f.dna_len = (uint32_t)r.dna.size();
-          f.tail_off = put(r.tail);
-          f.tail_len = (uint32_t)r.tail.size();
-          f.offset = r.offset;
-          f.dir = st ? '-' : '+';
-          sf.push_back(f);
-        }
-        vf[gid].shape_end[st] = (uint32_t)sf.size();
-      }
-    }
-  }
+  for (const Job& job : h->jobs) append_format_tables(job, vf, sf, pool);
   if (pool.size() >= (1ull << 32)) return fail(h, COF_ERR_UNSUPPORTED, "row tables exceed 4 GB");
-  // Comparer tables per group.
-  for (PatternGroup& g : h->groups) {
-    const size_t V = g.gids.size();
-    const size_t msz = g.nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>);
-    std::vector<unsigned char> masks(std::max<size_t>(V, 1) * msz, 0);
-    int maxpos = 0;
-    g.nonN_sum = 0;
-    for (size_t i = 0; i < V; ++i) {
-      const Variant& var = *var_of[g.gids[i]];
-      if (g.nw == 1) fill_mask<1>(((VariantMask<1>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
-      else fill_mask<2>(((VariantMask<2>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
-      int c = 0;
-      for (char ch : var.key) {
-        c += bs_class_of((unsigned char)ch) != 0;
-        g.nonN_sum += ch != 'N';
-      }
-      maxpos = std::max(maxpos, c);
-    }
-    COF_CUDA(h, g.vmask.ensure(masks.size()));
-    COF_CUDA(h, cudaMemcpyAsync(g.vmask.p, masks.data(), masks.size(), cudaMemcpyHostToDevice, h->stream));
-    g.bs_slots = h->force_popc ? 0 : bs_slots_for(maxpos);
-    if (g.bs_slots) {
-      // Per variant, the positions that can mismatch as byte offsets of their
-      // class word in the comparer's shared-memory table.
-      const int S = g.bs_slots;
-      const uint32_t row = (uint32_t)bs_row_for(g.L);
-      std::vector<uint32_t> off(std::max<size_t>(V, 1) * (S / 2), 0), thr(std::max<size_t>(V, 1), 0),
-          gid(std::max<size_t>(V, 1), 0);
-      for (size_t i = 0; i < V; ++i) {
-        const Variant& var = *var_of[g.gids[i]];
-        int sl = 0;
-        for (size_t k = 0; k < var.key.size(); ++k) {
-          const uint32_t c = bs_class_of((unsigned char)var.key[k]);
-          if (!c) continue;
-          const uint32_t byte_off = (c * row + (uint32_t)k) * 8;  // uint2 table element (two groups)
-          off[i * (S / 2) + sl / 2] |= byte_off << (16 * (sl & 1));
-          ++sl;
-        }
-        thr[i] = var.threshold;
-        gid[i] = g.gids[i];
-      }
-      COF_CUDA(h, g.bs_off.ensure(off.size() * 4));
-      COF_CUDA(h, g.bs_thr.ensure(thr.size() * 4));
-      COF_CUDA(h, g.bs_gid.ensure(gid.size() * 4));
-      COF_CUDA(h, cudaMemcpyAsync(g.bs_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, h->stream));
-      COF_CUDA(h, cudaMemcpyAsync(g.bs_thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, h->stream));
-      COF_CUDA(h, cudaMemcpyAsync(g.bs_gid.p, gid.data(), gid.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    }
-    // The host vectors die at the end of this iteration: wait for the copies.
-    COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (size_t gi = 0; gi < h->groups.size(); ++gi) {
+    cof_status st = build_group_tables(h, h->groups[gi], group_vars[gi]);
+    if (st) return st;
   }
   COF_CUDA(h, h->vfmt.ensure(std::max<size_t>(total, 1) * sizeof(VariantFmt)));
   COF_CUDA(h, h->sfmt.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));

@@ -1,0 +1,169 @@
+// Internal types of libcasoff.so shared by engine.cu and server.cu: device
+// buffers, the resident genome, pattern groups and the handle.  Not part of
+// the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/cof.h"
+#include "cof_internal.h"
+#include "kernels.cuh"
+
+namespace cof {
+namespace eng {
+
+constexpr uint64_t kSegPositions = 1ull << 26;  // start positions per finder/comparer pass
+constexpr uint64_t kSegWords = kSegPositions / 32;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+  template <typename T>
+  T* as() const {
+    return (T*)p;
+  }
+};
+
+struct HostPinned {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~HostPinned() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMallocHost(&p, bytes ? bytes : 1);
+    if (e == cudaSuccess) cap = bytes;
+    return e;
+  }
+};
+
+// A genome resident on the device.
+struct DevGenome {
+  uint64_t n = 0;
+  uint32_t n_rec = 0;
+  uint64_t n_exc = 0;
+  DevBuf hi, lo, ot, exc_pos, exc_byte, rec_start, rec_name_off, rec_name_len, rec_names;
+  bool loaded = false;
+  GenomeView view() const {
+    GenomeView g;
+    g.hi = hi.as<uint32_t>();
+    g.lo = lo.as<uint32_t>();
+    g.ot = ot.as<uint32_t>();
+    g.exc_pos = exc_pos.as<uint64_t>();
+    g.exc_byte = exc_byte.as<uint8_t>();
+    g.n_exc = n_exc;
+    g.n = n;
+    g.rec_start = rec_start.as<uint64_t>();
+    g.rec_name_off = rec_name_off.as<uint32_t>();
+    g.rec_name_len = rec_name_len.as<uint32_t>();
+    g.rec_names = rec_names.as<char>();
+    g.n_rec = n_rec;
+    return g;
+  }
+};
+
+struct KernelStat {
+  uint64_t launches = 0;
+  double ms = 0;
+  double units = 0;
+};
+
+// Compare variants (of one or more jobs) that share one padded pattern.
+struct PatternGroup {
+  std::string pattern;
+  uint32_t L = 0;
+  FinderPattern fpat{};
+  int nw = 1;                  // 32-bit words per window (popcount comparer)
+  int bs_slots = 0;            // bit-sliced slot count, 0 = popcount comparer
+  std::vector<uint32_t> gids;  // global variant ids, ascending
+  double nonN_sum = 0;         // sum of non-N positions over the group's variants
+  DevBuf vmask, bs_off, bs_thr, bs_gid;
+};
+
+}  // namespace eng
+}  // namespace cof
+
+using namespace cof;
+using namespace cof::eng;
+
+struct cof_handle {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;   // comparer, formatting, copies
+  cudaStream_t stream2 = nullptr;  // finder passes, one segment ahead of the comparer
+  cudaEvent_t ev_start = nullptr, ev_found[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
+  std::string err;
+
+  // The batch: one or more parsed input files ("jobs").  Variant ids are
+  // global and job-major (job j owns [job_gid0[j], job_gid0[j+1])), so one
+  // sort of the hit keys yields every job's rows contiguously, in job order.
+  std::vector<Job> jobs;
+  std::vector<uint32_t> job_gid0;
+  bool jobs_on_device = false;
+  bool force_popc = false;
+  std::vector<PatternGroup> groups;  // jobs sharing a padded pattern share finder + comparer passes
+  DevBuf vfmt, sfmt, pool;           // row formatting tables over all variants
+  DevGenome genome, scratch;
+
+  DevBuf queue[2], qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small,
+      job_start, job_bytes;
+  HostPinned host_text;
+  std::string summary_text;
+  std::vector<std::map<std::string, unsigned long long>> summaries;  // per job
+  bool summary_on = false;
+  uint64_t last_hits = 0, last_rows = 0;
+  std::vector<uint64_t> job_byte0;  // row text of job j: [job_byte0[j], job_byte0[j+1]) of host_text
+
+  bool profiling = false;
+  std::map<std::string, KernelStat> stats;
+  cudaEvent_t timer_a = nullptr, timer_b = nullptr;
+};
+
+
+namespace cof {
+namespace eng {
+
+cof_status fail(cof_handle* h, cof_status st, const std::string& msg);
+
+#define COF_CUDA(h, call)                                                                           \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      return ::cof::eng::fail(h, e_ == cudaErrorMemoryAllocation ? COF_ERR_NOMEM : COF_ERR_CUDA,    \
+                              std::string(#call) + ": " + cudaGetErrorString(e_));                  \
+  } while (0)
+
+// PAM-scan pattern from the forward pattern and its reverse complement.
+bool make_finder_pattern(const std::string& fwd, const std::string& rev, FinderPattern& fp);
+std::string revcomp(const std::string& s);
+// Initialises g (pattern, L, word count, finder pattern) for a padded pattern.
+void init_group(PatternGroup& g, const std::string& pattern);
+// Builds and uploads g's comparer tables for its variants `vars` (g.gids
+// already set, one id per variant).  Synchronizes h->stream.
+cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars);
+// Row shapes of `vars` (variant i gets id first_gid + i) appended to the
+// formatting tables vf (indexed by id), sf and pool.
+void append_format_tables(const Job& job, std::vector<VariantFmt>& vf, std::vector<ShapeFmt>& sf, std::string& pool);
+
+}  // namespace eng
+}  // namespace cof

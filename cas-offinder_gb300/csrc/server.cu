@@ -1,0 +1,432 @@
+// Served mode: continuous batching of search requests over the resident genome.
+//
+// The reference runs one input file per process (main.cpp:72-157).  A server
+// keeps the packed genome resident and searches many requests (each one input
+// file) at once.  The genome is walked as a ring of segments; one step
+// processes one segment for every active request.  Requests are admitted at
+// any step boundary -- while others are already running -- as long as the
+// active compare variants fit the variant budget, and each request is complete
+// once it has seen every segment of the ring, wherever it joined.  Active
+// requests with the same padded pattern share one PAM scan and one comparer
+// launch per step, but keep their own variants, ids and thresholds, so every
+// request's rows are exactly those of a search of that input file alone.
+//
+// Threads: cof_server_submit / wait / release may be called from any host
+// thread; all device work runs on the server's worker thread, on the handle's
+// streams.  While a server runs, the handle must not be used for anything else.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+
+#include "engine_internal.h"
+
+namespace {
+
+using namespace cof;
+using namespace cof::eng;
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  uint64_t ticket = 0;
+  Job job;
+  uint32_t nvar = 0;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  uint64_t steps_seen = 0;
+  uint32_t gid0 = 0;            // first id of its variants in the active tables
+  std::vector<uint64_t> hits;   // hit keys with request-local variant ids
+  bool done = false;
+  cof_status status = COF_OK;
+  std::string err;
+  std::string rows;
+  uint64_t n_rows = 0;
+};
+
+using ReqPtr = std::shared_ptr<Request>;
+
+}  // namespace
+
+struct cof_server {
+  cof_handle* h = nullptr;
+  uint64_t max_active_variants = 0;
+  uint64_t hit_buffer_bytes = 0;
+
+  std::thread worker;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  bool stop = false;
+  std::deque<ReqPtr> pending;
+  std::vector<ReqPtr> active;
+  std::unordered_map<uint64_t, ReqPtr> tickets;
+  uint64_t next_ticket = 1;
+  std::string last_error;
+  std::atomic<uint64_t> steps{0};
+  uint64_t admitted = 0, completed = 0, max_active_seen = 0;
+
+  // worker-only state
+  std::vector<PatternGroup> groups;
+  bool tables_dirty = true;
+  uint64_t ring = 0, cur = 0;  // ring length in segments, current segment
+  DevBuf step_hits, step_count, fmt_hits, fmt_sorted, fmt_bytes, fmt_off, fmt_cnt, fmt_tmp, fmt_text, fmt_vf, fmt_sf,
+      fmt_pool, fmt_small;
+};
+
+namespace {
+
+// Rebuilds the comparer tables of the active set: ids are assigned request by
+// request in admission order, groups keyed by padded pattern.
+cof_status rebuild_tables(cof_server* s) {
+  cof_handle* h = s->h;
+  s->groups.clear();
+  std::map<std::string, size_t> group_of;
+  std::vector<std::vector<const Variant*>> vars;
+  uint32_t next = 0;
+  for (const ReqPtr& r : s->active) {
+    r->gid0 = next;
+    auto it = group_of.find(r->job.pattern);
+    if (it == group_of.end()) {
+      it = group_of.emplace(r->job.pattern, s->groups.size()).first;
+      s->groups.emplace_back();
+      init_group(s->groups.back(), r->job.pattern);
+      vars.emplace_back();
+    }
+    for (size_t v = 0; v < r->job.variants.size(); ++v) {
+      s->groups[it->second].gids.push_back(next + (uint32_t)v);
+      vars[it->second].push_back(&r->job.variants[v]);
+    }
+    next += r->nvar;
+  }
+  for (size_t g = 0; g < s->groups.size(); ++g) {
+    cof_status st = build_group_tables(h, s->groups[g], vars[g]);
+    if (st) return st;
+  }
+  s->tables_dirty = false;
+  return COF_OK;
+}
+
+// One ring step: segment s->cur for every active group.  Appends each hit to
+// its request, with the request-local variant id.
+cof_status run_step(cof_server* s) {
+  cof_handle* h = s->h;
+  const GenomeView gv = h->genome.view();
+  const uint64_t n = h->genome.n;
+  uint64_t cap = std::max<uint64_t>(s->step_hits.cap / 8, 1u << 16);
+  COF_CUDA(h, s->step_hits.ensure(cap * 8));
+  COF_CUDA(h, s->step_count.ensure(8));
+  COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(s->groups.size(), 1) * 4));
+  COF_CUDA(h, h->queue[0].ensure(2 * kSegPositions * 4));
+  COF_CUDA(h, h->queue[1].ensure(2 * kSegPositions * 4));
+  uint64_t count = 0;
+  for (;;) {
+    COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<size_t>(s->groups.size(), 1) * 4, h->stream));
+    COF_CUDA(h, cudaMemsetAsync(s->step_count.p, 0, 8, h->stream));
+    COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
+    COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
+    uint64_t pass = 0;
+    for (size_t gi = 0; gi < s->groups.size(); ++gi) {
+      const PatternGroup& g = s->groups[gi];
+      const uint64_t npos = n >= g.L ? n - g.L + 1 : 0;
+      const uint64_t words = (npos + 31) / 32;
+      const uint64_t w0 = s->cur * kSegWords, w1 = std::min(words, w0 + kSegWords);
+      if (w0 >= w1 || g.gids.empty()) continue;
+      const int b = (int)(pass & 1);
+      uint32_t* qc = h->qcounts.as<uint32_t>() + gi;
+      uint32_t* q = h->queue[b].as<uint32_t>();
+      if (pass >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
+      launch_finder(gv, w0, w1, g.fpat, q, qc, h->stream2);
+      COF_CUDA(h, cudaEventRecord(h->ev_found[b], h->stream2));
+      COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_found[b], 0));
+      const uint32_t V = (uint32_t)g.gids.size();
+      if (!g.bs_slots ||
+          !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_off.as<uint32_t>(), g.bs_thr.as<uint32_t>(),
+                              g.bs_gid.as<uint32_t>(), V, g.bs_slots, g.L, s->step_hits.as<uint64_t>(),
+                              s->step_count.as<unsigned long long>(), cap, h->sm_count, h->stream))
+        launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, s->step_hits.as<uint64_t>(),
+                        s->step_count.as<unsigned long long>(), cap, h->sm_count, h->stream);
+      COF_CUDA(h, cudaEventRecord(h->ev_used[b], h->stream));
+      ++pass;
+    }
+    COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream2));
+    COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_start, 0));
+    COF_CUDA(h, cudaGetLastError());
+    COF_CUDA(h, cudaMemcpyAsync(&count, s->step_count.p, 8, cudaMemcpyDeviceToHost, h->stream));
+    COF_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (count <= cap) break;
+    if (count * 8 > s->hit_buffer_bytes)
+      return fail(h, COF_ERR_NOMEM, "one ring step found " + std::to_string(count) +
+                                        " hits, more than the hit buffer budget allows");
+    cap = count + count / 8;
+    COF_CUDA(h, s->step_hits.ensure(cap * 8));
+  }
+  if (count) {
+    std::vector<uint64_t> keys(count);
+    COF_CUDA(h, cudaMemcpy(keys.data(), s->step_hits.p, count * 8, cudaMemcpyDeviceToHost));
+    // Requests own consecutive id ranges in admission order.
+    for (uint64_t k : keys) {
+      const uint32_t gid = (uint32_t)(k >> 44);
+      size_t a = 0, z = s->active.size();
+      while (z - a > 1) {
+        const size_t mid = (a + z) / 2;
+        if (s->active[mid]->gid0 <= gid) a = mid;
+        else z = mid;
+      }
+      Request& r = *s->active[a];
+      r.hits.push_back(((uint64_t)(gid - r.gid0) << 44) | (k & ((1ull << 44) - 1)));
+    }
+  }
+  ++s->steps;
+  return COF_OK;
+}
+
+// Sorts a finished request's hits and formats its rows on the device.
+cof_status format_request(cof_server* s, Request& r) {
+  cof_handle* h = s->h;
+  std::sort(r.hits.begin(), r.hits.end());
+  const uint64_t nh = r.hits.size();
+  if (!nh) return COF_OK;
+  std::vector<VariantFmt> vf;
+  std::vector<ShapeFmt> sf;
+  std::string pool;
+  append_format_tables(r.job, vf, sf, pool);
+  COF_CUDA(h, s->fmt_vf.ensure(vf.size() * sizeof(VariantFmt)));
+  COF_CUDA(h, s->fmt_sf.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
+  COF_CUDA(h, s->fmt_pool.ensure(std::max<size_t>(pool.size(), 1)));
+  COF_CUDA(h, s->fmt_hits.ensure(nh * 8));
+  COF_CUDA(h, s->fmt_bytes.ensure(nh * 8));
+  COF_CUDA(h, s->fmt_off.ensure(nh * 8));
+  COF_CUDA(h, s->fmt_cnt.ensure(nh * 4));
+  COF_CUDA(h, s->fmt_small.ensure(16));
+  COF_CUDA(h, cudaMemcpyAsync(s->fmt_vf.p, vf.data(), vf.size() * sizeof(VariantFmt), cudaMemcpyHostToDevice, h->stream));
+  if (!sf.empty())
+    COF_CUDA(h, cudaMemcpyAsync(s->fmt_sf.p, sf.data(), sf.size() * sizeof(ShapeFmt), cudaMemcpyHostToDevice, h->stream));
+  if (!pool.empty())
+    COF_CUDA(h, cudaMemcpyAsync(s->fmt_pool.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(s->fmt_hits.p, r.hits.data(), nh * 8, cudaMemcpyHostToDevice, h->stream));
+  const GenomeView gv = h->genome.view();
+  FormatTables ft{s->fmt_vf.as<VariantFmt>(), s->fmt_sf.as<ShapeFmt>(), s->fmt_pool.as<char>()};
+  launch_row_lengths(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_bytes.as<uint64_t>(), s->fmt_cnt.as<uint32_t>(),
+                     h->stream);
+  size_t t1 = 0, t2 = 0;
+  COF_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
+                                            (int64_t)nh, h->stream));
+  COF_CUDA(h, cub::DeviceReduce::Sum(nullptr, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(), (int64_t)nh,
+                                     h->stream));
+  COF_CUDA(h, s->fmt_tmp.ensure(std::max(t1, t2)));
+  t1 = s->fmt_tmp.cap;
+  COF_CUDA(h, cub::DeviceScan::ExclusiveSum(s->fmt_tmp.p, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
+                                            (int64_t)nh, h->stream));
+  t2 = s->fmt_tmp.cap;
+  COF_CUDA(h, cub::DeviceReduce::Sum(s->fmt_tmp.p, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(),
+                                     (int64_t)nh, h->stream));
+  uint64_t last[3] = {0, 0, 0};
+  COF_CUDA(h, cudaMemcpyAsync(&last[0], s->fmt_off.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(&last[1], s->fmt_bytes.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaMemcpyAsync(&last[2], s->fmt_small.p, 8, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  const uint64_t bytes = last[0] + last[1];
+  COF_CUDA(h, s->fmt_text.ensure(bytes + 1));
+  launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), s->fmt_text.as<char>(),
+                    h->stream);
+  COF_CUDA(h, cudaGetLastError());
+  r.rows.resize(bytes);
+  COF_CUDA(h, cudaMemcpyAsync(&r.rows[0], s->fmt_text.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  r.n_rows = last[2];
+  return COF_OK;
+}
+
+void finish(cof_server* s, const ReqPtr& r, cof_status st, const std::string& err) {
+  std::lock_guard<std::mutex> lock(s->mu);
+  r->status = st;
+  r->err = err;
+  r->done = true;
+  r->t_done = now_s();
+  r->hits.clear();
+  r->hits.shrink_to_fit();
+  ++s->completed;
+  s->cv_done.notify_all();
+}
+
+void worker_main(cof_server* s) {
+  cof_handle* h = s->h;
+  cudaSetDevice(h->device);
+  const uint64_t words = (h->genome.n + 31) / 32;
+  s->ring = std::max<uint64_t>(1, (words + kSegWords - 1) / kSegWords);
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lock(s->mu);
+      s->cv_work.wait(lock, [&] { return s->stop || !s->pending.empty() || !s->active.empty(); });
+      if (s->stop) break;
+      // Admit waiting requests while the variant budget allows (always at
+      // least one, so a request larger than the budget still runs alone).
+      uint64_t used = 0;
+      for (const ReqPtr& r : s->active) used += r->nvar;
+      while (!s->pending.empty()) {
+        const ReqPtr& r = s->pending.front();
+        if (!s->active.empty() && used + r->nvar > s->max_active_variants) break;
+        used += r->nvar;
+        r->t_admit = now_s();
+        r->steps_seen = 0;
+        s->active.push_back(r);
+        s->pending.pop_front();
+        ++s->admitted;
+        s->tables_dirty = true;
+      }
+      s->max_active_seen = std::max<uint64_t>(s->max_active_seen, s->active.size());
+    }
+    cof_status st = COF_OK;
+    if (s->tables_dirty) st = rebuild_tables(s);
+    if (!st) st = run_step(s);
+    std::vector<ReqPtr> finished;
+    for (const ReqPtr& r : s->active)
+      if (st || ++r->steps_seen >= s->ring) finished.push_back(r);
+    for (const ReqPtr& r : finished) {
+      cof_status fs = st ? st : format_request(s, *r);
+      finish(s, r, fs, fs ? h->err : std::string());
+    }
+    if (!finished.empty()) {
+      std::lock_guard<std::mutex> lock(s->mu);
+      s->active.erase(std::remove_if(s->active.begin(), s->active.end(), [](const ReqPtr& r) { return r->done; }),
+                      s->active.end());
+      s->tables_dirty = true;
+    }
+    s->cur = (s->cur + 1) % s->ring;
+  }
+  // Stopped: requests still queued or running end with COF_ERR_STATE.
+  std::vector<ReqPtr> left;
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    left.insert(left.end(), s->active.begin(), s->active.end());
+    left.insert(left.end(), s->pending.begin(), s->pending.end());
+    s->active.clear();
+    s->pending.clear();
+  }
+  for (const ReqPtr& r : left) finish(s, r, COF_ERR_STATE, "server stopped");
+}
+
+}  // namespace
+
+extern "C" {
+
+cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_t hit_buffer_bytes,
+                            cof_server** out) {
+  if (!h || !out) return COF_ERR_ARG;
+  *out = nullptr;
+  if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
+  cof_server* s = new cof_server();
+  s->h = h;
+  s->max_active_variants = max_active_variants ? max_active_variants : (1u << 17);
+  if (s->max_active_variants >= (1u << 20)) s->max_active_variants = (1u << 20) - 1;
+  s->hit_buffer_bytes = hit_buffer_bytes ? hit_buffer_bytes : (8ull << 30);
+  s->worker = std::thread(worker_main, s);
+  *out = s;
+  return COF_OK;
+}
+
+cof_status cof_server_submit(cof_server* s, const char* text, size_t len, uint64_t* ticket) {
+  if (!s || (!text && len) || !ticket) return COF_ERR_ARG;
+  auto r = std::make_shared<Request>();
+  std::string err;
+  if (!parse_job(text ? text : "", len, r->job, err) || !build_shapes(r->job, err)) {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->last_error = err;
+    return COF_ERR_INPUT;
+  }
+  if (r->job.pattern.size() > (size_t)kMaxL) {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->last_error = "pattern longer than " + std::to_string(kMaxL);
+    return COF_ERR_UNSUPPORTED;
+  }
+  r->nvar = (uint32_t)r->job.variants.size();
+  r->t_submit = now_s();
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    if (s->stop) return COF_ERR_STATE;
+    if (r->nvar >= (1u << 20)) {
+      s->last_error = "request has more than 2^20 compare variants";
+      return COF_ERR_UNSUPPORTED;
+    }
+    r->ticket = s->next_ticket++;
+    *ticket = r->ticket;
+    s->tickets[r->ticket] = r;
+    if (r->nvar == 0) {  // nothing to search: done at once
+      r->done = true;
+      r->t_admit = r->t_done = r->t_submit;
+      ++s->completed;
+      s->cv_done.notify_all();
+      return COF_OK;
+    }
+    s->pending.push_back(r);
+  }
+  s->cv_work.notify_one();
+  return COF_OK;
+}
+
+cof_status cof_server_wait(cof_server* s, uint64_t ticket, int timeout_ms, const char** rows, size_t* rows_len,
+                           double* latency_ms) {
+  if (!s) return COF_ERR_ARG;
+  std::unique_lock<std::mutex> lock(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return COF_ERR_ARG;
+  ReqPtr r = it->second;
+  auto ready = [&] { return r->done; };
+  if (timeout_ms < 0) s->cv_done.wait(lock, ready);
+  else if (!s->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), ready)) return COF_ERR_TIMEOUT;
+  if (rows) *rows = r->rows.data();
+  if (rows_len) *rows_len = r->rows.size();
+  if (latency_ms) *latency_ms = (r->t_done - r->t_submit) * 1e3;
+  if (r->status) s->last_error = r->err;
+  return r->status;
+}
+
+cof_status cof_server_release(cof_server* s, uint64_t ticket) {
+  if (!s) return COF_ERR_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end() || !it->second->done) return COF_ERR_ARG;
+  s->tickets.erase(it);
+  return COF_OK;
+}
+
+cof_status cof_server_stats(cof_server* s, uint64_t* steps, uint64_t* admitted, uint64_t* completed,
+                            uint64_t* pending, uint64_t* active, uint64_t* max_active) {
+  if (!s) return COF_ERR_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (steps) *steps = s->steps.load();
+  if (max_active) *max_active = s->max_active_seen;
+  if (admitted) *admitted = s->admitted;
+  if (completed) *completed = s->completed;
+  if (pending) *pending = s->pending.size();
+  if (active) *active = s->active.size();
+  return COF_OK;
+}
+
+const char* cof_server_last_error(cof_server* s) {
+  if (!s) return "null server";
+  std::lock_guard<std::mutex> lock(s->mu);
+  return s->last_error.c_str();
+}
+
+void cof_server_stop(cof_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  if (s->worker.joinable()) s->worker.join();
+  cudaSetDevice(s->h->device);
+  delete s;
+}
+
+}  // extern "C"

@@ -41,7 +41,8 @@ enum {
   COF_ERR_UNSUPPORTED = 7, /* pattern longer than COF_MAX_PATTERN */
   COF_ERR_NOT_GENOME = 8,  /* file is neither FASTA nor 2BIT ("Skipping non-acceptable file") */
   COF_ERR_DEVICE = 9,      /* a kernel reported an internal inconsistency */
-  COF_ERR_TOO_LARGE = 10   /* input larger than a fixed limit of the entry point */
+  COF_ERR_TOO_LARGE = 10,  /* input larger than a fixed limit of the entry point */
+  COF_ERR_TIMEOUT = 11     /* a wait ended before the request finished */
 };
 
 /* Longest pattern (PAM + spacer + DNA-bulge padding) the kernels accept. */
@@ -115,6 +116,36 @@ cof_status cof_batch_clear(cof_handle* h);
 cof_status cof_batch_add_input(cof_handle* h, const char* text, size_t len, uint32_t* job_index);
 cof_status cof_batch_size(const cof_handle* h, uint32_t* n_jobs);
 cof_status cof_job_rows(const cof_handle* h, uint32_t job, const char** rows, size_t* rows_len);
+/* ---- served mode: continuous batching of requests over the resident genome.
+ * No counterpart in the reference (one input file per process, main.cpp).
+ * A request is one input file (its genome line is ignored).  The server walks
+ * the genome as a ring of segments; every ring step searches one segment for
+ * all active requests, and waiting requests are admitted at any step boundary
+ * while the active compare variants fit `max_active_variants` (0 = 2^17; a
+ * request larger than that runs alone).  A request finishes after one full
+ * ring, wherever it joined.  Active requests with the same padded pattern
+ * share the PAM scan and the comparer launch of each step, but each request's
+ * rows are exactly those of cof_search on that input file alone.  One step's
+ * hits must fit `hit_buffer_bytes` (0 = 8 GiB).  While a server runs, use the
+ * handle only through server calls; submit/wait/release are thread-safe. */
+typedef struct cof_server cof_server;
+cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_t hit_buffer_bytes,
+                            cof_server** out);
+/* Parses and queues a request; *ticket identifies it.  COF_ERR_INPUT (message
+ * in cof_server_last_error) for a malformed input file. */
+cof_status cof_server_submit(cof_server* s, const char* text, size_t len, uint64_t* ticket);
+/* Waits up to timeout_ms (negative: no limit) for a request.  COF_OK: *rows
+ * holds its TSV rows (valid until cof_server_release) and *latency_ms the time
+ * from submit to completion; COF_ERR_TIMEOUT: not finished yet. */
+cof_status cof_server_wait(cof_server* s, uint64_t ticket, int timeout_ms, const char** rows, size_t* rows_len,
+                           double* latency_ms);
+cof_status cof_server_release(cof_server* s, uint64_t ticket);
+cof_status cof_server_stats(cof_server* s, uint64_t* steps, uint64_t* admitted, uint64_t* completed,
+                            uint64_t* pending, uint64_t* active, uint64_t* max_active);
+const char* cof_server_last_error(cof_server* s);
+/* Stops the worker; requests not finished end with COF_ERR_STATE. */
+void cof_server_stop(cof_server* s);
+
 /* Hit count of the last search (hits = (variant, position, strand) triples
  * with mismatches <= threshold, before expansion into bulge rows). */
 cof_status cof_last_hit_count(const cof_handle* h, uint64_t* n_hits, uint64_t* n_rows);

@@ -1,0 +1,89 @@
+"""Served mode: requests admitted while others run (continuous batching over
+the genome ring) give exactly the rows of each input file searched alone."""
+import random
+import threading
+import time
+
+import pytest
+
+import cases
+from test_gpu_batch import batch_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def make_genome_and_requests(P, tmp_path):
+    rng = random.Random(55)
+    seqs = [P.synth_record(512, r, n, n_frac=0.01, n_run_min=50, n_run_max=500)
+            for r, n in enumerate([200000, 120000])]
+    genome = str(tmp_path / "genome.fa")
+    texts = batch_inputs(rng, genome)
+    for t in texts:
+        lines = t.strip().split("\n")
+        pat = lines[1].split()
+        dna = int(pat[1]) if len(pat) == 3 else 0
+        rna = int(pat[2]) if len(pat) == 3 else 0
+        cases.plant_sites(rng, seqs, pat[0], [l.split()[0] for l in lines[2:]], 20, 6, dna, rna)
+    P.write_fasta(genome, ["chr1", "chr2"], seqs)
+    return genome, texts
+
+
+def oracle_rows(oracle, tmp_path, texts):
+    want = []
+    for j, t in enumerate(texts):
+        path = str(tmp_path / f"req{j}.txt")
+        open(path, "w").write(t)
+        out = str(tmp_path / f"req{j}.tsv")
+        r = cases.run_cli(oracle, path, out, threads=4)
+        assert r.returncode == 0, r.stderr.decode()
+        want.append(open(out, "rb").read())
+    return want
+
+
+def test_server_mix_equals_alone(P, built, oracle, tmp_path):
+    genome, texts = make_genome_and_requests(P, tmp_path)
+    want = oracle_rows(oracle, tmp_path, texts)
+    assert all(len(cases.rows_of(w)) > 0 for w in want)
+    with P.CasOFFinder(0) as eng:
+        # A short ring (64 Ki positions per segment would be finer; the genome is
+        # one segment here), so force overlap with a small variant budget.
+        eng.load_genome_file(genome)
+        with P.Server(eng, max_active_variants=120) as srv:
+            tickets = [None] * len(texts)
+
+            def client():
+                for j, t in enumerate(texts):
+                    tickets[j] = srv.submit(t)
+                    time.sleep(0.002)
+
+            th = threading.Thread(target=client)
+            th.start()
+            th.join()
+            got = [srv.wait(t) for t in tickets]
+            stats = srv.stats()
+        for j in range(len(texts)):
+            rows, lat = got[j]
+            assert lat >= 0
+            assert P.HEADER.encode() + rows == want[j], f"request {j} in the mix"
+        assert stats["admitted"] == len(texts) and stats["completed"] == len(texts)
+        assert stats["max_active"] >= 2  # requests ran together
+        # Each request alone on a fresh server: the same rows.
+        with P.Server(eng) as srv:
+            for j in (0, 3):
+                rows, _ = srv.wait(srv.submit(texts[j]))
+                assert P.HEADER.encode() + rows == want[j], f"request {j} alone"
+
+
+def test_server_rejects_bad_input_and_times_out_cleanly(P, built, tmp_path):
+    genome, texts = make_genome_and_requests(P, tmp_path)
+    with P.CasOFFinder(0) as eng:
+        eng.load_genome_file(genome)
+        with P.Server(eng) as srv:
+            with pytest.raises(P.CofError) as e:
+                srv.submit(f"{genome}\nNNNNNNNNNNNNNNNNNNNNNGG\nACGT 3 x y\n")
+            assert "Malformed" in e.value.message
+            t = srv.submit(texts[0])
+            r = srv.wait(t, timeout_ms=0)  # may or may not be done already
+            if r is None:
+                r = srv.wait(t)
+            assert r is not None
