@@ -74,6 +74,86 @@ def batched_jobs(seed=5, n=1024, genome_path="synthetic"):
     return texts
 
 
+SERVED_PAMS = [("NGG", 20, False), ("NRG", 20, False), ("NNGRRT", 21, False), ("TTTV", 23, True)]
+
+
+def served_requests(seed=9, n=12, genome_path="synthetic"):
+    """Requests of the served workload: 1-512 guides (log-uniform), a PAM from
+    {NGG, NRG, NNGRRT, TTTV}, max mismatches 2-6, DNA and RNA bulges 0-2."""
+    import math
+    import random
+    rng = random.Random(seed)
+    out = []
+    for _ in range(n):
+        pam, spacer, pam5 = rng.choice(SERVED_PAMS)
+        ng = int(round(math.exp(rng.uniform(0.0, math.log(512)))))
+        dna, rna = rng.randint(0, 2), rng.randint(0, 2)
+        pattern = (pam + "N" * spacer) if pam5 else ("N" * spacer + pam)
+        lines = [genome_path, pattern + (f" {dna} {rna}" if (dna or rna) else "")]
+        for _ in range(ng):
+            sp = "".join(rng.choice("ACGT") for _ in range(spacer))
+            g = ("N" * len(pam) + sp) if pam5 else (sp + "N" * len(pam))
+            lines.append(f"{g} {rng.randint(2, 6)}")
+        out.append(("\n".join(lines) + "\n", ng))
+    return out
+
+
+def run_served(P, eng, lens, args):
+    """Served mode: the same requests arriving as a Poisson stream at several
+    rates; p50/p99 latency (submit to rows in host memory) and guide-Gbp/s,
+    against the plain path run once per request."""
+    import random
+    import statistics
+    import threading
+    gbp = sum(lens) / 1e9
+    reqs = served_requests(n=args.served_requests)
+    guides = sum(ng for _, ng in reqs)
+    # Plain: each request alone through cof_read_input + cof_search.
+    eng.readInputFile(reqs[0][0])
+    eng.search_view()
+    plain_ms = []
+    for text, _ in reqs:
+        eng.readInputFile(text)
+        eng.synchronize()
+        eng.timer_start()
+        eng.search_view()
+        plain_ms.append(eng.timer_stop())
+    out = {"workload": f"{len(reqs)} requests, 1-512 guides each (log-uniform; {guides} guides), PAM NGG/NRG/"
+                       "NNGRRT/TTTV, mm 2-6, DNA/RNA bulge 0-2, on the same 3.1 Gbp genome",
+           "plain_value": guides * gbp / (sum(plain_ms) / 1e3), "unit": "guide-Gbp/s",
+           "plain_latency_ms": {"p50": statistics.median(plain_ms), "max": max(plain_ms)}, "rates": []}
+    for rate in args.served_rates:
+        rng = random.Random(int(rate * 1000))
+        lat, tickets = [None] * len(reqs), [None] * len(reqs)
+        with P.Server(eng) as srv:
+            t0 = time.perf_counter()
+
+            def client():
+                t = t0
+                for j, (text, _) in enumerate(reqs):
+                    t += rng.expovariate(rate)
+                    d = t - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    tickets[j] = srv.submit(text)
+
+            th = threading.Thread(target=client)
+            th.start()
+            th.join()
+            for j in range(len(reqs)):
+                _, lat[j] = srv.wait(tickets[j])
+            span = time.perf_counter() - t0
+            st = srv.stats()
+        lat_sorted = sorted(lat)
+        p99 = lat_sorted[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
+        out["rates"].append({"arrivals_per_s": rate, "p50_ms": statistics.median(lat), "p99_ms": p99,
+                             "value": guides * gbp / span, "makespan_s": span, "max_active": st["max_active"],
+                             "ring_steps": st["steps"]})
+    out["value"] = max(r["value"] for r in out["rates"])
+    out["speedup_vs_plain"] = out["value"] / out["plain_value"]
+    return out
+
+
 def input_text(genome_path, guides):
     return f"{genome_path}\n{PATTERN} {DNA} {RNA}\n" + "".join(f"{g} {MM}\n" for g in guides)
 
@@ -251,6 +331,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 1,024-guide batched comparison")
     ap.add_argument("--batched-steps", type=int, default=2)
     ap.add_argument("--plain-sample", type=int, default=32, help="plain searches timed for the comparison")
+    ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
+    ap.add_argument("--served-requests", type=int, default=12)
+    ap.add_argument("--served-rates", type=float, nargs="+", default=[2.0, 20.0, 200.0])
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     world, rank, local = dist_setup()
@@ -360,6 +443,7 @@ def main():
 
     launches = int(stats["finder"]["launches"] + stats["comparer"]["launches"] + 2 * stats["format"]["launches"])
     batched = None if args.no_batched else run_batched(P, eng, lens, rates, args)
+    served = None if args.no_served else run_served(P, eng, lens, args)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "guide-Gbp/s", "n_gpus": world, "steps": args.steps,
@@ -381,6 +465,7 @@ def main():
                                 else None, "basis": "0.375 B per genome position (3 bit planes)"},
             "kernel_ms_per_step": {k: v["ms"] / max(1, args.steps) for k, v in stats.items()},
             "batched": batched,
+            "served": served,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "gpu_launches": launches,

@@ -103,7 +103,7 @@ def lib():
             "cof_set_comparer": (c.c_int, [vp, c.c_int]),
             "cof_comparer_info": (c.c_int, [vp, c.POINTER(c.c_int), c.POINTER(c.c_int)]),
             "cof_batch_clear": (c.c_int, [vp]),
-            "cof_server_start": (c.c_int, [vp, u64, u64, c.POINTER(vp)]),
+            "cof_server_start": (c.c_int, [vp, u64, u64, u64, c.POINTER(vp)]),
             "cof_server_submit": (c.c_int, [vp, c.c_char_p, sz, c.POINTER(u64)]),
             "cof_server_wait": (c.c_int, [vp, u64, c.c_int, c.POINTER(c.c_void_p), c.POINTER(sz),
                                           c.POINTER(c.c_double)]),
@@ -366,11 +366,12 @@ class Server:
     """Served mode over an engine's resident genome (see include/cof.h).
     While it runs, use the engine only through this server."""
 
-    def __init__(self, engine, max_active_variants=0, hit_buffer_bytes=0):
+    def __init__(self, engine, max_active_variants=0, hit_buffer_bytes=0, segment_positions=0):
         self._L = engine._L
         self._eng = engine
         s = ctypes.c_void_p()
-        st = self._L.cof_server_start(engine._h, max_active_variants, hit_buffer_bytes, ctypes.byref(s))
+        st = self._L.cof_server_start(engine._h, max_active_variants, hit_buffer_bytes, segment_positions,
+                                      ctypes.byref(s))
         if st != COF_OK:
             raise CofError(st, self._L.cof_last_error(engine._h).decode())
         self._s = s

@@ -423,4 +423,36 @@ void launch_job_bounds(const uint64_t* sorted, uint64_t n, const uint32_t* job_g
   job_bounds_kernel<<<(njobs + 1 + 127) / 128, 128, 0, stream>>>(sorted, n, job_gid0, njobs, offsets, row_bytes, out);
 }
 
+// For each request a (ids from gid0[a]), the index of its first hit in the
+// sorted keys; gid0 has one sentinel entry past the last request.
+__global__ void run_starts_kernel(const uint64_t* __restrict__ sorted, uint64_t n, const uint32_t* __restrict__ gid0,
+                                  uint32_t m, uint64_t* __restrict__ out) {
+  const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= m) return;
+  const uint64_t key = (uint64_t)gid0[a] << 44;
+  uint64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const uint64_t mid = (lo + hi) >> 1;
+    if (sorted[mid] < key) lo = mid + 1;
+    else hi = mid;
+  }
+  out[a] = lo;
+}
+
+__global__ void rebase_hits_kernel(const uint64_t* __restrict__ src, uint64_t n, uint32_t gid0,
+                                   uint64_t* __restrict__ dst) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i] - ((uint64_t)gid0 << 44);
+}
+
+void launch_run_starts(const uint64_t* sorted, uint64_t n, const uint32_t* gid0, uint32_t m, uint64_t* out,
+                       cudaStream_t stream) {
+  run_starts_kernel<<<(m + 127) / 128, 128, 0, stream>>>(sorted, n, gid0, m, out);
+}
+
+void launch_rebase_hits(const uint64_t* src, uint64_t n, uint32_t gid0, uint64_t* dst, cudaStream_t stream) {
+  if (!n) return;
+  rebase_hits_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(src, n, gid0, dst);
+}
+
 }  // namespace cof

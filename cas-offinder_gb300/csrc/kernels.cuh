@@ -130,4 +130,11 @@ void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64
 void launch_job_bounds(const uint64_t* sorted, uint64_t n, const uint32_t* job_gid0, uint32_t njobs,
                        const uint64_t* offsets, const uint64_t* row_bytes, uint64_t* out, cudaStream_t stream);
 
+// Served mode: first index of each of m requests' id ranges (ids from
+// gid0[a]) in sorted hit keys, and a copy of a run of keys with the request's
+// first id subtracted.
+void launch_run_starts(const uint64_t* sorted, uint64_t n, const uint32_t* gid0, uint32_t m, uint64_t* out,
+                       cudaStream_t stream);
+void launch_rebase_hits(const uint64_t* src, uint64_t n, uint32_t gid0, uint64_t* dst, cudaStream_t stream);
+
 }  // namespace cof

@@ -44,7 +44,8 @@ struct Request {
   double t_submit = 0, t_admit = 0, t_done = 0;
   uint64_t steps_seen = 0;
   uint32_t gid0 = 0;            // first id of its variants in the active tables
-  std::vector<uint64_t> hits;   // hit keys with request-local variant ids
+  DevBuf hits;                  // device hit keys with request-local variant ids
+  uint64_t n_hits = 0;
   bool done = false;
   cof_status status = COF_OK;
   std::string err;
@@ -76,9 +77,10 @@ struct cof_server {
   // worker-only state
   std::vector<PatternGroup> groups;
   bool tables_dirty = true;
-  uint64_t ring = 0, cur = 0;  // ring length in segments, current segment
-  DevBuf step_hits, step_count, fmt_hits, fmt_sorted, fmt_bytes, fmt_off, fmt_cnt, fmt_tmp, fmt_text, fmt_vf, fmt_sf,
-      fmt_pool, fmt_small;
+  uint64_t seg_words = kSegWords;  // plane words (32 start positions each) per ring segment
+  uint64_t ring = 0, cur = 0;      // ring length in segments, current segment
+  DevBuf step_hits, step_sorted, step_count, step_bounds, step_gid0, sort_tmp, fmt_hits, fmt_bytes, fmt_off, fmt_cnt,
+      fmt_tmp, fmt_text, fmt_vf, fmt_sf, fmt_pool, fmt_small;
 };
 
 namespace {
@@ -137,7 +139,7 @@ cof_status run_step(cof_server* s) {
       const PatternGroup& g = s->groups[gi];
       const uint64_t npos = n >= g.L ? n - g.L + 1 : 0;
       const uint64_t words = (npos + 31) / 32;
-      const uint64_t w0 = s->cur * kSegWords, w1 = std::min(words, w0 + kSegWords);
+      const uint64_t w0 = s->cur * s->seg_words, w1 = std::min(words, w0 + s->seg_words);
       if (w0 >= w1 || g.gids.empty()) continue;
       const int b = (int)(pass & 1);
       uint32_t* qc = h->qcounts.as<uint32_t>() + gi;
@@ -169,20 +171,46 @@ cof_status run_step(cof_server* s) {
     COF_CUDA(h, s->step_hits.ensure(cap * 8));
   }
   if (count) {
-    std::vector<uint64_t> keys(count);
-    COF_CUDA(h, cudaMemcpy(keys.data(), s->step_hits.p, count * 8, cudaMemcpyDeviceToHost));
-    // Requests own consecutive id ranges in admission order.
-    for (uint64_t k : keys) {
-      const uint32_t gid = (uint32_t)(k >> 44);
-      size_t a = 0, z = s->active.size();
-      while (z - a > 1) {
-        const size_t mid = (a + z) / 2;
-        if (s->active[mid]->gid0 <= gid) a = mid;
-        else z = mid;
-      }
+    // Sort the step's hits: each request's ids are one consecutive range, so
+    // its hits become one run, appended to the request's own device buffer.
+    const size_t A = s->active.size();
+    COF_CUDA(h, s->step_sorted.ensure(count * 8));
+    COF_CUDA(h, s->step_bounds.ensure((A + 1) * 8));
+    COF_CUDA(h, s->step_gid0.ensure((A + 1) * 4));
+    size_t tmp = 0;
+    COF_CUDA(h, cub::DeviceRadixSort::SortKeys(nullptr, tmp, s->step_hits.as<uint64_t>(),
+                                               s->step_sorted.as<uint64_t>(), (int64_t)count, 0, 64, h->stream));
+    COF_CUDA(h, s->sort_tmp.ensure(tmp));
+    tmp = s->sort_tmp.cap;
+    COF_CUDA(h, cub::DeviceRadixSort::SortKeys(s->sort_tmp.p, tmp, s->step_hits.as<uint64_t>(),
+                                               s->step_sorted.as<uint64_t>(), (int64_t)count, 0, 64, h->stream));
+    std::vector<uint32_t> gid0(A);
+    for (size_t a = 0; a < A; ++a) gid0[a] = s->active[a]->gid0;
+    COF_CUDA(h, cudaMemcpyAsync(s->step_gid0.p, gid0.data(), A * 4, cudaMemcpyHostToDevice, h->stream));
+    launch_run_starts(s->step_sorted.as<uint64_t>(), count, s->step_gid0.as<uint32_t>(), (uint32_t)A,
+                      s->step_bounds.as<uint64_t>(), h->stream);
+    std::vector<uint64_t> start(A + 1);
+    COF_CUDA(h, cudaMemcpyAsync(start.data(), s->step_bounds.p, A * 8, cudaMemcpyDeviceToHost, h->stream));
+    COF_CUDA(h, cudaStreamSynchronize(h->stream));
+    start[A] = count;
+    for (size_t a = 0; a < A; ++a) {
       Request& r = *s->active[a];
-      r.hits.push_back(((uint64_t)(gid - r.gid0) << 44) | (k & ((1ull << 44) - 1)));
+      const uint64_t k = start[a + 1] - start[a];
+      if (!k) continue;
+      if ((r.n_hits + k) * 8 > r.hits.cap) {  // grow by doubling, keeping the hits so far
+        DevBuf bigger;
+        COF_CUDA(h, bigger.ensure(std::max<uint64_t>((r.n_hits + k) * 8, 2 * r.hits.cap)));
+        if (r.n_hits)
+          COF_CUDA(h, cudaMemcpyAsync(bigger.p, r.hits.p, r.n_hits * 8, cudaMemcpyDeviceToDevice, h->stream));
+        COF_CUDA(h, cudaStreamSynchronize(h->stream));
+        std::swap(r.hits.p, bigger.p);
+        std::swap(r.hits.cap, bigger.cap);
+      }
+      launch_rebase_hits(s->step_sorted.as<uint64_t>() + start[a], k, r.gid0, r.hits.as<uint64_t>() + r.n_hits,
+                         h->stream);
+      r.n_hits += k;
     }
+    COF_CUDA(h, cudaGetLastError());
   }
   ++s->steps;
   return COF_OK;
@@ -191,8 +219,7 @@ cof_status run_step(cof_server* s) {
 // Sorts a finished request's hits and formats its rows on the device.
 cof_status format_request(cof_server* s, Request& r) {
   cof_handle* h = s->h;
-  std::sort(r.hits.begin(), r.hits.end());
-  const uint64_t nh = r.hits.size();
+  const uint64_t nh = r.n_hits;
   if (!nh) return COF_OK;
   std::vector<VariantFmt> vf;
   std::vector<ShapeFmt> sf;
@@ -211,17 +238,21 @@ cof_status format_request(cof_server* s, Request& r) {
     COF_CUDA(h, cudaMemcpyAsync(s->fmt_sf.p, sf.data(), sf.size() * sizeof(ShapeFmt), cudaMemcpyHostToDevice, h->stream));
   if (!pool.empty())
     COF_CUDA(h, cudaMemcpyAsync(s->fmt_pool.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, h->stream));
-  COF_CUDA(h, cudaMemcpyAsync(s->fmt_hits.p, r.hits.data(), nh * 8, cudaMemcpyHostToDevice, h->stream));
-  const GenomeView gv = h->genome.view();
-  FormatTables ft{s->fmt_vf.as<VariantFmt>(), s->fmt_sf.as<ShapeFmt>(), s->fmt_pool.as<char>()};
-  launch_row_lengths(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_bytes.as<uint64_t>(), s->fmt_cnt.as<uint32_t>(),
-                     h->stream);
-  size_t t1 = 0, t2 = 0;
+  size_t t0 = 0, t1 = 0, t2 = 0;
+  COF_CUDA(h, cub::DeviceRadixSort::SortKeys(nullptr, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
+                                             (int64_t)nh, 0, 64, h->stream));
   COF_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
                                             (int64_t)nh, h->stream));
   COF_CUDA(h, cub::DeviceReduce::Sum(nullptr, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(), (int64_t)nh,
                                      h->stream));
-  COF_CUDA(h, s->fmt_tmp.ensure(std::max(t1, t2)));
+  COF_CUDA(h, s->fmt_tmp.ensure(std::max(t0, std::max(t1, t2))));
+  t0 = s->fmt_tmp.cap;
+  COF_CUDA(h, cub::DeviceRadixSort::SortKeys(s->fmt_tmp.p, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
+                                             (int64_t)nh, 0, 64, h->stream));
+  const GenomeView gv = h->genome.view();
+  FormatTables ft{s->fmt_vf.as<VariantFmt>(), s->fmt_sf.as<ShapeFmt>(), s->fmt_pool.as<char>()};
+  launch_row_lengths(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_bytes.as<uint64_t>(), s->fmt_cnt.as<uint32_t>(),
+                     h->stream);
   t1 = s->fmt_tmp.cap;
   COF_CUDA(h, cub::DeviceScan::ExclusiveSum(s->fmt_tmp.p, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
                                             (int64_t)nh, h->stream));
@@ -251,8 +282,6 @@ void finish(cof_server* s, const ReqPtr& r, cof_status st, const std::string& er
   r->err = err;
   r->done = true;
   r->t_done = now_s();
-  r->hits.clear();
-  r->hits.shrink_to_fit();
   ++s->completed;
   s->cv_done.notify_all();
 }
@@ -261,7 +290,7 @@ void worker_main(cof_server* s) {
   cof_handle* h = s->h;
   cudaSetDevice(h->device);
   const uint64_t words = (h->genome.n + 31) / 32;
-  s->ring = std::max<uint64_t>(1, (words + kSegWords - 1) / kSegWords);
+  s->ring = std::max<uint64_t>(1, (words + s->seg_words - 1) / s->seg_words);
   for (;;) {
     {
       std::unique_lock<std::mutex> lock(s->mu);
@@ -292,6 +321,11 @@ void worker_main(cof_server* s) {
       if (st || ++r->steps_seen >= s->ring) finished.push_back(r);
     for (const ReqPtr& r : finished) {
       cof_status fs = st ? st : format_request(s, *r);
+      if (r->hits.p) {  // the request's device hits are no longer needed
+        cudaFree(r->hits.p);
+        r->hits.p = nullptr;
+        r->hits.cap = 0;
+      }
       finish(s, r, fs, fs ? h->err : std::string());
     }
     if (!finished.empty()) {
@@ -311,7 +345,14 @@ void worker_main(cof_server* s) {
     s->active.clear();
     s->pending.clear();
   }
-  for (const ReqPtr& r : left) finish(s, r, COF_ERR_STATE, "server stopped");
+  for (const ReqPtr& r : left) {
+    if (r->hits.p) {
+      cudaFree(r->hits.p);
+      r->hits.p = nullptr;
+      r->hits.cap = 0;
+    }
+    finish(s, r, COF_ERR_STATE, "server stopped");
+  }
 }
 
 }  // namespace
@@ -319,7 +360,7 @@ void worker_main(cof_server* s) {
 extern "C" {
 
 cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_t hit_buffer_bytes,
-                            cof_server** out) {
+                            uint64_t segment_positions, cof_server** out) {
   if (!h || !out) return COF_ERR_ARG;
   *out = nullptr;
   if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
@@ -328,6 +369,7 @@ cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_
   s->max_active_variants = max_active_variants ? max_active_variants : (1u << 17);
   if (s->max_active_variants >= (1u << 20)) s->max_active_variants = (1u << 20) - 1;
   s->hit_buffer_bytes = hit_buffer_bytes ? hit_buffer_bytes : (8ull << 30);
+  if (segment_positions) s->seg_words = std::min<uint64_t>(kSegWords, std::max<uint64_t>(1, segment_positions / 32));
   s->worker = std::thread(worker_main, s);
   *out = s;
   return COF_OK;

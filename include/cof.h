@@ -129,8 +129,11 @@ cof_status cof_job_rows(const cof_handle* h, uint32_t job, const char** rows, si
  * hits must fit `hit_buffer_bytes` (0 = 8 GiB).  While a server runs, use the
  * handle only through server calls; submit/wait/release are thread-safe. */
 typedef struct cof_server cof_server;
+/* `segment_positions` sets the ring's granularity (rounded down to a multiple
+ * of 32, at most 2^26 = the default for 0): smaller segments let requests join
+ * and leave sooner at the cost of more launches per ring. */
 cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_t hit_buffer_bytes,
-                            cof_server** out);
+                            uint64_t segment_positions, cof_server** out);
 /* Parses and queues a request; *ticket identifies it.  COF_ERR_INPUT (message
  * in cof_server_last_error) for a malformed input file. */
 cof_status cof_server_submit(cof_server* s, const char* text, size_t len, uint64_t* ticket);

@@ -2,7 +2,6 @@
 the genome ring) give exactly the rows of each input file searched alone."""
 import random
 import threading
-import time
 
 import pytest
 
@@ -45,16 +44,16 @@ def test_server_mix_equals_alone(P, built, oracle, tmp_path):
     want = oracle_rows(oracle, tmp_path, texts)
     assert all(len(cases.rows_of(w)) > 0 for w in want)
     with P.CasOFFinder(0) as eng:
-        # A short ring (64 Ki positions per segment would be finer; the genome is
-        # one segment here), so force overlap with a small variant budget.
+        # 32 Ki positions per segment: a ring of 10 segments over this genome,
+        # and a small variant budget, so requests join the ring mid-way while
+        # others are running.
         eng.load_genome_file(genome)
-        with P.Server(eng, max_active_variants=120) as srv:
+        with P.Server(eng, max_active_variants=250, segment_positions=1 << 15) as srv:
             tickets = [None] * len(texts)
 
-            def client():
+            def client():  # back to back: later requests arrive while the first ones run
                 for j, t in enumerate(texts):
                     tickets[j] = srv.submit(t)
-                    time.sleep(0.002)
 
             th = threading.Thread(target=client)
             th.start()
@@ -67,8 +66,9 @@ def test_server_mix_equals_alone(P, built, oracle, tmp_path):
             assert P.HEADER.encode() + rows == want[j], f"request {j} in the mix"
         assert stats["admitted"] == len(texts) and stats["completed"] == len(texts)
         assert stats["max_active"] >= 2  # requests ran together
+        assert stats["steps"] > 10  # more steps than one ring: requests joined mid-ring
         # Each request alone on a fresh server: the same rows.
-        with P.Server(eng) as srv:
+        with P.Server(eng, segment_positions=1 << 15) as srv:
             for j in (0, 3):
                 rows, _ = srv.wait(srv.submit(texts[j]))
                 assert P.HEADER.encode() + rows == want[j], f"request {j} alone"
