@@ -159,13 +159,16 @@ cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<
   std::vector<unsigned char> masks(std::max<size_t>(V, 1) * msz, 0);
   int maxpos = 0;
   g.nonN_sum = 0;
+  g.concrete_only = true;
   for (size_t i = 0; i < V; ++i) {
     const Variant& var = *vars[i];
     if (g.nw == 1) fill_mask<1>(((VariantMask<1>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
     else fill_mask<2>(((VariantMask<2>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
     int c = 0;
     for (char ch : var.key) {
-      c += bs_class_of((unsigned char)ch) != 0;
+      const uint32_t cls = bs_class_of((unsigned char)ch);
+      c += cls != 0;
+      if (cls > 4) g.concrete_only = false;
       g.nonN_sum += ch != 'N';
     }
     maxpos = std::max(maxpos, c);
@@ -311,8 +314,14 @@ cof_status record_start(cof_handle* h, std::vector<EventPair>& evs, const char* 
   EventPair p;
   p.name = name;
   p.units = units;
-  COF_CUDA(h, cudaEventCreate(&p.a));
-  COF_CUDA(h, cudaEventCreate(&p.b));
+  for (cudaEvent_t* e : {&p.a, &p.b}) {
+    if (!h->event_pool.empty()) {
+      *e = h->event_pool.back();
+      h->event_pool.pop_back();
+    } else {
+      COF_CUDA(h, cudaEventCreate(e));
+    }
+  }
   COF_CUDA(h, cudaEventRecord(p.a, st));
   evs.push_back(p);
   return COF_OK;
@@ -331,8 +340,8 @@ void collect(cof_handle* h, std::vector<EventPair>& evs) {
       s.ms += ms;
       s.units += p.units;
     }
-    cudaEventDestroy(p.a);
-    cudaEventDestroy(p.b);
+    h->event_pool.push_back(p.a);
+    h->event_pool.push_back(p.b);
   }
   evs.clear();
 }
@@ -382,7 +391,7 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       const uint32_t V = (uint32_t)g.gids.size();
       if (!g.bs_slots ||
           !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_off.as<uint32_t>(), g.bs_thr.as<uint32_t>(),
-                              g.bs_gid.as<uint32_t>(), V, g.bs_slots, g.L, h->hits.as<uint64_t>(),
+                              g.bs_gid.as<uint32_t>(), V, g.bs_slots, g.L, g.concrete_only, h->hits.as<uint64_t>(),
                               h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream))
         launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, h->hits.as<uint64_t>(),
                         h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream);
@@ -424,8 +433,8 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
     COF_CUDA(h, cudaStreamSynchronize(h->stream));
     if (nhits <= cap) break;
     for (EventPair& p : evs) {  // discard the overflowing pass's timings
-      cudaEventDestroy(p.a);
-      cudaEventDestroy(p.b);
+      h->event_pool.push_back(p.a);
+      h->event_pool.push_back(p.b);
     }
     evs.clear();
     cap = nhits + nhits / 8;
@@ -603,6 +612,7 @@ void cof_close(cof_handle* h) {
   cudaStream_t s = h->stream, s2 = h->stream2;
   cudaEvent_t evs[7] = {h->timer_a, h->timer_b, h->ev_start, h->ev_found[0], h->ev_found[1], h->ev_used[0],
                         h->ev_used[1]};
+  for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
   delete h;  // frees device buffers
   for (cudaEvent_t ev : evs)
     if (ev) cudaEventDestroy(ev);

@@ -95,6 +95,7 @@ struct PatternGroup {
   FinderPattern fpat{};
   int nw = 1;                  // 32-bit words per window (popcount comparer)
   int bs_slots = 0;            // bit-sliced slot count, 0 = popcount comparer
+  bool concrete_only = true;   // no variant uses a degenerate IUPAC code
   std::vector<uint32_t> gids;  // global variant ids, ascending
   double nonN_sum = 0;         // sum of non-N positions over the group's variants
   DevBuf vmask, bs_off, bs_thr, bs_gid;
@@ -136,6 +137,7 @@ struct cof_handle {
 
   bool profiling = false;
   std::map<std::string, KernelStat> stats;
+  std::vector<cudaEvent_t> event_pool;  // reused timing events (profiling)
   cudaEvent_t timer_a = nullptr, timer_b = nullptr;
 };
 

@@ -110,10 +110,12 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
 // byte offsets ((class * row + k) * 8, 0 = padding), packed two per word;
 // `vthr` the thresholds; `vgid` the global variant indices.  Returns false if
 // no kernel instance fits (then use launch_comparer).
+// `concrete_only`: no variant uses a degenerate IUPAC code (only the four
+// concrete-base class rows are built).
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                         const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, int slots,
-                        uint32_t L, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
-                        cudaStream_t stream);
+                        uint32_t L, bool concrete_only, uint64_t* hits, unsigned long long* hit_count,
+                        uint64_t hit_cap, int sm_count, cudaStream_t stream);
 int bs_slots_for(int max_positions);  // 0 when more than 32 positions can mismatch
 int bs_row_for(uint32_t L);           // words per class row of the shared table
 uint32_t bs_class_of(unsigned char p);  // class row of a pattern byte (0: never mismatches)
