@@ -220,10 +220,15 @@ __device__ __forceinline__ void load_variant(const uint32_t* __restrict__ voff, 
 template <int S, int ROW>
 __device__ __forceinline__ void count_tile(const uint32_t (&packed)[S / 2], uint32_t kadd, uint32_t gid, bool active,
                                            const uint2* table, const uint32_t* ents, uint32_t ntile, unsigned G,
-                                           uint64_t seg_pos0, uint64_t* __restrict__ hits,
-                                           unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+                                           const uint32_t (&gvalid)[kGroups], uint64_t seg_pos0,
+                                           uint64_t* __restrict__ hits, unsigned long long* __restrict__ hit_count,
+                                           uint64_t hit_cap) {
   constexpr int NB = bit_width(S);
   constexpr int kPairWords = 16 * ROW;
+  uint32_t kmask[NB];  // bit i of the threshold constant as an all-ones / all-zeros word
+#pragma unroll
+  for (int i = 0; i < NB; ++i) kmask[i] = 0u - ((kadd >> i) & 1u);
+  const uint32_t lane_on = active ? kFull : 0u;
   uint32_t off[S];
 #pragma unroll
   for (int s = 0; s < S; s += 2) {
@@ -242,9 +247,8 @@ __device__ __forceinline__ void count_tile(const uint32_t (&packed)[S / 2], uint
       CountTree<S, 0, NB>::run(xa, ba);
       uint32_t ca = 0;
 #pragma unroll
-      for (int i = 0; i < NB; ++i) ca = maj3(ba[i], ((kadd >> i) & 1) ? kFull : 0u, ca);
-      const uint32_t na = min(32u, ntile - (uint32_t)p * 64);
-      uint32_t hm = ~ca & (active ? (na == 32 ? kFull : ((1u << na) - 1)) : 0u);
+      for (int i = 0; i < NB; ++i) ca = maj3(ba[i], kmask[i], ca);
+      uint32_t hm = ~ca & gvalid[2 * p] & lane_on;
       while (hm) {
         const unsigned c = __ffs(hm) - 1;
         hm &= hm - 1;
@@ -270,15 +274,10 @@ __device__ __forceinline__ void count_tile(const uint32_t (&packed)[S / 2], uint
     uint32_t ca = 0, cb = 0;
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
-      const uint32_t ki = ((kadd >> i) & 1) ? kFull : 0u;
-      ca = maj3(ba[i], ki, ca);
-      cb = maj3(bb[i], ki, cb);
+      ca = maj3(ba[i], kmask[i], ca);
+      cb = maj3(bb[i], kmask[i], cb);
     }
-    const uint32_t na = min(32u, ntile - min(ntile, (uint32_t)p * 64));
-    const uint32_t nb = min(32u, ntile - min(ntile, (uint32_t)p * 64 + 32));
-    const uint32_t va = active ? (na == 32 ? kFull : ((1u << na) - 1)) : 0u;
-    const uint32_t vbm = active ? (nb == 32 ? kFull : ((1u << nb) - 1)) : 0u;
-    const uint32_t hita = ~ca & va, hitb = ~cb & vbm;
+    const uint32_t hita = ~ca & gvalid[2 * p] & lane_on, hitb = ~cb & gvalid[2 * p + 1] & lane_on;
     if (hita | hitb) {
 #pragma unroll
       for (int half = 0; half < 2; ++half) {
@@ -300,7 +299,7 @@ __device__ __forceinline__ void count_tile(const uint32_t (&packed)[S / 2], uint
 }
 
 template <int S, int ROW, int NK>
-__global__ void __launch_bounds__(32 * kMaxWarps, (S <= 20 ? 3 : 2)) comparer_bs_kernel(
+__global__ void __launch_bounds__(32 * kMaxWarps, (S <= 20 ? 4 : S <= 28 ? 3 : 2)) comparer_bs_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
     const uint32_t* __restrict__ queue, const uint32_t* __restrict__ qcount, uint64_t seg_pos0,
     const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vthr, const uint32_t* __restrict__ vgid,
@@ -349,9 +348,16 @@ __global__ void __launch_bounds__(32 * kMaxWarps, (S <= 20 ? 3 : 2)) comparer_bs
     const uint2* table = tables + B * kBufWords;
     const uint32_t* ents = ents_all + B * (kGroups * 32);
     const uint32_t ntile = min(tile_n, n - t * tile_n);
+    uint32_t gvalid[kGroups];  // candidates present in each group of the tile
+#pragma unroll
+    for (int g = 0; g < kGroups; ++g) {
+      const uint32_t have = ntile > (uint32_t)g * 32 ? ntile - (uint32_t)g * 32 : 0u;
+      gvalid[g] = have >= 32 ? kFull : ((1u << have) - 1);
+    }
     for (uint32_t vb = warp * 32; vb < nvar; vb += blockDim.x) {
       if (!one_chunk) load_variant<S>(voff, vthr, vgid, nvar, vb + lane, packed0, kadd0, gid0, active0);
-      count_tile<S, ROW>(packed0, kadd0, gid0, active0, table, ents, ntile, G, seg_pos0, hits, hit_count, hit_cap);
+      count_tile<S, ROW>(packed0, kadd0, gid0, active0, table, ents, ntile, G, gvalid, seg_pos0, hits, hit_count,
+                         hit_cap);
     }
     if (tn < ntiles)
       build_group<NK, ROW>(raw0, seg_pos0, L, lane, tables + (B ^ 1) * kBufWords + (warp >> 1) * kPairWords, warp & 1,

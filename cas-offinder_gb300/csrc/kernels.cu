@@ -46,10 +46,11 @@ __device__ __forceinline__ uint32_t bits_at(uint32_t w0, uint32_t w1, uint32_t w
 
 // ---------------------------------------------------------------- finder
 // One thread = 32 consecutive start positions (one plane word).  A warp's
-// candidates are staged in shared memory in scan order, then written to the
-// queue with one atomic reservation and coalesced stores.
+// candidates (up to kFinderStage) are staged in shared memory in scan order,
+// then written to the queue with one atomic reservation and coalesced stores;
+// a warp with more candidates (dense patterns) stores them directly.
 constexpr int kFinderThreads = 128;
-constexpr int kFinderStage = 32 * 64;  // a warp emits at most 32 words x 32 starts x 2 strands
+constexpr int kFinderStage = 512;  // staged entries per warp; denser warps store directly
 
 __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
@@ -101,24 +102,28 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     }
     const uint32_t total = __shfl_sync(kFull, incl, 31);
     if (total == 0) continue;  // warp-uniform
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(qcount, total);
+    base = __shfl_sync(kFull, base, 0);
+    const bool staged = total <= (uint32_t)kFinderStage;  // warp-uniform
+    uint32_t* dst = staged ? my : queue + base;
     uint32_t at = incl - cnt;
     const uint32_t rel = (uint32_t)((w - w_begin) << 5);
     while (fwd) {
       const unsigned b = __ffs(fwd) - 1;
       fwd &= fwd - 1;
-      my[at++] = (rel + b) << 1;
+      dst[at++] = (rel + b) << 1;
     }
     while (rev) {
       const unsigned b = __ffs(rev) - 1;
       rev &= rev - 1;
-      my[at++] = ((rel + b) << 1) | 1u;
+      dst[at++] = ((rel + b) << 1) | 1u;
     }
-    __syncwarp();
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(qcount, total);
-    base = __shfl_sync(kFull, base, 0);
-    for (uint32_t i = lane; i < total; i += 32) queue[base + i] = my[i];
-    __syncwarp();
+    if (staged) {
+      __syncwarp();
+      for (uint32_t i = lane; i < total; i += 32) queue[base + i] = my[i];
+      __syncwarp();
+    }
   }
 }
 
