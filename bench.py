@@ -193,6 +193,13 @@ class ClockSampler:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
                                           "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            # Timing starts once sampling runs, so nvidia-smi's start-up
+            # stays outside the timed region.
+            t0 = time.time()
+            while time.time() - t0 < 5.0 and self.proc.poll() is None:
+                if os.path.exists(self.path) and os.path.getsize(self.path) > 0:
+                    break
+                time.sleep(0.01)
         return self
 
     def __exit__(self, *exc):
@@ -322,7 +329,7 @@ def run_reference_arm(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--genome-gbp", type=float, default=3.1)

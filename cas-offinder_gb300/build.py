@@ -28,6 +28,9 @@ CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
 CU_SOURCES = ["kernels.cu", "comparer_bs.cu", "engine.cu", "server.cu", "pipe_rates.cu", "noalloc.cu"]
 CPP_SOURCES = ["input.cpp", "genome_io.cpp", "synth.cpp"]
+# comparer_bs_inst.cu is compiled once per (table row words, window words,
+# concrete-only) instance set of the bit-sliced comparer.
+BS_INSTANCES = [(row, nk, conc) for row, nk in ((36, 1), (36, 2), (68, 2)) for conc in (1, 0)]
 
 
 def nvcc():
@@ -64,16 +67,20 @@ def build(verbose=False):
     hdrs = _headers()
     jobs = []
     objs = []
-    for src in CU_SOURCES + CPP_SOURCES:
+    units = [(src, src + ".o", []) for src in CU_SOURCES + CPP_SOURCES]
+    units += [("comparer_bs_inst.cu", f"comparer_bs_{row}_{nk}_{conc}.o",
+               [f"-DCOF_BS_ROW={row}", f"-DCOF_BS_NK={nk}", f"-DCOF_BS_CONC={conc}"])
+              for row, nk, conc in BS_INSTANCES]
+    for src, oname, defs in units:
         path = os.path.join(CSRC, src)
         if not os.path.exists(path):
             continue
-        obj = os.path.join(BUILD, src + ".o")
+        obj = os.path.join(BUILD, oname)
         objs.append(obj)
         if not _stale(obj, [path] + hdrs):
             continue
         if src.endswith(".cu"):
-            cmd = [nvcc(), *NVCC_FLAGS, "-c", path, "-o", obj]
+            cmd = [nvcc(), *NVCC_FLAGS, *defs, "-c", path, "-o", obj]
         else:
             cmd = ["g++", *CXX_FLAGS, "-c", path, "-o", obj]
         jobs.append(cmd)

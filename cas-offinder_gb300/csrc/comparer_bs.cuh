@@ -1,0 +1,486 @@
+// Bit-sliced comparer: replaces comparer/comparer_cpu (cas-offinder.cl:73-155,
+// :214-286) for compare variants with at most 32 positions that can mismatch.
+//
+// Work unit: a tile of 64*W strand-oriented candidates (W pairs of 32-candidate
+// groups, W = warps = ceil(variants / 32), at most 8) against every compare
+// variant.
+//  1. Build: warp w builds pair w.  Each lane extracts two candidates'
+//     oriented windows from the genome planes (loaded one tile ahead); 32x32
+//     bit transposes (shuffles) turn the windows of a group into per-position
+//     words whose bit c is candidate c.  Lane k then writes, for window
+//     position k, the class words: for each kind of pattern byte (concrete
+//     base, 3-base code, 2-base code) the mismatch mask of the two groups as
+//     one uint2 (one LOP3 each), so one 64-bit shared load serves 64
+//     candidates.  Variants that use only A/C/G/T (and N) need 4 class rows
+//     instead of 14, and the table shrinks to match.  Two table buffers: tile
+//     t+1 is built while tile t is counted, one barrier per tile.
+//  2. Count: each lane owns one compare variant, described by the list of its
+//     positions that can mismatch as shared-memory addresses of the matching
+//     class word (N positions are skipped).  Per pair the lane loads one uint2
+//     per listed position ([register + immediate] addressing, no arithmetic)
+//     and adds the words bit-sliced with a carry-save full-adder tree (explicit
+//     LOP3: 2 per word), so the candidates' mismatch counts come out as 5-6 bit
+//     planes.  A carry chain against the variant's threshold gives the hit
+//     mask; hits (rare; one warp-uniform branch per pair) decode their exact
+//     count from the planes.  Entries past the end of the queue are dropped
+//     there, so full and partial tiles run the same code.
+// Per lane and 64 candidates: S loads + ~4.1 S LOP3 for 64 variant tests.
+//
+// Kernel templates; comparer_bs_inst.cu instantiates them, once per
+// (ROW, NK, CONC) object, so the instances compile in parallel.
+#pragma once
+#include <algorithm>
+#include <type_traits>
+
+#include "kernels.cuh"
+
+namespace cof {
+namespace bs {
+
+namespace {
+
+constexpr unsigned kFull = 0xFFFFFFFFu;
+constexpr int kMaxWarps = 8;  // warps per block (one group each)
+
+// One LOP3 with truth table LUT over (a, b, c) = (0xF0, 0xCC, 0xAA).
+template <uint32_t LUT>
+__device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("lop3.b32 %0, %1, %2, %3, %4;" : "=r"(d) : "r"(a), "r"(b), "r"(c), "n"(LUT));
+  return d;
+}
+__device__ __forceinline__ uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) { return lop3<0xE8>(a, b, c); }
+__device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) { return lop3<0x96>(a, b, c); }
+
+// 32x32 bit transpose across the warp: lane i holds row i; afterwards lane i
+// holds column i (bit j = bit i of row j).
+__device__ __forceinline__ uint32_t warp_transpose(uint32_t x, unsigned lane) {
+#pragma unroll
+  for (int j = 16; j > 0; j >>= 1) {
+    const uint32_t m = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu : j == 2 ? 0x33333333u
+                                                                                                    : 0x55555555u;
+    const bool upper = (lane & j) != 0;
+    const uint32_t y = __shfl_xor_sync(kFull, x, j);
+    // upper lanes take the partner's bits shifted down, lower lanes shifted up;
+    // a rotate moves them in both cases without touching the kept half.
+    const uint32_t r = __funnelshift_l(y, y, upper ? 32 - j : j);
+    const uint32_t keep = upper ? ~m : m;
+    x = lop3<0xE2>(x, keep, r);  // (x & keep) | (r & ~keep)
+  }
+  return x;
+}
+
+
+
+// Reduces N bit-sliced one-bit inputs of weight 2^LEV to binary planes.
+template <int N, int LEV, int NB>
+struct CountTree {
+  static constexpr int kFA = N >= 3 ? (N - 1) / 2 : 0;
+  static constexpr int kLeft = N - 2 * kFA;
+  static constexpr int kCarry = kFA + (kLeft == 2 ? 1 : 0);
+  __device__ __forceinline__ static void run(const uint32_t* v, uint32_t* bits) {
+    uint32_t c[kCarry > 0 ? kCarry : 1];
+    uint32_t acc = v[0];
+#pragma unroll
+    for (int f = 0; f < kFA; ++f) {
+      const uint32_t a = v[1 + 2 * f], b = v[2 + 2 * f];
+      c[f] = maj3(acc, a, b);
+      acc = xor3(acc, a, b);
+    }
+    if (kLeft == 2) {
+      c[kFA] = acc & v[N - 1];
+      acc ^= v[N - 1];
+    }
+    if (LEV < NB) bits[LEV] = acc;
+    CountTree<kCarry, LEV + 1, NB>::run(c, bits);
+  }
+};
+template <int LEV, int NB>
+struct CountTree<1, LEV, NB> {
+  __device__ __forceinline__ static void run(const uint32_t* v, uint32_t* bits) {
+    if (LEV < NB) bits[LEV] = v[0];
+#pragma unroll
+    for (int i = LEV + 1; i < NB; ++i) bits[i] = 0;
+  }
+};
+template <int LEV, int NB>
+struct CountTree<0, LEV, NB> {
+  __device__ __forceinline__ static void run(const uint32_t*, uint32_t* bits) {
+#pragma unroll
+    for (int i = LEV; i < NB; ++i) bits[i] = 0;
+  }
+};
+
+__host__ __device__ constexpr int bit_width(int s) { return s <= 1 ? 1 : 1 + bit_width(s >> 1); }
+
+// Raw genome words of one candidate window, loaded one tile ahead.
+template <int NK>
+struct RawWindow {
+  uint32_t e;
+  uint32_t h[NK + 1], l[NK + 1], o[NK + 1];
+};
+
+// Queue entry `idx` (0xFFFFFFFF past the end), loaded two tiles ahead.
+__device__ __forceinline__ uint32_t load_entry(const uint32_t* __restrict__ queue, uint32_t idx, uint32_t n) {
+  return idx < n ? queue[idx] : 0xFFFFFFFFu;
+}
+
+// Staging of window words in shared memory: per thread, two candidates x
+// three planes x (NK + 1) words, slot-major ([slot][thread]).
+template <int NK>
+struct Stage {
+  static constexpr int kSlots = 3 * (NK + 1);            // per candidate
+  static constexpr uint32_t kStride = 32 * kMaxWarps;   // words per slot
+  static constexpr size_t kBytes = 2 * kSlots * kStride * 4;
+};
+
+// 4-byte asynchronous global -> shared copy; `bytes` 0 writes a zero without
+// reading the source.
+__device__ __forceinline__ void cp_async4(uint32_t dst, const uint32_t* src, uint32_t bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes));
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Starts the copy of entry `e`'s window words (planes hi, lo, ot; NK + 1 words
+// each) into the staging slots at shared address `dst` (slot stride
+// Stage<NK>::kStride words); a missing entry stages zeros.
+template <int NK>
+__device__ __forceinline__ void stage_planes(uint32_t dst, const uint32_t* __restrict__ hi,
+                                             const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
+                                             uint32_t e, uint64_t seg_pos0) {
+  const bool have = e != 0xFFFFFFFFu;
+  const uint64_t w = have ? (seg_pos0 + (e >> 1)) >> 5 : 0;
+  const uint32_t bytes = have ? 4u : 0u;
+  constexpr uint32_t kS = Stage<NK>::kStride * 4;
+#pragma unroll
+  for (int i = 0; i <= NK; ++i) {
+    cp_async4(dst + (0 * (NK + 1) + i) * kS, hi + w + i, bytes);
+    cp_async4(dst + (1 * (NK + 1) + i) * kS, lo + w + i, bytes);
+    cp_async4(dst + (2 * (NK + 1) + i) * kS, ot + w + i, bytes);
+  }
+}
+
+// Reads back a staged window (after cp_async_wait_all).
+template <int NK>
+__device__ __forceinline__ void unstage(RawWindow<NK>& r, const uint32_t* st, uint32_t e) {
+  constexpr uint32_t kS = Stage<NK>::kStride;
+  r.e = e;
+#pragma unroll
+  for (int i = 0; i <= NK; ++i) {
+    r.h[i] = st[(0 * (NK + 1) + i) * kS];
+    r.l[i] = st[(1 * (NK + 1) + i) * kS];
+    r.o[i] = st[(2 * (NK + 1) + i) * kS];
+  }
+}
+
+// The window of one candidate, strand-oriented: positions 0..L-1 in bits
+// 0..L-1 of (h, l, o) words; a '-' strand window is the reverse complement.
+template <int NK>
+__device__ __forceinline__ void orient(const RawWindow<NK>& raw, uint64_t seg_pos0, uint32_t L, uint32_t (&hw)[NK],
+                                       uint32_t (&lw)[NK], uint32_t (&ow)[NK]) {
+  const bool have = raw.e != 0xFFFFFFFFu;
+  const unsigned r = have ? (unsigned)((seg_pos0 + (raw.e >> 1)) & 31) : 0u;
+#pragma unroll
+  for (int i = 0; i < NK; ++i) {
+    hw[i] = __funnelshift_r(raw.h[i], raw.h[i + 1], r);
+    lw[i] = __funnelshift_r(raw.l[i], raw.l[i + 1], r);
+    ow[i] = __funnelshift_r(raw.o[i], raw.o[i + 1], r);
+  }
+  if (have && (raw.e & 1)) {
+    // Reverse complement: reverse the L positions, flip hi of bases.
+    if (NK == 1) {
+      const unsigned sh = 32 - L;
+      hw[0] = ~(__brev(hw[0]) >> sh) & (0xFFFFFFFFu >> sh);
+      lw[0] = __brev(lw[0]) >> sh;
+      ow[0] = __brev(ow[0]) >> sh;
+    } else {
+      const unsigned sh = 64 - L;
+      const uint64_t mask = ~0ull >> sh;
+      const uint64_t H = ~(__brevll(((uint64_t)hw[NK - 1] << 32) | hw[0]) >> sh) & mask;
+      const uint64_t Lo = __brevll(((uint64_t)lw[NK - 1] << 32) | lw[0]) >> sh;
+      const uint64_t O = __brevll(((uint64_t)ow[NK - 1] << 32) | ow[0]) >> sh;
+      hw[0] = (uint32_t)H;
+      hw[NK - 1] = (uint32_t)(H >> 32);
+      lw[0] = (uint32_t)Lo;
+      lw[NK - 1] = (uint32_t)(Lo >> 32);
+      ow[0] = (uint32_t)O;
+      ow[NK - 1] = (uint32_t)(O >> 32);
+    }
+  }
+}
+
+// Class rows of the shared table: 0 never mismatches (padding slots), 1-4 the
+// concrete bases, 5-14 the degenerate codes.
+template <bool CONC>
+struct TableRows {
+  static constexpr int kRows = CONC ? 5 : 15;
+};
+
+// Builds pair p of a tile from two groups of candidates (`ra` -> .x, `rb` ->
+// .y): oriented windows, transposed, expanded to class words in `pt` (the
+// pair's table, [row][ROW] uint2) and candidate entries in `ents` (64).
+template <int NK, int ROW, bool CONC>
+__device__ __forceinline__ void build_pair(const RawWindow<NK>& ra, const RawWindow<NK>& rb, uint64_t seg_pos0,
+                                           uint32_t L, unsigned lane, uint2* pt, uint32_t* ents) {
+  uint32_t ha[NK], la[NK], oa[NK], hb[NK], lb[NK], ob[NK];
+  orient<NK>(ra, seg_pos0, L, ha, la, oa);
+  orient<NK>(rb, seg_pos0, L, hb, lb, ob);
+  ents[lane] = ra.e;
+  ents[32 + lane] = rb.e;
+#pragma unroll
+  for (int i = 0; i < NK; ++i) {
+    const uint32_t h0 = warp_transpose(ha[i], lane), h1 = warp_transpose(hb[i], lane);
+    const uint32_t l0 = warp_transpose(la[i], lane), l1 = warp_transpose(lb[i], lane);
+    const uint32_t o0 = warp_transpose(oa[i], lane), o1 = warp_transpose(ob[i], lane);
+    const unsigned k = i * 32 + lane;
+    if (k < (unsigned)ROW) {
+      // One LOP3 of (h, l, o) each; truth tables over (0xF0, 0xCC, 0xAA).
+#define COF_ROW(r, LUT) pt[(r) * ROW + k] = make_uint2(lop3<LUT>(h0, l0, o0), lop3<LUT>(h1, l1, o1))
+      COF_ROW(1, 0xFE);  // T: h | l | o (mismatch unless T)
+      COF_ROW(2, 0xFB);  // C: h | ~l | o
+      COF_ROW(3, 0xEF);  // A: ~h | l | o
+      COF_ROW(4, 0xBF);  // G: ~h | ~l | o
+      if (!CONC) {
+        COF_ROW(5, 0x01);   // V: ~h & ~l & ~o (mismatch only T)
+        COF_ROW(6, 0x04);   // D: ~h & l & ~o (only C)
+        COF_ROW(7, 0x10);   // B: h & ~l & ~o (only A)
+        COF_ROW(8, 0x40);   // H: h & l & ~o (only G)
+        COF_ROW(9, 0x05);   // R: ~h & ~o (C or T)
+        COF_ROW(10, 0x50);  // Y: h & ~o (A or G)
+        COF_ROW(11, 0x14);  // K: (h ^ l) & ~o (A or C)
+        COF_ROW(12, 0x41);  // M: ~(h ^ l) & ~o (G or T)
+        COF_ROW(13, 0x44);  // W: l & ~o (C or G)
+        COF_ROW(14, 0x11);  // S: ~l & ~o (A or T)
+      }
+#undef COF_ROW
+    }
+  }
+}
+
+// 64-bit shared-memory load at a shared-window byte address plus a constant.
+template <uint32_t IMM>
+__device__ __forceinline__ void lds64(uint32_t addr, uint32_t& x, uint32_t& y) {
+  asm volatile("ld.shared.v2.u32 {%0, %1}, [%2+%3];" : "=r"(x), "=r"(y) : "r"(addr), "n"(IMM));
+}
+
+// The compare variant of a lane: the shared addresses of its slots' class
+// words in pair 0 of buffer 0, the carry masks of its threshold test and its
+// id; inactive lanes (past the last variant) get no hits.
+template <int S>
+__device__ __forceinline__ void load_variant(const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vthr,
+                                             const uint32_t* __restrict__ vgid, uint32_t nvar, uint32_t v,
+                                             uint32_t table_base, uint32_t (&addr)[S],
+                                             uint32_t (&kmask)[bit_width(S)], uint32_t& gid, uint32_t& lane_on) {
+  constexpr int NB = bit_width(S);
+  const bool active = v < nvar;
+#pragma unroll
+  for (int s = 0; s < S; s += 2) {
+    const uint32_t pk = active ? voff[(size_t)v * (S / 2) + s / 2] : 0u;
+    addr[s] = table_base + (pk & 0xFFFFu);
+    addr[s + 1] = table_base + (pk >> 16);
+  }
+  // count > thr  <=>  count + (2^NB - 1 - thr) carries out of NB bits.
+  const uint32_t thr = active ? min(vthr[v], (uint32_t)((1u << NB) - 1)) : 0u;
+  const uint32_t kadd = (1u << NB) - 1 - thr;
+#pragma unroll
+  for (int i = 0; i < NB; ++i) kmask[i] = 0u - ((kadd >> i) & 1u);
+  gid = active ? vgid[v] : 0u;
+  lane_on = active ? kFull : 0u;
+}
+
+// Appends the hits of one group (mask `hm`, count planes `bits`).  Entries
+// past the end of the queue (0xFFFFFFFF) are not candidates.
+template <int NB>
+__device__ __forceinline__ void emit_hits(uint32_t hm, const uint32_t (&bits)[NB], const uint32_t* ents,
+                                          uint32_t gid, uint64_t seg_pos0, uint64_t* __restrict__ hits,
+                                          unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+  while (hm) {
+    const unsigned c = __ffs(hm) - 1;
+    hm &= hm - 1;
+    const uint32_t e = ents[c];
+    if (e == 0xFFFFFFFFu) continue;
+    uint32_t mm = 0;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) mm |= ((bits[i] >> c) & 1u) << i;
+    const unsigned long long at = atomicAdd(hit_count, 1ull);
+    if (at < hit_cap) hits[at] = make_hit(gid, seg_pos0 + (e >> 1), e & 1, mm);
+  }
+}
+
+// Counts one lane's variant against pairs P.. W-1 of the current tile (`addr`
+// points into the current buffer; the pair index is a compile-time constant,
+// so every load address is [register + immediate]).
+template <int P, int S, int ROW, bool CONC>
+__device__ __forceinline__ void count_pairs(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
+                                            uint32_t lane_on, uint32_t gid, unsigned W, const uint32_t* ents,
+                                            uint64_t seg_pos0, uint64_t* __restrict__ hits,
+                                            unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+  if constexpr (P < kMaxWarps) {
+    if ((unsigned)P >= W) return;
+    constexpr int NB = bit_width(S);
+    constexpr uint32_t kPairBytes = TableRows<CONC>::kRows * ROW * 8;
+    constexpr uint32_t kImm = P * kPairBytes;
+    uint32_t xa[S], xb[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) lds64<kImm>(addr[s], xa[s], xb[s]);
+    uint32_t ba[NB], bb[NB];
+    CountTree<S, 0, NB>::run(xa, ba);
+    CountTree<S, 0, NB>::run(xb, bb);
+    uint32_t ca = 0, cb = 0;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      ca = maj3(ba[i], kmask[i], ca);
+      cb = maj3(bb[i], kmask[i], cb);
+    }
+    const uint32_t hita = ~ca & lane_on, hitb = ~cb & lane_on;
+    if (__any_sync(kFull, hita | hitb)) {
+      emit_hits<NB>(hita, ba, ents + P * 64, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NB>(hitb, bb, ents + P * 64 + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+    }
+    count_pairs<P + 1, S, ROW, CONC>(addr, kmask, lane_on, gid, W, ents, seg_pos0, hits, hit_count, hit_cap);
+  }
+}
+
+// Registers per thread: 72 lets four 224-thread CTAs share an SM (the usual
+// 7-warp case); wider slot lists get more.
+template <int S, int NK>
+struct MaxRegs {
+  static constexpr int value = (S <= 20 && NK == 1) ? 72 : (S <= 20 ? 80 : S <= 28 ? 96 : 104);
+};
+
+template <int S, int ROW, int NK, bool CONC>
+__global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::value)) comparer_bs_kernel(
+    const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
+    const uint32_t* __restrict__ queue, const uint32_t* __restrict__ qcount, uint64_t seg_pos0,
+    const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vthr, const uint32_t* __restrict__ vgid,
+    uint32_t nvar, uint32_t L, uint64_t* __restrict__ hits, unsigned long long* __restrict__ hit_count,
+    uint64_t hit_cap) {
+  constexpr int NB = bit_width(S);
+  constexpr int kPairWords = TableRows<CONC>::kRows * ROW;  // uint2 per pair
+  constexpr int kBufWords = kMaxWarps * kPairWords;
+  extern __shared__ uint2 smem2[];
+  uint2* tables = smem2;                                    // [2 buffers][kMaxWarps pairs][rows][ROW]
+  uint32_t* ents_all = (uint32_t*)(smem2 + 2 * kBufWords);  // [2 buffers][kMaxWarps pairs][64]
+  const uint32_t table_base = (uint32_t)__cvta_generic_to_shared(tables);
+  const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned W = blockDim.x >> 5;  // pairs per tile = warps
+  const unsigned tile_n = W * 64;
+
+  // Row 0 (pattern bytes that never mismatch: padding slots) stays zero.
+  for (unsigned i = threadIdx.x; i < 2 * kMaxWarps * ROW; i += blockDim.x)
+    tables[(i / ROW) * kPairWords + i % ROW] = make_uint2(0, 0);
+
+  const uint32_t n = *qcount;
+  const uint32_t ntiles = (n + tile_n - 1) / tile_n;
+  constexpr uint32_t kBufBytes = kBufWords * sizeof(uint2);
+  uint32_t t = blockIdx.x;
+  const uint32_t ca = warp * 64 + lane, cb = ca + 32;  // this lane's candidates within a tile
+  // Window words of the next tile are staged here by cp.async while the
+  // current tile is counted (per thread: candidate a's slots, then b's).
+  const uint32_t* stage = ents_all + 2 * kMaxWarps * 64 + threadIdx.x;
+  const uint32_t stage_a = (uint32_t)__cvta_generic_to_shared(stage);
+  const uint32_t stage_b = stage_a + Stage<NK>::kSlots * Stage<NK>::kStride * 4;
+  // With at most one variant per thread the lane's variant stays in registers
+  // for the whole kernel; its addresses follow the current buffer.
+  const bool one_chunk = nvar <= blockDim.x;
+  uint32_t addr[S], kmask[NB], gid = 0, lane_on = 0;
+  if (one_chunk) load_variant<S>(voff, vthr, vgid, nvar, warp * 32 + lane, table_base, addr, kmask, gid, lane_on);
+  // Entries: e* of the tile being staged, n* of the tile after it.
+  uint32_t ea = load_entry(queue, t * tile_n + ca, n), eb = load_entry(queue, t * tile_n + cb, n);
+  stage_planes<NK>(stage_a, hi, lo, ot, ea, seg_pos0);
+  stage_planes<NK>(stage_b, hi, lo, ot, eb, seg_pos0);
+  uint32_t na = load_entry(queue, (t + gridDim.x) * tile_n + ca, n);
+  uint32_t nb = load_entry(queue, (t + gridDim.x) * tile_n + cb, n);
+  cp_async_wait_all();
+  if (t < ntiles) {
+    RawWindow<NK> ra, rb;
+    unstage<NK>(ra, stage, ea);
+    unstage<NK>(rb, stage + Stage<NK>::kSlots * Stage<NK>::kStride, eb);
+    build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + warp * kPairWords, ents_all + warp * 64);
+  }
+  __syncthreads();
+  // One tile per step: count the tile in buffer `cur` while the next tile's
+  // words are in flight, then build the next tile into buffer cur ^ 1.
+  unsigned cur = 0;
+  while (t < ntiles) {
+    const uint32_t tn = t + gridDim.x;
+    ea = na;
+    eb = nb;
+    stage_planes<NK>(stage_a, hi, lo, ot, ea, seg_pos0);
+    stage_planes<NK>(stage_b, hi, lo, ot, eb, seg_pos0);
+    na = load_entry(queue, (tn + gridDim.x) * tile_n + ca, n);
+    nb = load_entry(queue, (tn + gridDim.x) * tile_n + cb, n);
+    const uint32_t* ents = ents_all + cur * (kMaxWarps * 64);
+    for (uint32_t vb = warp * 32; vb < nvar; vb += blockDim.x) {
+      if (!one_chunk)
+        load_variant<S>(voff, vthr, vgid, nvar, vb + lane, table_base + cur * kBufBytes, addr, kmask, gid, lane_on);
+      count_pairs<0, S, ROW, CONC>(addr, kmask, lane_on, gid, W, ents, seg_pos0, hits, hit_count, hit_cap);
+    }
+    cp_async_wait_all();
+    if (tn < ntiles) {
+      RawWindow<NK> ra, rb;
+      unstage<NK>(ra, stage, ea);
+      unstage<NK>(rb, stage + Stage<NK>::kSlots * Stage<NK>::kStride, eb);
+      build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + (cur ^ 1) * kBufWords + warp * kPairWords,
+                                ents_all + (cur ^ 1) * (kMaxWarps * 64) + warp * 64);
+    }
+    __syncthreads();
+    const uint32_t d = cur ? 0u - kBufBytes : kBufBytes;
+#pragma unroll
+    for (int s = 0; s < S; ++s) addr[s] += d;
+    cur ^= 1;
+    t = tn;
+  }
+}
+
+template <int ROW, int NK, bool CONC>
+constexpr size_t bs_smem_bytes() {
+  return 2 * ((size_t)kMaxWarps * TableRows<CONC>::kRows * ROW * sizeof(uint2) + kMaxWarps * 64 * 4) +
+         Stage<NK>::kBytes;
+}
+
+template <int S, int ROW, int NK, bool CONC>
+void launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
+               const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, uint32_t L,
+               uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
+  // Warps per block: enough lanes for every variant (so few lanes idle), at most 8.
+  const int warps = (int)std::min<uint32_t>(kMaxWarps, (nvar + 31) / 32);
+  const int threads = 32 * warps;
+  constexpr size_t smem = bs_smem_bytes<ROW, NK, CONC>();
+  cudaFuncSetAttribute(comparer_bs_kernel<S, ROW, NK, CONC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, comparer_bs_kernel<S, ROW, NK, CONC>, threads, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  comparer_bs_kernel<S, ROW, NK, CONC><<<sm_count * per_sm, threads, smem, stream>>>(
+      g.hi, g.lo, g.ot, queue, qcount, seg_pos0, voff, vthr, vgid, nvar, L, hits, hit_count, hit_cap);
+}
+
+}  // namespace
+
+template <int ROW, int NK, bool CONC>
+bool dispatch_s(int slots, const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
+                const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, uint32_t L,
+                uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
+#define COF_BS_CASE(SV)                                                                                          \
+  case SV:                                                                                                       \
+    launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, voff, vthr, vgid, nvar, L, hits, hit_count, hit_cap, \
+                                 sm_count, stream);                                                              \
+    return true;
+  switch (slots) {
+    COF_BS_CASE(8)
+    COF_BS_CASE(12)
+    COF_BS_CASE(16)
+    COF_BS_CASE(20)
+    COF_BS_CASE(24)
+    COF_BS_CASE(28)
+    COF_BS_CASE(32)
+    default:
+      return false;
+  }
+#undef COF_BS_CASE
+}
+
+}  // namespace bs
+}  // namespace cof
