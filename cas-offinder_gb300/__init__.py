@@ -40,7 +40,7 @@ EXPORTS = [
     "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
     "cof_server_start", "cof_server_submit", "cof_server_wait", "cof_server_release", "cof_server_stats",
     "cof_server_last_error", "cof_server_stop",
-    "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table",
+    "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table", "cofx_bs_programs",
 ]
 
 _lib = None
@@ -121,6 +121,7 @@ def lib():
             "cofx_pipe_rates": (c.c_int, [c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double),
                                           c.POINTER(c.c_double)]),
             "cofx_mismatch_table": (None, [vp]),
+            "cofx_bs_programs": (c.c_int, [c.c_char_p, sz, vp, vp, sz, vp, sz, vp, sz]),
             "cofx_synth_record": (u64, [u64, u32, u64, c.c_double, c.c_double, u32, c.c_double, u32, u32, vp]),
         }
         for name, (res, args) in sig.items():
@@ -146,6 +147,25 @@ def mismatch_table():
     out = np.zeros(65536, np.uint8)
     lib().cofx_mismatch_table(_ptr(out))
     return out.reshape(256, 256)
+
+
+def bs_programs(text):
+    """The bit-sliced comparer's lane programs for one input file (test hook):
+    dict with chunks, m, slots, row, prog / pgid (uint32 arrays) and the
+    variants as (key, threshold) in id order."""
+    import numpy as np
+    raw = text.encode() if isinstance(text, str) else bytes(text)
+    info = np.zeros(6, dtype=np.uint32)
+    st = lib().cofx_bs_programs(raw, len(raw), _ptr(info), None, 0, None, 0, None, 0)
+    if st != 0:
+        raise CofError(st, "input does not fit the bit-sliced comparer" if st == 2 else "parse error")
+    chunks, m, slots, row, nvar, kb = (int(x) for x in info)
+    prog = np.zeros(max(chunks, 1) * (1 + slots // 2 + m - 1) * 32, dtype=np.uint32)
+    pgid = np.zeros(max(chunks, 1) * m * 32, dtype=np.uint32)
+    keys = ctypes.create_string_buffer(kb + 1)
+    lib().cofx_bs_programs(raw, len(raw), _ptr(info), _ptr(prog), prog.size, _ptr(pgid), pgid.size, keys, kb + 1)
+    variants = [(ln.split("\t")[0], int(ln.split("\t")[1])) for ln in keys.raw[:kb].decode().splitlines()]
+    return {"chunks": chunks, "m": m, "slots": slots, "row": row, "prog": prog, "pgid": pgid, "variants": variants}
 
 
 def plane_words(n):

@@ -50,6 +50,7 @@ struct Variant {
   std::string id;        // id of the first guide that produced the key
   uint16_t threshold;    // its mismatch limit (the reference stores cl_ushort)
   std::vector<BulgeRecord> bulges;
+  uint32_t order = 0;    // rank of its first insertion among the file's variants
 };
 
 // One output row shape for (variant, bulge record, strand).  `head` is

@@ -8,8 +8,8 @@ namespace bs {
 // Launches the instance for `slots` (8..32); false when none fits.
 template <int ROW, int NK, bool CONC>
 bool dispatch_s(int slots, const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-                const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, uint32_t L,
-                uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
+                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L, uint64_t* hits,
+                unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
 }  // namespace bs
 using bs::dispatch_s;
 
@@ -42,11 +42,15 @@ uint32_t bs_class_of(unsigned char p) {
 }
 
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-                        const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, int slots,
+                        const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
                         uint32_t L, bool concrete_only, uint64_t* hits, unsigned long long* hit_count,
                         uint64_t hit_cap, int sm_count, cudaStream_t stream) {
-  if (nvar == 0) return true;
-#define COF_BS_ROW(ROWV, NKV)                                                                                        return concrete_only ? dispatch_s<ROWV, NKV, true>(slots, g, queue, qcount, seg_pos0, voff, vthr, vgid, nvar, L,                                                       hits, hit_count, hit_cap, sm_count, stream)                                         : dispatch_s<ROWV, NKV, false>(slots, g, queue, qcount, seg_pos0, voff, vthr, vgid, nvar, L,                                                        hits, hit_count, hit_cap, sm_count, stream);
+  if (chunks == 0) return true;
+#define COF_BS_ROW(ROWV, NKV)                                                                                       \
+  return concrete_only ? dispatch_s<ROWV, NKV, true>(slots, g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L,  \
+                                                      hits, hit_count, hit_cap, sm_count, stream)                   \
+                       : dispatch_s<ROWV, NKV, false>(slots, g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, \
+                                                       hits, hit_count, hit_cap, sm_count, stream);
   if (L <= 32) COF_BS_ROW(36, 1)
   if (L <= 36) COF_BS_ROW(36, 2)
   if (L <= 64) COF_BS_ROW(68, 2)

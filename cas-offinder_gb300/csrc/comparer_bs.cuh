@@ -126,12 +126,11 @@ __device__ __forceinline__ uint32_t load_entry(const uint32_t* __restrict__ queu
 }
 
 // Staging of window words in shared memory: per thread, two candidates x
-// three planes x (NK + 1) words, slot-major ([slot][thread]).
+// three planes x (NK + 1) words, slot-major ([slot][thread], slot stride =
+// threads per block).
 template <int NK>
 struct Stage {
-  static constexpr int kSlots = 3 * (NK + 1);            // per candidate
-  static constexpr uint32_t kStride = 32 * kMaxWarps;   // words per slot
-  static constexpr size_t kBytes = 2 * kSlots * kStride * 4;
+  static constexpr int kSlots = 3 * (NK + 1);  // per candidate
 };
 
 // 4-byte asynchronous global -> shared copy; `bytes` 0 writes a zero without
@@ -142,16 +141,15 @@ __device__ __forceinline__ void cp_async4(uint32_t dst, const uint32_t* src, uin
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Starts the copy of entry `e`'s window words (planes hi, lo, ot; NK + 1 words
-// each) into the staging slots at shared address `dst` (slot stride
-// Stage<NK>::kStride words); a missing entry stages zeros.
+// each) into the staging slots at shared address `dst` (slot stride kS
+// bytes); a missing entry stages zeros.
 template <int NK>
-__device__ __forceinline__ void stage_planes(uint32_t dst, const uint32_t* __restrict__ hi,
+__device__ __forceinline__ void stage_planes(uint32_t dst, uint32_t kS, const uint32_t* __restrict__ hi,
                                              const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
                                              uint32_t e, uint64_t seg_pos0) {
   const bool have = e != 0xFFFFFFFFu;
   const uint64_t w = have ? (seg_pos0 + (e >> 1)) >> 5 : 0;
   const uint32_t bytes = have ? 4u : 0u;
-  constexpr uint32_t kS = Stage<NK>::kStride * 4;
 #pragma unroll
   for (int i = 0; i <= NK; ++i) {
     cp_async4(dst + (0 * (NK + 1) + i) * kS, hi + w + i, bytes);
@@ -160,10 +158,9 @@ __device__ __forceinline__ void stage_planes(uint32_t dst, const uint32_t* __res
   }
 }
 
-// Reads back a staged window (after cp_async_wait_all).
+// Reads back a staged window (after cp_async_wait_all); slot stride kS words.
 template <int NK>
-__device__ __forceinline__ void unstage(RawWindow<NK>& r, const uint32_t* st, uint32_t e) {
-  constexpr uint32_t kS = Stage<NK>::kStride;
+__device__ __forceinline__ void unstage(RawWindow<NK>& r, const uint32_t* st, uint32_t kS, uint32_t e) {
   r.e = e;
 #pragma unroll
   for (int i = 0; i <= NK; ++i) {
@@ -263,139 +260,209 @@ __device__ __forceinline__ void lds64(uint32_t addr, uint32_t& x, uint32_t& y) {
   asm volatile("ld.shared.v2.u32 {%0, %1}, [%2+%3];" : "=r"(x), "=r"(y) : "r"(addr), "n"(IMM));
 }
 
-// The compare variant of a lane: the shared addresses of its slots' class
-// words in pair 0 of buffer 0, the carry masks of its threshold test and its
-// id; inactive lanes (past the last variant) get no hits.
+// A lane program's first variant (program layout in kernels.cuh): the shared
+// addresses of its slots' class words (pair 0 of the buffer at `tbase`), the
+// carry masks of its threshold bias and whether it is a real variant.
 template <int S>
-__device__ __forceinline__ void load_variant(const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vthr,
-                                             const uint32_t* __restrict__ vgid, uint32_t nvar, uint32_t v,
-                                             uint32_t table_base, uint32_t (&addr)[S],
-                                             uint32_t (&kmask)[bit_width(S)], uint32_t& gid, uint32_t& lane_on) {
+__device__ __forceinline__ void load_program(const uint32_t* __restrict__ pr, uint32_t tbase, uint32_t (&addr)[S],
+                                             uint32_t (&kmask)[bit_width(S)], uint32_t& kadd, uint32_t& first_on) {
   constexpr int NB = bit_width(S);
-  const bool active = v < nvar;
+  const uint32_t h = __ldg(pr);
 #pragma unroll
   for (int s = 0; s < S; s += 2) {
-    const uint32_t pk = active ? voff[(size_t)v * (S / 2) + s / 2] : 0u;
-    addr[s] = table_base + (pk & 0xFFFFu);
-    addr[s + 1] = table_base + (pk >> 16);
+    const uint32_t pk = __ldg(pr + (1 + s / 2) * 32);
+    addr[s] = tbase + (pk & 0xFFFFu);
+    addr[s + 1] = tbase + (pk >> 16);
   }
-  // count > thr  <=>  count + (2^NB - 1 - thr) carries out of NB bits.
-  const uint32_t thr = active ? min(vthr[v], (uint32_t)((1u << NB) - 1)) : 0u;
-  const uint32_t kadd = (1u << NB) - 1 - thr;
+  kadd = h & 0xFFu;
 #pragma unroll
   for (int i = 0; i < NB; ++i) kmask[i] = 0u - ((kadd >> i) & 1u);
-  gid = active ? vgid[v] : 0u;
-  lane_on = active ? kFull : 0u;
+  first_on = (h & 0x100u) ? kFull : 0u;
 }
 
-// Appends the hits of one group (mask `hm`, count planes `bits`).  Entries
-// past the end of the queue (0xFFFFFFFF) are not candidates.
-template <int NB>
-__device__ __forceinline__ void emit_hits(uint32_t hm, const uint32_t (&bits)[NB], const uint32_t* ents,
-                                          uint32_t gid, uint64_t seg_pos0, uint64_t* __restrict__ hits,
-                                          unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+// Appends the hits of one group: mask `hm`, count planes `bits` holding
+// count + `bias`.  Entries past the end of the queue (0xFFFFFFFF) are not
+// candidates.
+template <int NP>
+__device__ __forceinline__ void emit_hits(uint32_t hm, const uint32_t (&bits)[NP], uint32_t bias,
+                                          const uint32_t* ents, uint32_t gid, uint64_t seg_pos0,
+                                          uint64_t* __restrict__ hits, unsigned long long* __restrict__ hit_count,
+                                          uint64_t hit_cap) {
   while (hm) {
     const unsigned c = __ffs(hm) - 1;
     hm &= hm - 1;
     const uint32_t e = ents[c];
     if (e == 0xFFFFFFFFu) continue;
-    uint32_t mm = 0;
+    uint32_t v = 0;
 #pragma unroll
-    for (int i = 0; i < NB; ++i) mm |= ((bits[i] >> c) & 1u) << i;
+    for (int i = 0; i < NP; ++i) v |= ((bits[i] >> c) & 1u) << i;
     const unsigned long long at = atomicAdd(hit_count, 1ull);
-    if (at < hit_cap) hits[at] = make_hit(gid, seg_pos0 + (e >> 1), e & 1, mm);
+    if (at < hit_cap) hits[at] = make_hit(gid, seg_pos0 + (e >> 1), e & 1, v - bias);
   }
 }
 
-// Counts one lane's variant against pairs P.. W-1 of the current tile (`addr`
-// points into the current buffer; the pair index is a compile-time constant,
-// so every load address is [register + immediate]).
+// Count planes + a per-lane constant (bit i of it as the all-ones / all-zeros
+// word kmask[i]): NB + 1 planes out.
+template <int NB>
+__device__ __forceinline__ void add_bias(const uint32_t (&b)[NB], const uint32_t (&kmask)[NB], uint32_t (&p)[NB + 1]) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    p[i] = xor3(b[i], kmask[i], c);
+    c = maj3(b[i], kmask[i], c);
+  }
+  p[NB] = c;
+}
+
+// One update step of bit-sliced counters: + a - b (one bit each per
+// candidate).  Where exactly one of a, b is set the counter moves by one:
+// up (carry = p & t) when a is set, down (borrow = ~p & t) otherwise.
+template <int NP>
+__device__ __forceinline__ void step_update(uint32_t (&p)[NP], uint32_t a, uint32_t b) {
+  uint32_t t = a ^ b;
+#pragma unroll
+  for (int i = 0; i < NP; ++i) {
+    const uint32_t pi = p[i];
+    p[i] = pi ^ t;
+    if (i + 1 < NP) t = lop3<0x90>(t, pi, a);  // t & ~(pi ^ a)
+  }
+}
+
+// Runs one lane program on pairs P.. W-1 of the current tile (`addr` points
+// at pair 0 of the current buffer, `tbase` is that buffer's base; the pair
+// index is a compile-time constant, so every load is [register + immediate]).
 template <int P, int S, int ROW, bool CONC>
-__device__ __forceinline__ void count_pairs(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
-                                            uint32_t lane_on, uint32_t gid, unsigned W, const uint32_t* ents,
-                                            uint64_t seg_pos0, uint64_t* __restrict__ hits,
+__device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
+                                            uint32_t kadd, uint32_t first_on, const uint32_t* __restrict__ steps,
+                                            const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase, unsigned W,
+                                            const uint32_t* ents, uint64_t seg_pos0, uint64_t* __restrict__ hits,
                                             unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
   if constexpr (P < kMaxWarps) {
     if ((unsigned)P >= W) return;
     constexpr int NB = bit_width(S);
-    constexpr uint32_t kPairBytes = TableRows<CONC>::kRows * ROW * 8;
-    constexpr uint32_t kImm = P * kPairBytes;
+    constexpr uint32_t kImm = P * TableRows<CONC>::kRows * ROW * 8;
     uint32_t xa[S], xb[S];
 #pragma unroll
     for (int s = 0; s < S; ++s) lds64<kImm>(addr[s], xa[s], xb[s]);
     uint32_t ba[NB], bb[NB];
     CountTree<S, 0, NB>::run(xa, ba);
     CountTree<S, 0, NB>::run(xb, bb);
-    uint32_t ca = 0, cb = 0;
+    const uint32_t* pe = ents + P * 64;
+    if (m == 1) {
+      // One variant per lane: only the carry out of count + bias matters.
+      uint32_t ca = 0, cb = 0;
 #pragma unroll
-    for (int i = 0; i < NB; ++i) {
-      ca = maj3(ba[i], kmask[i], ca);
-      cb = maj3(bb[i], kmask[i], cb);
+      for (int i = 0; i < NB; ++i) {
+        ca = maj3(ba[i], kmask[i], ca);
+        cb = maj3(bb[i], kmask[i], cb);
+      }
+      const uint32_t hita = ~ca & first_on, hitb = ~cb & first_on;
+      if (__any_sync(kFull, hita | hitb)) {
+        const uint32_t gid = __ldg(gids);
+        emit_hits<NB>(hita, ba, 0u, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+        emit_hits<NB>(hitb, bb, 0u, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+      }
+    } else {
+      // Biased counters (count + bias in NB + 1 planes): a variant passes
+      // while the top plane is clear.
+      uint32_t pa[NB + 1], pb[NB + 1];
+      add_bias<NB>(ba, kmask, pa);
+      add_bias<NB>(bb, kmask, pb);
+      uint32_t hita = ~pa[NB] & first_on, hitb = ~pb[NB] & first_on;
+      if (__any_sync(kFull, hita | hitb)) {
+        const uint32_t gid = __ldg(gids);
+        emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+        emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+      }
+      uint32_t e = 32;  // gid index of the lane's next tested variant, x 32
+      for (uint32_t i = 0; i + 1 < m; ++i) {
+        const uint32_t w = __ldg(steps + i * 32);
+        uint32_t a0, a1, b0, b1;
+        lds64<kImm>(tbase + (w & 0x7FFFu), a0, a1);
+        lds64<kImm>(tbase + (w >> 16), b0, b1);
+        step_update<NB + 1>(pa, a0, b0);
+        step_update<NB + 1>(pb, a1, b1);
+        const uint32_t on = (w & 0x8000u) ? kFull : 0u;
+        hita = ~pa[NB] & on;
+        hitb = ~pb[NB] & on;
+        if (__any_sync(kFull, hita | hitb)) {
+          const uint32_t gid = (hita | hitb) ? __ldg(gids + e) : 0u;
+          emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+          emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+        }
+        e += on & 32u;
+      }
     }
-    const uint32_t hita = ~ca & lane_on, hitb = ~cb & lane_on;
-    if (__any_sync(kFull, hita | hitb)) {
-      emit_hits<NB>(hita, ba, ents + P * 64, gid, seg_pos0, hits, hit_count, hit_cap);
-      emit_hits<NB>(hitb, bb, ents + P * 64 + 32, gid, seg_pos0, hits, hit_count, hit_cap);
-    }
-    count_pairs<P + 1, S, ROW, CONC>(addr, kmask, lane_on, gid, W, ents, seg_pos0, hits, hit_count, hit_cap);
+    run_program<P + 1, S, ROW, CONC>(addr, kmask, kadd, first_on, steps, gids, m, tbase, W, ents, seg_pos0, hits,
+                                     hit_count, hit_cap);
   }
 }
 
-// Registers per thread: 72 lets four 224-thread CTAs share an SM (the usual
-// 7-warp case); wider slot lists get more.
+// Registers per thread: 72 lets four 224-thread (or seven 128-thread) CTAs
+// share an SM; wider slot lists get more.
 template <int S, int NK>
 struct MaxRegs {
-  static constexpr int value = (S <= 20 && NK == 1) ? 72 : (S <= 20 ? 80 : S <= 28 ? 96 : 104);
+  static constexpr int value = (S > 16 && S <= 20 && NK == 1) ? 72 : (S <= 20 ? 80 : S <= 28 ? 96 : 104);
 };
+
+// Shared memory of a CTA of W warps: two table buffers of W pairs, their
+// candidate entries, and the staging slots.
+template <int ROW, int NK, bool CONC>
+__host__ __device__ constexpr size_t bs_smem_bytes(unsigned W) {
+  return 2 * ((size_t)W * TableRows<CONC>::kRows * ROW * sizeof(uint2) + W * 64 * 4) +
+         2 * Stage<NK>::kSlots * (32 * W) * 4;
+}
 
 template <int S, int ROW, int NK, bool CONC>
 __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::value)) comparer_bs_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
     const uint32_t* __restrict__ queue, const uint32_t* __restrict__ qcount, uint64_t seg_pos0,
-    const uint32_t* __restrict__ voff, const uint32_t* __restrict__ vthr, const uint32_t* __restrict__ vgid,
-    uint32_t nvar, uint32_t L, uint64_t* __restrict__ hits, unsigned long long* __restrict__ hit_count,
-    uint64_t hit_cap) {
+    const uint32_t* __restrict__ prog, const uint32_t* __restrict__ pgid, uint32_t chunks, uint32_t m, uint32_t L,
+    uint64_t* __restrict__ hits, unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
   constexpr int NB = bit_width(S);
   constexpr int kPairWords = TableRows<CONC>::kRows * ROW;  // uint2 per pair
-  constexpr int kBufWords = kMaxWarps * kPairWords;
-  extern __shared__ uint2 smem2[];
-  uint2* tables = smem2;                                    // [2 buffers][kMaxWarps pairs][rows][ROW]
-  uint32_t* ents_all = (uint32_t*)(smem2 + 2 * kBufWords);  // [2 buffers][kMaxWarps pairs][64]
-  const uint32_t table_base = (uint32_t)__cvta_generic_to_shared(tables);
   const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned W = blockDim.x >> 5;  // pairs per tile = warps
   const unsigned tile_n = W * 64;
+  const uint32_t kBufWords = W * kPairWords;
+  const uint32_t kBufBytes = kBufWords * (uint32_t)sizeof(uint2);
+  extern __shared__ uint2 smem2[];
+  uint2* tables = smem2;                                    // [2 buffers][W pairs][rows][ROW]
+  uint32_t* ents_all = (uint32_t*)(smem2 + 2 * kBufWords);  // [2 buffers][W pairs][64]
+  const uint32_t table_base = (uint32_t)__cvta_generic_to_shared(tables);
+  // Window words of the next tile are staged here by cp.async while the
+  // current tile is counted (per thread: candidate a's slots, then b's).
+  const uint32_t kS = blockDim.x;  // staging slot stride, words
+  const uint32_t* stage = ents_all + 2 * W * 64 + threadIdx.x;
+  const uint32_t stage_a = (uint32_t)__cvta_generic_to_shared(stage);
+  const uint32_t stage_b = stage_a + Stage<NK>::kSlots * kS * 4;
+  const uint32_t words = 1 + S / 2 + (m - 1);  // per lane program
 
   // Row 0 (pattern bytes that never mismatch: padding slots) stays zero.
-  for (unsigned i = threadIdx.x; i < 2 * kMaxWarps * ROW; i += blockDim.x)
+  for (unsigned i = threadIdx.x; i < 2 * W * ROW; i += blockDim.x)
     tables[(i / ROW) * kPairWords + i % ROW] = make_uint2(0, 0);
 
   const uint32_t n = *qcount;
   const uint32_t ntiles = (n + tile_n - 1) / tile_n;
-  constexpr uint32_t kBufBytes = kBufWords * sizeof(uint2);
   uint32_t t = blockIdx.x;
   const uint32_t ca = warp * 64 + lane, cb = ca + 32;  // this lane's candidates within a tile
-  // Window words of the next tile are staged here by cp.async while the
-  // current tile is counted (per thread: candidate a's slots, then b's).
-  const uint32_t* stage = ents_all + 2 * kMaxWarps * 64 + threadIdx.x;
-  const uint32_t stage_a = (uint32_t)__cvta_generic_to_shared(stage);
-  const uint32_t stage_b = stage_a + Stage<NK>::kSlots * Stage<NK>::kStride * 4;
-  // With at most one variant per thread the lane's variant stays in registers
-  // for the whole kernel; its addresses follow the current buffer.
-  const bool one_chunk = nvar <= blockDim.x;
-  uint32_t addr[S], kmask[NB], gid = 0, lane_on = 0;
-  if (one_chunk) load_variant<S>(voff, vthr, vgid, nvar, warp * 32 + lane, table_base, addr, kmask, gid, lane_on);
+  // With one chunk per warp the lane's program stays in registers for the
+  // whole kernel; its addresses follow the current buffer.
+  const bool resident = chunks <= W;
+  uint32_t addr[S], kmask[NB], kadd = 0, first_on = 0;
+  if (resident && warp < chunks)
+    load_program<S>(prog + (size_t)warp * words * 32 + lane, table_base, addr, kmask, kadd, first_on);
   // Entries: e* of the tile being staged, n* of the tile after it.
   uint32_t ea = load_entry(queue, t * tile_n + ca, n), eb = load_entry(queue, t * tile_n + cb, n);
-  stage_planes<NK>(stage_a, hi, lo, ot, ea, seg_pos0);
-  stage_planes<NK>(stage_b, hi, lo, ot, eb, seg_pos0);
+  stage_planes<NK>(stage_a, kS * 4, hi, lo, ot, ea, seg_pos0);
+  stage_planes<NK>(stage_b, kS * 4, hi, lo, ot, eb, seg_pos0);
   uint32_t na = load_entry(queue, (t + gridDim.x) * tile_n + ca, n);
   uint32_t nb = load_entry(queue, (t + gridDim.x) * tile_n + cb, n);
   cp_async_wait_all();
   if (t < ntiles) {
     RawWindow<NK> ra, rb;
-    unstage<NK>(ra, stage, ea);
-    unstage<NK>(rb, stage + Stage<NK>::kSlots * Stage<NK>::kStride, eb);
+    unstage<NK>(ra, stage, kS, ea);
+    unstage<NK>(rb, stage + Stage<NK>::kSlots * kS, kS, eb);
     build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + warp * kPairWords, ents_all + warp * 64);
   }
   __syncthreads();
@@ -406,67 +473,80 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     const uint32_t tn = t + gridDim.x;
     ea = na;
     eb = nb;
-    stage_planes<NK>(stage_a, hi, lo, ot, ea, seg_pos0);
-    stage_planes<NK>(stage_b, hi, lo, ot, eb, seg_pos0);
+    stage_planes<NK>(stage_a, kS * 4, hi, lo, ot, ea, seg_pos0);
+    stage_planes<NK>(stage_b, kS * 4, hi, lo, ot, eb, seg_pos0);
     na = load_entry(queue, (tn + gridDim.x) * tile_n + ca, n);
     nb = load_entry(queue, (tn + gridDim.x) * tile_n + cb, n);
-    const uint32_t* ents = ents_all + cur * (kMaxWarps * 64);
-    for (uint32_t vb = warp * 32; vb < nvar; vb += blockDim.x) {
-      if (!one_chunk)
-        load_variant<S>(voff, vthr, vgid, nvar, vb + lane, table_base + cur * kBufBytes, addr, kmask, gid, lane_on);
-      count_pairs<0, S, ROW, CONC>(addr, kmask, lane_on, gid, W, ents, seg_pos0, hits, hit_count, hit_cap);
+    const uint32_t* ents = ents_all + cur * (W * 64);
+    const uint32_t tbase = table_base + cur * kBufBytes;
+    for (uint32_t c = warp; c < chunks; c += W) {
+      const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
+      if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
+      run_program<0, S, ROW, CONC>(addr, kmask, kadd, first_on, pr + (1 + S / 2) * 32, pgid + (size_t)c * m * 32 + lane,
+                                   m, tbase, W, ents, seg_pos0, hits, hit_count, hit_cap);
     }
     cp_async_wait_all();
     if (tn < ntiles) {
       RawWindow<NK> ra, rb;
-      unstage<NK>(ra, stage, ea);
-      unstage<NK>(rb, stage + Stage<NK>::kSlots * Stage<NK>::kStride, eb);
+      unstage<NK>(ra, stage, kS, ea);
+      unstage<NK>(rb, stage + Stage<NK>::kSlots * kS, kS, eb);
       build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + (cur ^ 1) * kBufWords + warp * kPairWords,
-                                ents_all + (cur ^ 1) * (kMaxWarps * 64) + warp * 64);
+                                ents_all + (cur ^ 1) * (W * 64) + warp * 64);
     }
     __syncthreads();
-    const uint32_t d = cur ? 0u - kBufBytes : kBufBytes;
+    if (resident) {
+      const uint32_t d = cur ? 0u - kBufBytes : kBufBytes;
 #pragma unroll
-    for (int s = 0; s < S; ++s) addr[s] += d;
+      for (int s = 0; s < S; ++s) addr[s] += d;
+    }
     cur ^= 1;
     t = tn;
   }
 }
 
-template <int ROW, int NK, bool CONC>
-constexpr size_t bs_smem_bytes() {
-  return 2 * ((size_t)kMaxWarps * TableRows<CONC>::kRows * ROW * sizeof(uint2) + kMaxWarps * 64 * 4) +
-         Stage<NK>::kBytes;
+// Warps per CTA (= pairs of candidate groups per tile): one per chunk up to
+// eight; above that the count in [4, 8] that splits the chunks most evenly.
+inline unsigned bs_warps(uint32_t chunks) {
+  if (chunks <= (uint32_t)kMaxWarps) return chunks ? chunks : 1;
+  unsigned best = kMaxWarps, waste = ~0u;
+  for (unsigned w = kMaxWarps; w >= 4; --w) {
+    const unsigned x = (unsigned)(((chunks + w - 1) / w) * w - chunks);
+    if (x < waste) {
+      waste = x;
+      best = w;
+    }
+  }
+  return best;
 }
 
 template <int S, int ROW, int NK, bool CONC>
 void launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-               const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, uint32_t L,
-               uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
-  // Warps per block: enough lanes for every variant (so few lanes idle), at most 8.
-  const int warps = (int)std::min<uint32_t>(kMaxWarps, (nvar + 31) / 32);
-  const int threads = 32 * warps;
-  constexpr size_t smem = bs_smem_bytes<ROW, NK, CONC>();
-  cudaFuncSetAttribute(comparer_bs_kernel<S, ROW, NK, CONC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+               const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L, uint64_t* hits,
+               unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
+  const unsigned warps = bs_warps(chunks);
+  const int threads = 32 * (int)warps;
+  const size_t smem = bs_smem_bytes<ROW, NK, CONC>(warps);
+  cudaFuncSetAttribute(comparer_bs_kernel<S, ROW, NK, CONC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)bs_smem_bytes<ROW, NK, CONC>(kMaxWarps));
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, comparer_bs_kernel<S, ROW, NK, CONC>, threads, smem) !=
           cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
   comparer_bs_kernel<S, ROW, NK, CONC><<<sm_count * per_sm, threads, smem, stream>>>(
-      g.hi, g.lo, g.ot, queue, qcount, seg_pos0, voff, vthr, vgid, nvar, L, hits, hit_count, hit_cap);
+      g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, hits, hit_count, hit_cap);
 }
 
 }  // namespace
 
 template <int ROW, int NK, bool CONC>
 bool dispatch_s(int slots, const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-                const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, uint32_t L,
-                uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
-#define COF_BS_CASE(SV)                                                                                          \
-  case SV:                                                                                                       \
-    launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, voff, vthr, vgid, nvar, L, hits, hit_count, hit_cap, \
-                                 sm_count, stream);                                                              \
+                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L, uint64_t* hits,
+                unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
+#define COF_BS_CASE(SV)                                                                                            \
+  case SV:                                                                                                         \
+    launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, hits, hit_count, hit_cap, \
+                                 sm_count, stream);                                                                \
     return true;
   switch (slots) {
     COF_BS_CASE(8)

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <string>
@@ -153,6 +154,120 @@ void init_group(PatternGroup& g, const std::string& pattern) {
   make_finder_pattern(pattern, revcomp(pattern), g.fpat);
 }
 
+// Lane programs of the bit-sliced comparer (layout in kernels.cuh).
+//
+// Variants are taken in generation order -- job by job, then by first
+// insertion, the order in which the reference's parseInput produces them
+// (cas-offinder.cpp:647-682) -- where consecutive DNA-bulge variants of one
+// guide differ by one guide base moved across the gap and consecutive
+// RNA-bulge variants by one base.  Each such difference is one class word
+// added and one removed, so after a first variant counted in full the kernel
+// updates the count instead of recounting.  A chain breaks where the next
+// variant differs by more than two words each way or has another threshold;
+// every step is the exact set difference of the two variants' slots, so the
+// counts do not depend on how the chains are cut.  The steps per lane program
+// (m - 1) are chosen to minimise the work of the resulting 32-lane chunks.
+void build_bs_programs(const std::vector<const Variant*>& vars, const std::vector<uint32_t>& gids, int S,
+                       uint32_t row, std::vector<uint32_t>& prog, std::vector<uint32_t>& pgid, uint32_t& chunks,
+                       uint32_t& m_out) {
+  const size_t V = vars.size();
+  const int NB = [&] { int b = 1; while ((1 << b) <= S) ++b; return b; }();  // bit_width(S)
+  std::vector<std::vector<uint16_t>> slots(V);
+  std::vector<uint32_t> kadd(V);
+  for (size_t i = 0; i < V; ++i) {
+    const std::string& key = vars[i]->key;
+    for (size_t k = 0; k < key.size(); ++k) {
+      const uint32_t c = bs_class_of((unsigned char)key[k]);
+      if (c) slots[i].push_back((uint16_t)((c * row + (uint32_t)k) * 8));
+    }
+    std::sort(slots[i].begin(), slots[i].end());
+    kadd[i] = (1u << NB) - 1 - std::min<uint32_t>(vars[i]->threshold, (1u << NB) - 1);
+  }
+  // Generation order: jobs are contiguous runs of one variant array.
+  std::vector<uint64_t> rank(V);
+  uint64_t job = 0;
+  for (size_t i = 0; i < V; ++i) {
+    if (i && vars[i] != vars[i - 1] + 1) ++job;
+    rank[i] = (job << 32) | vars[i]->order;
+  }
+  std::vector<uint32_t> ord(V);
+  for (size_t i = 0; i < V; ++i) ord[i] = (uint32_t)i;
+  std::sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return rank[a] < rank[b]; });
+  // Steps from variant u to v: (added, removed) offset pairs, 0 = none.
+  auto diff = [&](uint32_t u, uint32_t v, std::vector<std::pair<uint16_t, uint16_t>>& st) {
+    std::vector<uint16_t> add, rem;
+    std::set_difference(slots[v].begin(), slots[v].end(), slots[u].begin(), slots[u].end(), std::back_inserter(add));
+    std::set_difference(slots[u].begin(), slots[u].end(), slots[v].begin(), slots[v].end(), std::back_inserter(rem));
+    st.clear();
+    const size_t k = std::max<size_t>(1, std::max(add.size(), rem.size()));
+    for (size_t j = 0; j < k; ++j)
+      st.emplace_back(j < add.size() ? add[j] : 0, j < rem.size() ? rem[j] : 0);
+  };
+  // Chains: cost of each link in steps (0 = chain break before this variant).
+  std::vector<uint32_t> link(V, 0);
+  std::vector<std::pair<uint16_t, uint16_t>> st;
+  for (size_t x = 1; x < V; ++x) {
+    const uint32_t u = ord[x - 1], v = ord[x];
+    if (kadd[u] != kadd[v]) continue;
+    diff(u, v, st);
+    if (st.size() <= 2) link[x] = (uint32_t)st.size();
+  }
+  // Pieces for a step budget of m - 1: greedy along the chains.
+  auto cut = [&](uint32_t m, std::vector<std::pair<size_t, size_t>>* pieces) {
+    size_t n = 0, begin = 0;
+    uint32_t used = 0;
+    for (size_t x = 0; x <= V; ++x) {
+      const bool extend = x < V && x > begin && link[x] && used + link[x] <= m - 1;
+      if (x > 0 && !extend) {
+        if (pieces) pieces->emplace_back(begin, x);
+        ++n;
+        begin = x;
+        used = 0;
+      } else if (extend) {
+        used += link[x];
+      }
+    }
+    return n;
+  };
+  // Work per chunk and pair of candidate groups, in issued instructions: a
+  // full count ~(4.6 S + 26), a step ~37.
+  uint32_t best_m = 1;
+  double best = 1e300;
+  for (uint32_t m = 1; m <= 24; ++m) {
+    const size_t pieces = cut(m, nullptr);
+    const double cost = (double)((pieces + 31) / 32) * (4.6 * S + 26 + 37.0 * (m - 1));
+    if (cost < best * 0.999) {
+      best = cost;
+      best_m = m;
+    }
+  }
+  std::vector<std::pair<size_t, size_t>> pieces;
+  cut(best_m, &pieces);
+  const uint32_t m = best_m;
+  chunks = (uint32_t)((pieces.size() + 31) / 32);
+  m_out = m;
+  const size_t words = 1 + S / 2 + (m - 1);
+  prog.assign(std::max<size_t>(chunks, 1) * words * 32, 0);
+  pgid.assign(std::max<size_t>(chunks, 1) * m * 32, 0xFFFFFFFFu);
+  for (size_t pi = 0; pi < pieces.size(); ++pi) {
+    const size_t c = pi / 32, l = pi % 32;
+    auto W = [&](size_t w) -> uint32_t& { return prog[(c * words + w) * 32 + l]; };
+    const uint32_t first = ord[pieces[pi].first];
+    W(0) = kadd[first] | (1u << 8);
+    for (size_t sl = 0; sl < slots[first].size(); ++sl) W(1 + sl / 2) |= (uint32_t)slots[first][sl] << (16 * (sl & 1));
+    pgid[(c * m + 0) * 32 + l] = gids[first];
+    size_t step = 0;
+    uint32_t e = 1;
+    for (size_t x = pieces[pi].first + 1; x < pieces[pi].second; ++x) {
+      diff(ord[x - 1], ord[x], st);
+      for (size_t j = 0; j < st.size(); ++j, ++step)
+        W(1 + S / 2 + step) = st[j].first | (j + 1 == st.size() ? 0x8000u : 0u) | ((uint32_t)st[j].second << 16);
+      pgid[(c * m + e) * 32 + l] = gids[ord[x]];
+      ++e;
+    }
+  }
+}
+
 cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars) {
   const size_t V = vars.size();
   const size_t msz = g.nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>);
@@ -176,34 +291,13 @@ cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<
   COF_CUDA(h, g.vmask.ensure(masks.size()));
   COF_CUDA(h, cudaMemcpyAsync(g.vmask.p, masks.data(), masks.size(), cudaMemcpyHostToDevice, h->stream));
   g.bs_slots = h->force_popc ? 0 : bs_slots_for(maxpos);
-  std::vector<uint32_t> off, thr, gid;
+  std::vector<uint32_t> prog, pgid;
   if (g.bs_slots) {
-    // Per variant, the positions that can mismatch as byte offsets of their
-    // class word in the comparer's shared-memory table.
-    const int S = g.bs_slots;
-    const uint32_t row = (uint32_t)bs_row_for(g.L);
-    off.assign(std::max<size_t>(V, 1) * (S / 2), 0);
-    thr.assign(std::max<size_t>(V, 1), 0);
-    gid.assign(std::max<size_t>(V, 1), 0);
-    for (size_t i = 0; i < V; ++i) {
-      const Variant& var = *vars[i];
-      int sl = 0;
-      for (size_t k = 0; k < var.key.size(); ++k) {
-        const uint32_t c = bs_class_of((unsigned char)var.key[k]);
-        if (!c) continue;
-        const uint32_t byte_off = (c * row + (uint32_t)k) * 8;  // uint2 table element (two groups)
-        off[i * (S / 2) + sl / 2] |= byte_off << (16 * (sl & 1));
-        ++sl;
-      }
-      thr[i] = var.threshold;
-      gid[i] = g.gids[i];
-    }
-    COF_CUDA(h, g.bs_off.ensure(off.size() * 4));
-    COF_CUDA(h, g.bs_thr.ensure(thr.size() * 4));
-    COF_CUDA(h, g.bs_gid.ensure(gid.size() * 4));
-    COF_CUDA(h, cudaMemcpyAsync(g.bs_off.p, off.data(), off.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    COF_CUDA(h, cudaMemcpyAsync(g.bs_thr.p, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    COF_CUDA(h, cudaMemcpyAsync(g.bs_gid.p, gid.data(), gid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    build_bs_programs(vars, g.gids, g.bs_slots, (uint32_t)bs_row_for(g.L), prog, pgid, g.bs_chunks, g.bs_m);
+    COF_CUDA(h, g.bs_prog.ensure(prog.size() * 4));
+    COF_CUDA(h, g.bs_pgid.ensure(pgid.size() * 4));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_prog.p, prog.data(), prog.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_pgid.p, pgid.data(), pgid.size() * 4, cudaMemcpyHostToDevice, h->stream));
   }
   // The host vectors die on return: wait for the copies.
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
@@ -390,8 +484,8 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       if ((st = record_start(h, evs, "comparer", (double)(s * G + gi), h->stream))) return st;
       const uint32_t V = (uint32_t)g.gids.size();
       if (!g.bs_slots ||
-          !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_off.as<uint32_t>(), g.bs_thr.as<uint32_t>(),
-                              g.bs_gid.as<uint32_t>(), V, g.bs_slots, g.L, g.concrete_only, h->hits.as<uint64_t>(),
+          !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_prog.as<uint32_t>(), g.bs_pgid.as<uint32_t>(),
+                              g.bs_chunks, g.bs_m, g.bs_slots, g.L, g.concrete_only, h->hits.as<uint64_t>(),
                               h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream))
         launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, h->hits.as<uint64_t>(),
                         h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream);
@@ -903,6 +997,41 @@ cof_status cof_comparer_chunk(cof_handle* h, const char* chr, uint64_t chrlen, c
 }
 
 uint64_t cof_plane_words(uint64_t n) { return plane_words(n); }
+
+int cofx_bs_programs(const char* input, size_t len, uint32_t* info, uint32_t* prog, size_t prog_cap, uint32_t* pgid,
+                     size_t pgid_cap, char* keys, size_t keys_cap) {
+  Job job;
+  std::string err;
+  if (!input || !info || !parse_job(input, len, job, err)) return 1;
+  std::vector<const Variant*> vars;
+  std::vector<uint32_t> gids;
+  int maxpos = 0;
+  for (size_t v = 0; v < job.variants.size(); ++v) {
+    vars.push_back(&job.variants[v]);
+    gids.push_back((uint32_t)v);
+    int c = 0;
+    for (char ch : job.variants[v].key) c += bs_class_of((unsigned char)ch) != 0;
+    maxpos = std::max(maxpos, c);
+  }
+  const int S = bs_slots_for(maxpos);
+  if (!S || vars.empty()) return 2;
+  const uint32_t row = (uint32_t)bs_row_for((uint32_t)job.pattern.size());
+  std::vector<uint32_t> pv, gv;
+  uint32_t chunks = 0, m = 1;
+  build_bs_programs(vars, gids, S, row, pv, gv, chunks, m);
+  std::string kt;
+  for (const Variant& v : job.variants) kt += v.key + "\t" + std::to_string(v.threshold) + "\n";
+  info[0] = chunks;
+  info[1] = m;
+  info[2] = (uint32_t)S;
+  info[3] = row;
+  info[4] = (uint32_t)vars.size();
+  info[5] = (uint32_t)kt.size();
+  if (prog && prog_cap >= pv.size()) std::memcpy(prog, pv.data(), pv.size() * 4);
+  if (pgid && pgid_cap >= gv.size()) std::memcpy(pgid, gv.data(), gv.size() * 4);
+  if (keys && keys_cap >= kt.size()) std::memcpy(keys, kt.data(), kt.size());
+  return 0;
+}
 
 void cofx_mismatch_table(uint8_t* out) {
   if (!out) return;

@@ -98,7 +98,10 @@ struct PatternGroup {
   bool concrete_only = true;   // no variant uses a degenerate IUPAC code
   std::vector<uint32_t> gids;  // global variant ids, ascending
   double nonN_sum = 0;         // sum of non-N positions over the group's variants
-  DevBuf vmask, bs_off, bs_thr, bs_gid;
+  // Bit-sliced comparer programs (layout in kernels.cuh): bs_chunks chunks of
+  // 32 lane programs, each a first variant and bs_m - 1 update steps.
+  uint32_t bs_chunks = 0, bs_m = 1;
+  DevBuf vmask, bs_prog, bs_pgid;
 };
 
 }  // namespace eng
@@ -163,6 +166,11 @@ void init_group(PatternGroup& g, const std::string& pattern);
 // Builds and uploads g's comparer tables for its variants `vars` (g.gids
 // already set, one id per variant).  Synchronizes h->stream.
 cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars);
+// Lane programs of the bit-sliced comparer for `vars` (ids `gids`), `S` slots,
+// class rows of `row` words; layout in kernels.cuh.
+void build_bs_programs(const std::vector<const Variant*>& vars, const std::vector<uint32_t>& gids, int S,
+                       uint32_t row, std::vector<uint32_t>& prog, std::vector<uint32_t>& pgid, uint32_t& chunks,
+                       uint32_t& m);
 // Row shapes of `vars` (variant i gets id first_gid + i) appended to the
 // formatting tables vf (indexed by id), sf and pool.
 void append_format_tables(const Job& job, std::vector<VariantFmt>& vf, std::vector<ShapeFmt>& sf, std::string& pool);

@@ -105,6 +105,7 @@ bool parse_job(const char* text, size_t len, Job& job, std::string& err) {
     v.id = id;
     v.threshold = thr;
     v.bulges.push_back(std::move(b));
+    v.order = (uint32_t)table.size();
     table.emplace(key, std::move(v));
   };
   try {

@@ -106,14 +106,24 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
                      const void* vars, uint32_t nvar, int nw, uint32_t L, uint64_t* hits,
                      unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
 // Bit-sliced comparer (comparer_bs.cu) for variants with at most 32 positions
-// that can mismatch.  `voff` holds, per variant, `slots` u16 shared-memory
-// byte offsets ((class * row + k) * 8, 0 = padding), packed two per word;
-// `vthr` the thresholds; `vgid` the global variant indices.  Returns false if
-// no kernel instance fits (then use launch_comparer).
-// `concrete_only`: no variant uses a degenerate IUPAC code (only the four
-// concrete-base class rows are built).
+// that can mismatch.  The variants come as `chunks` chunks of 32 lane
+// programs; a lane program tests up to `m` variants: its first variant is
+// counted in full, each later one by updating the count with one added and one
+// removed class word per step.  Words per lane program: 1 + slots/2 + (m - 1),
+// stored lane-minor (word w of lane l of chunk c at (c * words + w) * 32 + l):
+//   word 0           bits 0-7: 2^NB - 1 - min(threshold, 2^NB - 1), NB =
+//                    bit_width(slots); bit 8: the first variant is real
+//   words 1..slots/2 the first variant's slots: u16 shared-memory byte
+//                    offsets (class * row + k) * 8, two per word, 0 = padding
+//   then m - 1 steps bits 0-14: offset of the word added, bit 15: a variant
+//                    ends with this step (test it), bits 16-30: offset of the
+//                    word removed (offset 0 = nothing)
+// `pgid[(c * m + e) * 32 + l]` is the global id of lane l's e-th tested
+// variant.  Returns false if no kernel instance fits (then use
+// launch_comparer).  `concrete_only`: no variant uses a degenerate IUPAC code
+// (only the four concrete-base class rows are built).
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-                        const uint32_t* voff, const uint32_t* vthr, const uint32_t* vgid, uint32_t nvar, int slots,
+                        const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
                         uint32_t L, bool concrete_only, uint64_t* hits, unsigned long long* hit_count,
                         uint64_t hit_cap, int sm_count, cudaStream_t stream);
 int bs_slots_for(int max_positions);  // 0 when more than 32 positions can mismatch

@@ -6,6 +6,7 @@
 #ifndef COF_TOOLS_H
 #define COF_TOOLS_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -34,6 +35,17 @@ void cofx_mismatch_table(uint8_t* out);
  * and IADD (32-bit add).  These are the denominators of the comparer's
  * roofline.  Takes about a second.  Returns 0 on success. */
 int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd);
+
+/* Test hook: parses one input file (the whole text) and builds the lane
+ * programs of the bit-sliced comparer for its compare variants (layout in
+ * cas-offinder_gb300/csrc/kernels.cuh, launch_comparer_bs).  info[0..5] =
+ * {chunks, m, slots, class-row words, variants, bytes of keys}.  Each output
+ * is filled when its capacity suffices: prog chunks * (1 + slots/2 + m - 1) *
+ * 32 words, pgid chunks * m * 32 words, keys one "key\tthreshold\n" line per
+ * variant in id order.  Returns 0; 1 on a parse error; 2 when the variants do
+ * not fit the bit-sliced comparer. */
+int cofx_bs_programs(const char* input, size_t len, uint32_t* info, uint32_t* prog, size_t prog_cap, uint32_t* pgid,
+                     size_t pgid_cap, char* keys, size_t keys_cap);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,126 @@
+"""Lane programs of the bit-sliced comparer (host logic, no GPU).
+
+A lane program counts its first variant in full and reaches each later one by
+steps that add one class word and remove one.  Replaying the programs as set
+operations must produce every compare variant exactly once, with exactly its
+own slots and its own threshold bias -- whatever chains the builder chose."""
+import random
+
+import pytest
+
+CLASS = {c: i + 1 for i, c in enumerate("TCAGVDBHRYKMWS")}  # row of a pattern byte; others never mismatch
+
+
+def bit_width(s):
+    b = 1
+    while (1 << b) <= s:
+        b += 1
+    return b
+
+
+def replay(P, text):
+    r = P.bs_programs(text)
+    S, m, row = r["slots"], r["m"], r["row"]
+    words = 1 + S // 2 + (m - 1)
+    prog = r["prog"].reshape(max(r["chunks"], 1), words, 32)
+    pgid = r["pgid"].reshape(max(r["chunks"], 1), m, 32)
+    nb = bit_width(S)
+    seen = {}
+    for c in range(r["chunks"]):
+        for lane in range(32):
+            hdr = int(prog[c, 0, lane])
+            cur = set()
+            for w in range(S // 2):
+                pk = int(prog[c, 1 + w, lane])
+                for off in (pk & 0xFFFF, pk >> 16):
+                    if off:
+                        assert off not in cur
+                        cur.add(off)
+            kadd = hdr & 0xFF
+            e = 0
+            out = []
+            if hdr & 0x100:
+                out.append((int(pgid[c, 0, lane]), frozenset(cur), kadd))
+                e = 1
+            else:
+                assert not cur
+            for st in range(m - 1):
+                w = int(prog[c, 1 + S // 2 + st, lane])
+                add, rem, emit = w & 0x7FFF, w >> 16, bool(w & 0x8000)
+                assert rem < 0x8000
+                if rem:
+                    assert rem in cur, "a step removes a word the count does not hold"
+                    cur.remove(rem)
+                if add:
+                    assert add not in cur
+                    cur.add(add)
+                # the biased counter never overflows its NB + 1 planes
+                assert len(cur) <= S + 1
+                if emit:
+                    out.append((int(pgid[c, e, lane]), frozenset(cur), kadd))
+                    e += 1
+            for gid, slots, k in out:
+                assert gid not in seen, f"variant {gid} tested twice"
+                seen[gid] = (slots, k)
+    variants = r["variants"]
+    assert sorted(seen) == list(range(len(variants))), "every variant exactly once"
+    for gid, (key, thr) in enumerate(variants):
+        want = frozenset((CLASS[ch] * row + k) * 8 for k, ch in enumerate(key) if ch in CLASS)
+        slots, k = seen[gid]
+        assert slots == want, f"variant {gid} ({key}) counted over the wrong slots"
+        assert len(want) <= S
+        assert k == (1 << nb) - 1 - min(thr, (1 << nb) - 1)
+    return r
+
+
+def guide_input(guides, pattern, dna, rna, genome="g.fa"):
+    head = pattern + (f" {dna} {rna}" if dna or rna else "")
+    return "\n".join([genome, head] + [f"{g} {mm}" for g, mm in guides]) + "\n"
+
+
+def rand_guide(rng, n, alphabet="ACGT"):
+    return "".join(rng.choice(alphabet) for _ in range(n))
+
+
+def test_plain_workload_chains(P):
+    """NRG, DNA bulge 2, RNA bulge 1, four 20-nt guides: bulge variants chain,
+    so far fewer than one lane per variant is needed."""
+    rng = random.Random(3)
+    guides = [(rand_guide(rng, 20) + "NNN", 5) for _ in range(4)]
+    r = replay(P, guide_input(guides, "N" * 21 + "RG", 2, 1))
+    assert len(r["variants"]) > 200
+    assert r["m"] > 1
+    assert r["chunks"] * 32 < len(r["variants"])
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_inputs(P, seed):
+    rng = random.Random(100 + seed)
+    pam5 = seed % 2 == 1
+    pam = rng.choice(["NGG", "NRG", "NNGRRT", "TTTV", "NAG"])
+    spacer = rng.randint(12, 24)
+    dna, rna = rng.randint(0, 2), rng.randint(0, 2)
+    if pam5:
+        pam = rng.choice(["TTTV", "TTTN"])
+        pattern = pam + "N" * spacer
+    else:
+        pattern = "N" * spacer + pam
+    guides = []
+    for i in range(rng.randint(1, 12)):
+        g = rand_guide(rng, spacer, "ACGT" if i % 3 else "ACGTRYKMSWN")
+        guides.append(((("N" * len(pam)) + g) if pam5 else (g + "N" * len(pam)), rng.randint(0, 8)))
+    # a duplicate guide with another threshold (first inserter wins) and an
+    # all-threshold guide
+    guides.append((guides[0][0], 1))
+    guides.append((guides[-2][0], 65535 % 65536))
+    replay(P, guide_input(guides, pattern, dna, rna))
+
+
+def test_homopolymer_and_wide_thresholds(P):
+    guides = [("A" * 20 + "NGG", 3), ("ACGTACGTAAAACCCCGGGG" + "NGG", 0), ("T" * 20 + "NGG", 40)]
+    replay(P, guide_input(guides, "N" * 20 + "NGG", 2, 2))
+
+
+def test_single_variant(P):
+    r = replay(P, guide_input([("ACGTACGTACGTACGTACGT" + "NGG", 4)], "N" * 20 + "NGG", 0, 0))
+    assert r["chunks"] == 1 and r["m"] == 1
