@@ -10,9 +10,10 @@ guides + NNN with at most 5 mismatches.  All inputs are seeded.
 One step = one full search of the genome (PAM scan, compare, sort, row
 formatting on the GPU, rows copied to host memory).
   value : steps with the packed genome already resident in HBM.
-  e2e   : steps through the C ABI from host buffers: each step copies the
-          genome planes from pinned host memory (cof_genome_load_planes),
-          searches, and copies the rows back (cof_search).
+  e2e   : steps through the C ABI from host buffers: each step uploads the
+          genome planes from pinned host memory and searches them in one call
+          (cof_search_planes: the upload of segment s+1 overlaps the scan of
+          segment s), and copies the rows back.
 The genome planes (1.16 GB) are larger than L2, so no flush is needed between
 steps.  Timing: CUDA events on the engine's stream (cof_timer_start/stop),
 after warm-up steps, max over ranks.  Under torchrun each rank runs an
@@ -398,14 +399,12 @@ def main():
 
     # ---- e2e: host planes -> device, search, rows -> host, every step
     for _ in range(1):
-        eng.load_genome_planes(hi, lo, ot, n, None, None, names, starts)
-        eng.search_view()
+        eng.search_planes_view(hi, lo, ot, n, None, None, names, starts)
     dist_barrier(world)
     eng.synchronize()
     eng.timer_start()
     for _ in range(args.steps):
-        eng.load_genome_planes(hi, lo, ot, n, None, None, names, starts)
-        _, rows_len = eng.search_view()
+        _, rows_len = eng.search_planes_view(hi, lo, ot, n, None, None, names, starts)
     e2e_ms = dist_max(eng.timer_stop() / args.steps, world)
     e2e_value = world * N_GUIDES * gbp / (e2e_ms / 1e3)
 

@@ -32,7 +32,7 @@ HEADER = ("##Generated by Cas-OFFinder 3.0.0\n"
 # Every entry point include/cof.h declares (checked by the CPU tests).
 EXPORTS = [
     "cof_open", "cof_close", "cof_last_error", "cof_open_error", "cof_read_input", "cof_genome_path",
-    "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes",
+    "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes", "cof_search_planes",
     "cof_genome_info", "cof_search", "cof_last_hit_count", "cof_set_summary", "cof_summary_text",
     "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
     "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
@@ -83,6 +83,8 @@ def lib():
             "cof_genome_load_text": (c.c_int, [vp, c.c_char_p, u64, c.POINTER(c.c_char_p), c.POINTER(u64), u32]),
             "cof_genome_load_planes": (c.c_int, [vp, vp, vp, vp, u64, vp, vp, u64, c.POINTER(c.c_char_p),
                                                  c.POINTER(u64), u32]),
+            "cof_search_planes": (c.c_int, [vp, vp, vp, vp, u64, vp, vp, u64, c.POINTER(c.c_char_p),
+                                            c.POINTER(c.c_uint64), u32, c.POINTER(c.c_void_p), c.POINTER(sz)]),
             "cof_genome_info": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u32)]),
             "cof_search": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
             "cof_last_hit_count": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u64)]),
@@ -279,6 +281,17 @@ class CasOFFinder:
         p, n = ctypes.c_void_p(), ctypes.c_size_t()
         self._check(self._L.cof_search(self._h, ctypes.byref(p), ctypes.byref(n)))
         return _bytes_at(p.value, n.value)
+
+    def search_planes_view(self, hi, lo, ot, n, exc_pos, exc_byte, names, starts):
+        """Load + search in one call (cof_search_planes): the plane upload
+        overlaps the scan.  Returns (address, length) of the rows."""
+        arr_n = (ctypes.c_char_p * max(1, len(names)))(*[x.encode() if isinstance(x, str) else x for x in names])
+        arr_s = (ctypes.c_uint64 * max(1, len(starts)))(*starts)
+        p, m = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self._L.cof_search_planes(
+            self._h, _ptr(hi), _ptr(lo), _ptr(ot), n, _ptr(exc_pos), _ptr(exc_byte),
+            0 if exc_pos is None else exc_pos.size, arr_n, arr_s, len(names), ctypes.byref(p), ctypes.byref(m)))
+        return p.value, m.value
 
     def search_view(self):
         """(address, length) of the rows in the engine's pinned buffer, without a copy."""

@@ -322,9 +322,10 @@ __device__ __forceinline__ void step_update(uint32_t (&p)[NP], uint32_t a, uint3
   uint32_t t = a ^ b;
 #pragma unroll
   for (int i = 0; i < NP; ++i) {
-    const uint32_t pi = p[i];
-    p[i] = pi ^ t;
-    if (i + 1 < NP) t = lop3<0x90>(t, pi, a);  // t & ~(pi ^ a)
+    // The next carry first, so the plane's new value can take its register.
+    const uint32_t tn = i + 1 < NP ? lop3<0x90>(t, p[i], a) : 0u;  // t & ~(p ^ a)
+    p[i] ^= t;
+    t = tn;
   }
 }
 
@@ -375,8 +376,10 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
         emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
       }
       uint32_t e = 32;  // gid index of the lane's next tested variant, x 32
+      uint32_t wn = __ldg(steps);
       for (uint32_t i = 0; i + 1 < m; ++i) {
-        const uint32_t w = __ldg(steps + i * 32);
+        const uint32_t w = wn;
+        if (i + 2 < m) wn = __ldg(steps + (i + 1) * 32);  // one step ahead
         uint32_t a0, a1, b0, b1;
         lds64<kImm>(tbase + (w & 0x7FFFu), a0, a1);
         lds64<kImm>(tbase + (w >> 16), b0, b1);

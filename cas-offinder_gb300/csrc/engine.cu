@@ -42,9 +42,13 @@ std::mutex g_open_mu;
 std::string g_open_err;
 
 // Uploads a packed genome into `dg` (copies are stream-ordered on h->stream).
+// With `streamed` the plane copies go to h->stream3 one segment at a time
+// (events in h->upload_ev) and the call returns before they finish: the host
+// planes must stay valid until the search that waits on them is done.
 cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
                          uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
-                         const std::vector<std::string>& names, const std::vector<uint64_t>& starts) {
+                         const std::vector<std::string>& names, const std::vector<uint64_t>& starts,
+                         bool streamed = false) {
   const uint64_t W = plane_words(n);
   dg.loaded = false;
   // The record table must describe the genome like the reference's m_chrpos:
@@ -57,9 +61,30 @@ cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const
   COF_CUDA(h, dg.hi.ensure(W * 4));
   COF_CUDA(h, dg.lo.ensure(W * 4));
   COF_CUDA(h, dg.ot.ensure(W * 4));
-  COF_CUDA(h, cudaMemcpyAsync(dg.hi.p, hi, W * 4, cudaMemcpyHostToDevice, h->stream));
-  COF_CUDA(h, cudaMemcpyAsync(dg.lo.p, lo, W * 4, cudaMemcpyHostToDevice, h->stream));
-  COF_CUDA(h, cudaMemcpyAsync(dg.ot.p, ot, W * 4, cudaMemcpyHostToDevice, h->stream));
+  h->upload_pending = 0;
+  if (!streamed) {
+    COF_CUDA(h, cudaMemcpyAsync(dg.hi.p, hi, W * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(dg.lo.p, lo, W * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(dg.ot.p, ot, W * 4, cudaMemcpyHostToDevice, h->stream));
+  } else {
+    // The copy stream starts after everything already queued on the handle.
+    COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
+    COF_CUDA(h, cudaStreamWaitEvent(h->stream3, h->ev_start, 0));
+    const size_t chunks = (size_t)((W + kSegWords - 1) / kSegWords);
+    while (h->upload_ev.size() < chunks) {
+      cudaEvent_t e = nullptr;
+      COF_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      h->upload_ev.push_back(e);
+    }
+    for (size_t c = 0; c < chunks; ++c) {
+      const uint64_t w0 = c * kSegWords, nw = std::min<uint64_t>(W - w0, kSegWords);
+      COF_CUDA(h, cudaMemcpyAsync(dg.hi.as<uint32_t>() + w0, hi + w0, nw * 4, cudaMemcpyHostToDevice, h->stream3));
+      COF_CUDA(h, cudaMemcpyAsync(dg.lo.as<uint32_t>() + w0, lo + w0, nw * 4, cudaMemcpyHostToDevice, h->stream3));
+      COF_CUDA(h, cudaMemcpyAsync(dg.ot.as<uint32_t>() + w0, ot + w0, nw * 4, cudaMemcpyHostToDevice, h->stream3));
+      COF_CUDA(h, cudaEventRecord(h->upload_ev[c], h->stream3));
+    }
+    h->upload_pending = chunks;
+  }
   COF_CUDA(h, dg.exc_pos.ensure(n_exc * 8));
   COF_CUDA(h, dg.exc_byte.ensure(n_exc));
   if (n_exc) {
@@ -462,7 +487,7 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
   COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
   COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
-  uint64_t pass = 0;
+  uint64_t pass = 0, waited_seg = ~0ull;
   for (uint64_t s = 0; s < nseg; ++s) {
     for (size_t gi = 0; gi < G; ++gi) {
       const PatternGroup& g = h->groups[gi];
@@ -474,6 +499,12 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       uint32_t* qc = h->qcounts.as<uint32_t>() + s * G + gi;
       uint32_t* q = h->queue[b].as<uint32_t>();
       if (pass >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
+      if (h->upload_pending && waited_seg != s) {
+        // Segment s reads plane words up to w1 + 2: chunks s and s + 1.
+        const size_t c = std::min<size_t>((size_t)s + 1, h->upload_pending - 1);
+        COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->upload_ev[c], 0));
+        waited_seg = s;
+      }
       cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32, h->stream2);
       if (st) return st;
       launch_finder(gv, w0, w1, g.fpat, q, qc, h->stream2);
@@ -498,6 +529,10 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   // comparer was skipped; normally the last comparer already waited on it).
   COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream2));
   COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_start, 0));
+  if (h->upload_pending) {
+    // Row formatting reads the planes: the whole upload must be in.
+    COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->upload_ev[h->upload_pending - 1], 0));
+  }
   COF_CUDA(h, cudaGetLastError());
   return COF_OK;
 }
@@ -684,6 +719,7 @@ cof_status cof_open(int device, cof_handle** out) {
   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device);
   e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream3, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming);
   for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
     e = cudaEventCreateWithFlags(&h->ev_found[i], cudaEventDisableTiming);
@@ -703,7 +739,9 @@ void cof_close(cof_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
-  cudaStream_t s = h->stream, s2 = h->stream2;
+  if (h->stream3) cudaStreamSynchronize(h->stream3);
+  cudaStream_t s = h->stream, s2 = h->stream2, s3 = h->stream3;
+  for (cudaEvent_t e : h->upload_ev) cudaEventDestroy(e);
   cudaEvent_t evs[7] = {h->timer_a, h->timer_b, h->ev_start, h->ev_found[0], h->ev_found[1], h->ev_used[0],
                         h->ev_used[1]};
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
@@ -712,6 +750,7 @@ void cof_close(cof_handle* h) {
     if (ev) cudaEventDestroy(ev);
   if (s) cudaStreamDestroy(s);
   if (s2) cudaStreamDestroy(s2);
+  if (s3) cudaStreamDestroy(s3);
 }
 
 const char* cof_last_error(const cof_handle* h) { return h ? h->err.c_str() : "null handle"; }
@@ -847,6 +886,32 @@ cof_status cof_search(cof_handle* h, const char** rows, size_t* rows_len) {
   h->err.clear();
   cudaSetDevice(h->device);
   return do_search(h, rows, rows_len);
+}
+
+cof_status cof_search_planes(cof_handle* h, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot, uint64_t n,
+                             const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
+                             const char* const* names, const uint64_t* starts, uint32_t n_records,
+                             const char** rows, size_t* rows_len) {
+  if (!h || !hi || !lo || !ot || (n_exc && (!exc_pos || !exc_byte)) || (n_records && (!names || !starts)) || !rows ||
+      !rows_len)
+    return COF_ERR_ARG;
+  h->err.clear();
+  cudaSetDevice(h->device);
+  std::vector<std::string> nm;
+  std::vector<uint64_t> st;
+  for (uint32_t i = 0; i < n_records; ++i) {
+    nm.push_back(names[i] ? names[i] : "");
+    st.push_back(starts[i]);
+  }
+  cof_status r = upload_genome(h, h->genome, hi, lo, ot, n, exc_pos, exc_byte, n_exc, nm, st, true);
+  if (r == COF_OK) r = do_search(h, rows, rows_len);
+  // The host planes are not read after this call returns.
+  if (h->upload_pending) {
+    const cudaError_t e = cudaStreamSynchronize(h->stream3);
+    h->upload_pending = 0;
+    if (e != cudaSuccess && r == COF_OK) return fail(h, COF_ERR_CUDA, cudaGetErrorString(e));
+  }
+  return r;
 }
 
 cof_status cof_last_hit_count(const cof_handle* h, uint64_t* n_hits, uint64_t* n_rows) {

@@ -116,6 +116,11 @@ struct cof_handle {
   cudaStream_t stream = nullptr;   // comparer, formatting, copies
   cudaStream_t stream2 = nullptr;  // finder passes, one segment ahead of the comparer
   cudaEvent_t ev_start = nullptr, ev_found[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
+  // Streamed upload (cof_search_planes): plane copies per segment on stream3,
+  // upload_ev[c] recorded after chunk c; finders wait for their chunks.
+  cudaStream_t stream3 = nullptr;
+  std::vector<cudaEvent_t> upload_ev;
+  size_t upload_pending = 0;  // chunks of the current streamed upload (0: none)
   std::string err;
 
   // The batch: one or more parsed input files ("jobs").  Variant ids are

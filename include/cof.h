@@ -103,6 +103,19 @@ cof_status cof_genome_info(const cof_handle* h, uint64_t* n, uint32_t* n_records
  *      `*rows` points into a buffer owned by the handle, valid until the next
  *      search or cof_close. */
 cof_status cof_search(cof_handle* h, const char** rows, size_t* rows_len);
+/* Load + search in one call, for a genome that lives in host memory (the
+ * reference's per-file loop: setChrData, then loadNextChunk / findPattern /
+ * compareAll per chunk, cas-offinder.cpp:175-297, 330-469).  Arguments as
+ * cof_genome_load_planes, results as cof_search.  The planes are copied one
+ * segment at a time on a copy stream while earlier segments are already
+ * being scanned, so the copy hides under the search.  The host planes are
+ * read only during the call (pinned memory gives the overlap; pageable memory
+ * works, copied synchronously); afterwards the genome stays resident as
+ * after cof_genome_load_planes. */
+cof_status cof_search_planes(cof_handle* h, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot, uint64_t n,
+                             const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
+                             const char* const* names, const uint64_t* starts, uint32_t n_records,
+                             const char** rows, size_t* rows_len);
 /* ---- batched search: several input files ("jobs") over the resident genome
  * in one pass.  Jobs whose padded patterns are equal share one PAM scan and
  * one comparer launch per genome segment; each job keeps its own compare

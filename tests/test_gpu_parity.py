@@ -96,6 +96,39 @@ def test_abi_text_and_planes_loaders_agree(P, built, tmp_path):
         assert P.HEADER.encode() + eng.search() == want
 
 
+def test_search_planes_streams_like_resident_search(P, built):
+    """cof_search_planes (upload of segment s+1 overlapped with the scan of
+    segment s) gives the rows of load_genome_planes + cof_search, on a genome
+    of several 2^26-position segments, from pageable and from pinned memory;
+    afterwards the genome is resident."""
+    import random
+    rng = random.Random(11)
+    lens = [70_000_000, 45_000_000, 33_000_000]
+    seqs = [P.synth_record(21, r, n, gc=0.41, n_frac=0.02, n_run_min=100, n_run_max=5000)
+            for r, n in enumerate(lens)]
+    text, starts = P.reference_text(seqs)
+    names = [f"chr{i + 1}" for i in range(len(lens))]
+    hi, lo, ot, ep, eb = P.pack_text(text)
+    guides = ["".join(rng.choice("ACGT") for _ in range(20)) + "NNN" for _ in range(3)]
+    inp = "synthetic\n" + "N" * 21 + "RG 1 1\n" + "".join(f"{g} 5\n" for g in guides)
+    with P.CasOFFinder(0) as eng:
+        eng.readInputFile(inp)
+        eng.load_genome_planes(hi, lo, ot, len(text), ep, eb, names, starts)
+        want = eng.search()
+        assert len(cases.rows_of(want)) > 100
+        got = P._bytes_at(*eng.search_planes_view(hi, lo, ot, len(text), ep, eb, names, starts))
+        assert got == want
+        torch = pytest.importorskip("torch")
+        W = P.plane_words(len(text))
+        pinned = torch.empty(3 * W, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        pinned[:W], pinned[W:2 * W], pinned[2 * W:] = hi, lo, ot
+        got = P._bytes_at(*eng.search_planes_view(pinned[:W], pinned[W:2 * W], pinned[2 * W:], len(text), ep, eb,
+                                                  names, starts))
+        assert got == want
+        pinned[:] = 0  # the genome is resident: the host planes are no longer read
+        assert eng.search() == want
+
+
 def read_fasta(path):
     names, seqs = [], []
     for line in open(path, "rb").read().split(b"\n"):
