@@ -162,7 +162,7 @@ def bs_programs(text):
     if st != 0:
         raise CofError(st, "input does not fit the bit-sliced comparer" if st == 2 else "parse error")
     chunks, m, slots, row, nvar, kb = (int(x) for x in info)
-    prog = np.zeros(max(chunks, 1) * (1 + slots // 2 + m - 1) * 32, dtype=np.uint32)
+    prog = np.zeros(max(chunks, 1) * (1 + slots // 2 + 2 * (m // 2)) * 32, dtype=np.uint32)
     pgid = np.zeros(max(chunks, 1) * m * 32, dtype=np.uint32)
     keys = ctypes.create_string_buffer(kb + 1)
     lib().cofx_bs_programs(raw, len(raw), _ptr(info), _ptr(prog), prog.size, _ptr(pgid), pgid.size, keys, kb + 1)

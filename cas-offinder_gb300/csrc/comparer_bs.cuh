@@ -228,7 +228,13 @@ __device__ __forceinline__ void build_pair(const RawWindow<NK>& ra, const RawWin
   for (int i = 0; i < NK; ++i) {
     const uint32_t h0 = warp_transpose(ha[i], lane), h1 = warp_transpose(hb[i], lane);
     const uint32_t l0 = warp_transpose(la[i], lane), l1 = warp_transpose(lb[i], lane);
-    const uint32_t o0 = warp_transpose(oa[i], lane), o1 = warp_transpose(ob[i], lane);
+    // Windows holding a non-base byte (N, a separator, another byte) are rare:
+    // most pairs skip the third plane's transposes.
+    uint32_t o0 = 0, o1 = 0;
+    if (__any_sync(kFull, oa[i] | ob[i])) {
+      o0 = warp_transpose(oa[i], lane);
+      o1 = warp_transpose(ob[i], lane);
+    }
     const unsigned k = i * 32 + lane;
     if (k < (unsigned)ROW) {
       // One LOP3 of (h, l, o) each; truth tables over (0xF0, 0xCC, 0xAA).
@@ -334,7 +340,7 @@ __device__ __forceinline__ void step_update(uint32_t (&p)[NP], uint32_t a, uint3
 // index is a compile-time constant, so every load is [register + immediate]).
 template <int P, int S, int ROW, bool CONC>
 __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
-                                            uint32_t kadd, uint32_t first_on, const uint32_t* __restrict__ steps,
+                                            uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
                                             const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase, unsigned W,
                                             const uint32_t* ents, uint64_t seg_pos0, uint64_t* __restrict__ hits,
                                             unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
@@ -376,24 +382,29 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
         emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
       }
       uint32_t e = 32;  // gid index of the lane's next tested variant, x 32
-      uint32_t wn = __ldg(steps);
-      for (uint32_t i = 0; i + 1 < m; ++i) {
-        const uint32_t w = wn;
-        if (i + 2 < m) wn = __ldg(steps + (i + 1) * 32);  // one step ahead
+      auto step = [&](uint32_t w) {
         uint32_t a0, a1, b0, b1;
         lds64<kImm>(tbase + (w & 0x7FFFu), a0, a1);
         lds64<kImm>(tbase + (w >> 16), b0, b1);
         step_update<NB + 1>(pa, a0, b0);
         step_update<NB + 1>(pb, a1, b1);
         const uint32_t on = (w & 0x8000u) ? kFull : 0u;
-        hita = ~pa[NB] & on;
-        hitb = ~pb[NB] & on;
-        if (__any_sync(kFull, hita | hitb)) {
-          const uint32_t gid = (hita | hitb) ? __ldg(gids + e) : 0u;
-          emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-          emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+        const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
+        if (__any_sync(kFull, ha | hb)) {
+          const uint32_t gid = (ha | hb) ? __ldg(gids + e) : 0u;
+          emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+          emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
         }
         e += on & 32u;
+      };
+      // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
+      const uint32_t sp = m / 2;
+      uint2 wn = __ldg(steps);
+      for (uint32_t j = 0; j < sp; ++j) {
+        const uint2 w2 = wn;
+        if (j + 1 < sp) wn = __ldg(steps + (j + 1) * 32);
+        step(w2.x);
+        step(w2.y);
       }
     }
     run_program<P + 1, S, ROW, CONC>(addr, kmask, kadd, first_on, steps, gids, m, tbase, W, ents, seg_pos0, hits,
@@ -439,7 +450,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   const uint32_t* stage = ents_all + 2 * W * 64 + threadIdx.x;
   const uint32_t stage_a = (uint32_t)__cvta_generic_to_shared(stage);
   const uint32_t stage_b = stage_a + Stage<NK>::kSlots * kS * 4;
-  const uint32_t words = 1 + S / 2 + (m - 1);  // per lane program
+  const uint32_t words = 1 + S / 2 + 2 * (m / 2);  // per lane program
 
   // Row 0 (pattern bytes that never mismatch: padding slots) stays zero.
   for (unsigned i = threadIdx.x; i < 2 * W * ROW; i += blockDim.x)
@@ -485,8 +496,10 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     for (uint32_t c = warp; c < chunks; c += W) {
       const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
       if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
-      run_program<0, S, ROW, CONC>(addr, kmask, kadd, first_on, pr + (1 + S / 2) * 32, pgid + (size_t)c * m * 32 + lane,
-                                   m, tbase, W, ents, seg_pos0, hits, hit_count, hit_cap);
+      run_program<0, S, ROW, CONC>(addr, kmask, kadd, first_on,
+                                   (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
+                                   pgid + (size_t)c * m * 32 + lane, m, tbase, W, ents, seg_pos0, hits, hit_count,
+                                   hit_cap);
     }
     cp_async_wait_all();
     if (tn < ntiles) {

@@ -271,7 +271,7 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
   const uint32_t m = best_m;
   chunks = (uint32_t)((pieces.size() + 31) / 32);
   m_out = m;
-  const size_t words = 1 + S / 2 + (m - 1);
+  const size_t words = 1 + S / 2 + 2 * (m / 2);
   prog.assign(std::max<size_t>(chunks, 1) * words * 32, 0);
   pgid.assign(std::max<size_t>(chunks, 1) * m * 32, 0xFFFFFFFFu);
   for (size_t pi = 0; pi < pieces.size(); ++pi) {
@@ -286,7 +286,8 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
     for (size_t x = pieces[pi].first + 1; x < pieces[pi].second; ++x) {
       diff(ord[x - 1], ord[x], st);
       for (size_t j = 0; j < st.size(); ++j, ++step)
-        W(1 + S / 2 + step) = st[j].first | (j + 1 == st.size() ? 0x8000u : 0u) | ((uint32_t)st[j].second << 16);
+        prog[c * words * 32 + (1 + S / 2) * 32 + ((step / 2) * 32 + l) * 2 + step % 2] =
+            st[j].first | (j + 1 == st.size() ? 0x8000u : 0u) | ((uint32_t)st[j].second << 16);
       pgid[(c * m + e) * 32 + l] = gids[ord[x]];
       ++e;
     }

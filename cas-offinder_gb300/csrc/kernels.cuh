@@ -109,15 +109,18 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
 // that can mismatch.  The variants come as `chunks` chunks of 32 lane
 // programs; a lane program tests up to `m` variants: its first variant is
 // counted in full, each later one by updating the count with one added and one
-// removed class word per step.  Words per lane program: 1 + slots/2 + (m - 1),
-// stored lane-minor (word w of lane l of chunk c at (c * words + w) * 32 + l):
+// removed class word per step.  Words per lane program: words = 1 + slots/2 +
+// 2 * (m / 2); chunk c occupies words * 32 words from c * words * 32:
 //   word 0           bits 0-7: 2^NB - 1 - min(threshold, 2^NB - 1), NB =
 //                    bit_width(slots); bit 8: the first variant is real
 //   words 1..slots/2 the first variant's slots: u16 shared-memory byte
 //                    offsets (class * row + k) * 8, two per word, 0 = padding
-//   then m - 1 steps bits 0-14: offset of the word added, bit 15: a variant
-//                    ends with this step (test it), bits 16-30: offset of the
-//                    word removed (offset 0 = nothing)
+//   (these 1 + slots/2 words lane-minor: word w of lane l at w * 32 + l)
+//   then the m - 1 steps (padded to an even count with zero words) as pairs,
+//                    step s of lane l at (1 + slots/2) * 32 + ((s / 2) * 32
+//                    + l) * 2 + s % 2: bits 0-14 offset of the word added,
+//                    bit 15 a variant ends with this step (test it), bits
+//                    16-30 offset of the word removed (offset 0 = nothing)
 // `pgid[(c * m + e) * 32 + l]` is the global id of lane l's e-th tested
 // variant.  Returns false if no kernel instance fits (then use
 // launch_comparer).  `concrete_only`: no variant uses a degenerate IUPAC code

@@ -40,8 +40,8 @@ int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd);
  * programs of the bit-sliced comparer for its compare variants (layout in
  * cas-offinder_gb300/csrc/kernels.cuh, launch_comparer_bs).  info[0..5] =
  * {chunks, m, slots, class-row words, variants, bytes of keys}.  Each output
- * is filled when its capacity suffices: prog chunks * (1 + slots/2 + m - 1) *
- * 32 words, pgid chunks * m * 32 words, keys one "key\tthreshold\n" line per
+ * is filled when its capacity suffices: prog chunks * (1 + slots/2 + 2 *
+ * (m / 2)) * 32 words, pgid chunks * m * 32 words, keys one "key\tthreshold\n" line per
  * variant in id order.  Returns 0; 1 on a parse error; 2 when the variants do
  * not fit the bit-sliced comparer. */
 int cofx_bs_programs(const char* input, size_t len, uint32_t* info, uint32_t* prog, size_t prog_cap, uint32_t* pgid,

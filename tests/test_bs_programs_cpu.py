@@ -21,17 +21,17 @@ def bit_width(s):
 def replay(P, text):
     r = P.bs_programs(text)
     S, m, row = r["slots"], r["m"], r["row"]
-    words = 1 + S // 2 + (m - 1)
-    prog = r["prog"].reshape(max(r["chunks"], 1), words, 32)
+    words = 1 + S // 2 + 2 * (m // 2)
+    prog = r["prog"].reshape(max(r["chunks"], 1), words * 32)
     pgid = r["pgid"].reshape(max(r["chunks"], 1), m, 32)
     nb = bit_width(S)
     seen = {}
     for c in range(r["chunks"]):
         for lane in range(32):
-            hdr = int(prog[c, 0, lane])
+            hdr = int(prog[c, lane])
             cur = set()
             for w in range(S // 2):
-                pk = int(prog[c, 1 + w, lane])
+                pk = int(prog[c, (1 + w) * 32 + lane])
                 for off in (pk & 0xFFFF, pk >> 16):
                     if off:
                         assert off not in cur
@@ -44,8 +44,10 @@ def replay(P, text):
                 e = 1
             else:
                 assert not cur
-            for st in range(m - 1):
-                w = int(prog[c, 1 + S // 2 + st, lane])
+            for st in range(2 * (m // 2)):
+                w = int(prog[c, (1 + S // 2) * 32 + ((st // 2) * 32 + lane) * 2 + st % 2])
+                if st >= m - 1:
+                    assert w == 0, "padding step"
                 add, rem, emit = w & 0x7FFF, w >> 16, bool(w & 0x8000)
                 assert rem < 0x8000
                 if rem:
