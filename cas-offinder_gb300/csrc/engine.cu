@@ -637,8 +637,8 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
     return fail(h, COF_ERR_DEVICE, "row text of " + std::to_string(bytes) + " bytes for " + std::to_string(nrows) +
                                        " rows (" + std::to_string(nhits) + " hits)");
   COF_CUDA(h, h->text.ensure(bytes + 1));
-  launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), h->text.as<char>(),
-                    h->stream);
+  launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), bytes,
+                    h->text.as<char>(), h->stream);
   if ((st = record_stop(h, evs, h->stream))) return st;
   COF_CUDA(h, cudaGetLastError());
   COF_CUDA(h, h->host_text.ensure(bytes + 1));

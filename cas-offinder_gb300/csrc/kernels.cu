@@ -348,11 +348,9 @@ __global__ void row_len_kernel(GenomeView g, FormatTables ft, const uint64_t* __
   row_count[i] = vf.shape_end[h.strand] - vf.shape_begin[h.strand];
 }
 
-__global__ void write_rows_kernel(GenomeView g, FormatTables ft, const uint64_t* __restrict__ hits, uint64_t n_hits,
-                                  const uint64_t* __restrict__ offsets, char* __restrict__ out) {
-  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_hits) return;
-  const HitView h = decode(hits[i]);
+// Rows of one hit at `o` (the bytes row_len_kernel counted).
+__device__ __forceinline__ void write_row(const GenomeView& g, const FormatTables& ft, uint64_t key, char* o) {
+  const HitView h = decode(key);
   const VariantFmt vf = ft.var[h.gid];
   const uint32_t L = vf.L;
   const char* comp = ft.pool + vf.comp_off;
@@ -368,7 +366,6 @@ __global__ void write_rows_kernel(GenomeView g, FormatTables ft, const uint64_t*
   const uint64_t rel = h.pos - g.rec_start[rec];
   const char* name = g.rec_names + g.rec_name_off[rec];
   const uint32_t name_len = g.rec_name_len[rec];
-  char* o = out + offsets[i];
   for (uint32_t s = vf.shape_begin[h.strand]; s < vf.shape_end[h.strand]; ++s) {
     const ShapeFmt sh = ft.shape[s];
     for (uint32_t k = 0; k < sh.head_len; ++k) *o++ = ft.pool[sh.head_off + k];
@@ -389,6 +386,37 @@ __global__ void write_rows_kernel(GenomeView g, FormatTables ft, const uint64_t*
   }
 }
 
+// One thread per hit.  A block's rows are one contiguous byte range of the
+// output; when it fits in shared memory the threads write it there (placed
+// at the same offset mod 16 as in the output) and the block stores it with
+// 16-byte stores, otherwise the threads write straight to the output.
+constexpr int kRowThreads = 128;
+constexpr uint32_t kRowStage = 32768;
+
+__global__ void __launch_bounds__(kRowThreads) write_rows_kernel(GenomeView g, FormatTables ft,
+                                                                 const uint64_t* __restrict__ hits, uint64_t n_hits,
+                                                                 const uint64_t* __restrict__ offsets, uint64_t total,
+                                                                 char* __restrict__ out) {
+  __shared__ __align__(16) char stage[kRowStage];
+  const uint64_t i0 = (uint64_t)blockIdx.x * kRowThreads, i = i0 + threadIdx.x;
+  const uint64_t i1 = min(i0 + kRowThreads, n_hits);
+  const uint64_t base = offsets[i0], end = i1 < n_hits ? offsets[i1] : total;
+  const uint64_t a0 = base & ~15ull;  // stage[0] holds output byte a0
+  const bool staged = end - a0 <= kRowStage;
+  if (i < n_hits) write_row(g, ft, hits[i], staged ? stage + (offsets[i] - a0) : out + offsets[i]);
+  if (!staged) return;  // the same for the whole block
+  __syncthreads();
+  for (uint64_t c = a0 + 16 * threadIdx.x; c < end; c += 16 * kRowThreads) {
+    const char* src = stage + (c - a0);
+    if (c >= base && c + 16 <= end) {
+      *(uint4*)(out + c) = *(const uint4*)src;
+    } else {
+      for (uint32_t k = 0; k < 16; ++k)
+        if (c + k >= base && c + k < end) out[c + k] = src[k];
+    }
+  }
+}
+
 void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
                         uint64_t* row_bytes, uint32_t* row_count, cudaStream_t stream) {
   if (!n_hits) return;
@@ -396,9 +424,10 @@ void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint6
 }
 
 void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
-                       const uint64_t* offsets, char* out, cudaStream_t stream) {
+                       const uint64_t* offsets, uint64_t total, char* out, cudaStream_t stream) {
   if (!n_hits) return;
-  write_rows_kernel<<<(unsigned)((n_hits + 127) / 128), 128, 0, stream>>>(g, ft, hits, n_hits, offsets, out);
+  write_rows_kernel<<<(unsigned)((n_hits + kRowThreads - 1) / kRowThreads), kRowThreads, 0, stream>>>(
+      g, ft, hits, n_hits, offsets, total, out);
 }
 
 // Byte offset of each job's first row: job j's hits start at the first sorted

@@ -266,7 +266,7 @@ cof_status format_request(cof_server* s, Request& r) {
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
   const uint64_t bytes = last[0] + last[1];
   COF_CUDA(h, s->fmt_text.ensure(bytes + 1));
-  launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), s->fmt_text.as<char>(),
+  launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), bytes, s->fmt_text.as<char>(),
                     h->stream);
   COF_CUDA(h, cudaGetLastError());
   r.rows.resize(bytes);
