@@ -129,21 +129,27 @@ def run_served(P, eng, lens, args):
         with P.Server(eng) as srv:
             t0 = time.perf_counter()
 
-            def client():
-                t = t0
-                for j, (text, _) in enumerate(reqs):
-                    t += rng.expovariate(rate)
-                    d = t - time.perf_counter()
-                    if d > 0:
-                        time.sleep(d)
-                    tickets[j] = srv.submit(text)
+            # Each arrival is submitted from its own thread, as concurrent
+            # callers would (submit parses the input file on the caller's
+            # thread).
+            def submit(j, at):
+                d = at - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                tickets[j] = srv.submit(reqs[j][0])
 
-            th = threading.Thread(target=client)
-            th.start()
-            th.join()
+            threads, at = [], t0
             for j in range(len(reqs)):
-                _, lat[j] = srv.wait(tickets[j])
+                at += rng.expovariate(rate)
+                threads.append(threading.Thread(target=submit, args=(j, at)))
+                threads[-1].start()
+            for th in threads:
+                th.join()
+            for j in range(len(reqs)):
+                _, _, lat[j] = srv.wait_view(tickets[j])  # rows left in the server's pinned buffer
             span = time.perf_counter() - t0
+            for j in range(len(reqs)):
+                srv.release(tickets[j])
             st = srv.stats()
         lat_sorted = sorted(lat)
         p99 = lat_sorted[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
@@ -380,19 +386,24 @@ def main():
         addr, rows_len = eng.search_view()
     nh, nrows = eng.last_hit_count()
 
-    # ---- value: genome resident in HBM
-    dist_barrier(world)
+    # ---- per-kernel times (CUDA events around every launch): one profiled
+    # search, outside the timed region
     eng.synchronize()
     eng.reset_stats()
     eng.set_profiling(True)
+    eng.search_view()
+    eng.set_profiling(False)
+    stats = {k: eng.kernel_stats(k) for k in ("finder", "comparer", "format")}
+    tests_stat = eng.kernel_stats("comparer.tests")
+
+    # ---- value: genome resident in HBM (passes replayed as a CUDA graph)
+    dist_barrier(world)
+    eng.synchronize()
     with ClockSampler(local) as clk:
         eng.timer_start()
         for _ in range(args.steps):
             eng.search_view()
         ms = eng.timer_stop()
-    eng.set_profiling(False)
-    stats = {k: eng.kernel_stats(k) for k in ("finder", "comparer", "format")}
-    tests_stat = eng.kernel_stats("comparer.tests")
     ms_step = dist_max(ms / args.steps, world)
     gbp = sum(lens) / 1e9
     value = world * N_GUIDES * gbp / (ms_step / 1e3)
@@ -447,7 +458,10 @@ def main():
             cpu = {"value": None, "unit": "guide-Gbp/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {e}"[:300]}
 
-    launches = int(stats["finder"]["launches"] + stats["comparer"]["launches"] + 2 * stats["format"]["launches"])
+    # Kernels of ours per search (finder and comparer per segment; row
+    # lengths, row writing and job bounds once), times the timed searches.
+    launches = args.steps * int(stats["finder"]["launches"] + stats["comparer"]["launches"] +
+                                3 * stats["format"]["launches"])
     batched = None if args.no_batched else run_batched(P, eng, lens, rates, args)
     served = None if args.no_served else run_served(P, eng, lens, args)
     if rank == 0:
@@ -469,7 +483,7 @@ def main():
             "roofline_finder": {"bound": "hbm", "achieved": finder_gbs, "peak": peaks.get("hbm_gbs"),
                                 "unit": "GB/s", "frac": finder_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs")
                                 else None, "basis": "0.375 B per genome position (3 bit planes)"},
-            "kernel_ms_per_step": {k: v["ms"] / max(1, args.steps) for k, v in stats.items()},
+            "kernel_ms_per_step": {k: v["ms"] for k, v in stats.items()},
             "batched": batched,
             "served": served,
             "cpu_baseline": cpu,

@@ -431,6 +431,21 @@ class Server:
         self._L.cof_server_release(self._s, ticket)
         return rows, lat.value
 
+    def wait_view(self, ticket, timeout_ms=-1):
+        """(rows address, rows length, latency ms) without copying the rows,
+        or None on timeout; the rows stay valid until release(ticket)."""
+        p, n, lat = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_double()
+        st = self._L.cof_server_wait(self._s, ticket, timeout_ms, ctypes.byref(p), ctypes.byref(n),
+                                     ctypes.byref(lat))
+        if st == 11:
+            return None
+        if st != COF_OK:
+            raise CofError(st, self._L.cof_server_last_error(self._s).decode())
+        return p.value, n.value, lat.value
+
+    def release(self, ticket):
+        self._L.cof_server_release(self._s, ticket)
+
     def stats(self):
         vals = [ctypes.c_uint64() for _ in range(6)]
         self._L.cof_server_stats(self._s, *[ctypes.byref(v) for v in vals])

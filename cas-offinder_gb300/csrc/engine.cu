@@ -197,15 +197,20 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
                        uint32_t& m_out) {
   const size_t V = vars.size();
   const int NB = [&] { int b = 1; while ((1 << b) <= S) ++b; return b; }();  // bit_width(S)
-  std::vector<std::vector<uint16_t>> slots(V);
+  // Slots of each variant as sorted u16 offsets, S per variant (cnt used).
+  std::vector<uint16_t> slot((size_t)std::max<size_t>(V, 1) * S);
+  std::vector<uint8_t> cnt(V);
   std::vector<uint32_t> kadd(V);
   for (size_t i = 0; i < V; ++i) {
     const std::string& key = vars[i]->key;
-    for (size_t k = 0; k < key.size(); ++k) {
-      const uint32_t c = bs_class_of((unsigned char)key[k]);
-      if (c) slots[i].push_back((uint16_t)((c * row + (uint32_t)k) * 8));
+    uint16_t* sl = &slot[i * S];
+    int c = 0;
+    for (size_t k = 0; k < key.size() && c < S; ++k) {
+      const uint32_t cl = bs_class_of((unsigned char)key[k]);
+      if (cl) sl[c++] = (uint16_t)((cl * row + (uint32_t)k) * 8);
     }
-    std::sort(slots[i].begin(), slots[i].end());
+    std::sort(sl, sl + c);
+    cnt[i] = (uint8_t)c;
     kadd[i] = (1u << NB) - 1 - std::min<uint32_t>(vars[i]->threshold, (1u << NB) - 1);
   }
   // Generation order: jobs are contiguous runs of one variant array.
@@ -218,24 +223,29 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
   std::vector<uint32_t> ord(V);
   for (size_t i = 0; i < V; ++i) ord[i] = (uint32_t)i;
   std::sort(ord.begin(), ord.end(), [&](uint32_t a, uint32_t b) { return rank[a] < rank[b]; });
-  // Steps from variant u to v: (added, removed) offset pairs, 0 = none.
-  auto diff = [&](uint32_t u, uint32_t v, std::vector<std::pair<uint16_t, uint16_t>>& st) {
-    std::vector<uint16_t> add, rem;
-    std::set_difference(slots[v].begin(), slots[v].end(), slots[u].begin(), slots[u].end(), std::back_inserter(add));
-    std::set_difference(slots[u].begin(), slots[u].end(), slots[v].begin(), slots[v].end(), std::back_inserter(rem));
-    st.clear();
-    const size_t k = std::max<size_t>(1, std::max(add.size(), rem.size()));
-    for (size_t j = 0; j < k; ++j)
-      st.emplace_back(j < add.size() ? add[j] : 0, j < rem.size() ? rem[j] : 0);
+  // Steps from variant u to v: (added, removed) offset pairs, 0 = none; at
+  // most 2S.  Returns the step count (at least one, so v is tested).
+  auto diff = [&](uint32_t u, uint32_t v, uint16_t* add, uint16_t* rem) {
+    const uint16_t *x = &slot[(size_t)u * S], *y = &slot[(size_t)v * S];
+    int i = 0, j = 0, na = 0, nr = 0;
+    while (i < cnt[u] || j < cnt[v]) {
+      if (j >= cnt[v] || (i < cnt[u] && x[i] < y[j])) rem[nr++] = x[i++];
+      else if (i >= cnt[u] || y[j] < x[i]) add[na++] = y[j++];
+      else ++i, ++j;
+    }
+    const int k = std::max(1, std::max(na, nr));
+    for (int t = na; t < k; ++t) add[t] = 0;
+    for (int t = nr; t < k; ++t) rem[t] = 0;
+    return k;
   };
+  std::vector<uint16_t> add(2 * S + 1), rem(2 * S + 1);
   // Chains: cost of each link in steps (0 = chain break before this variant).
-  std::vector<uint32_t> link(V, 0);
-  std::vector<std::pair<uint16_t, uint16_t>> st;
+  std::vector<uint8_t> link(V, 0);
   for (size_t x = 1; x < V; ++x) {
     const uint32_t u = ord[x - 1], v = ord[x];
     if (kadd[u] != kadd[v]) continue;
-    diff(u, v, st);
-    if (st.size() <= 2) link[x] = (uint32_t)st.size();
+    const int k = diff(u, v, add.data(), rem.data());
+    if (k <= 2) link[x] = (uint8_t)k;
   }
   // Pieces for a step budget of m - 1: greedy along the chains.
   auto cut = [&](uint32_t m, std::vector<std::pair<size_t, size_t>>* pieces) {
@@ -276,35 +286,78 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
   pgid.assign(std::max<size_t>(chunks, 1) * m * 32, 0xFFFFFFFFu);
   for (size_t pi = 0; pi < pieces.size(); ++pi) {
     const size_t c = pi / 32, l = pi % 32;
-    auto W = [&](size_t w) -> uint32_t& { return prog[(c * words + w) * 32 + l]; };
+    uint32_t* base = &prog[c * words * 32];
     const uint32_t first = ord[pieces[pi].first];
-    W(0) = kadd[first] | (1u << 8);
-    for (size_t sl = 0; sl < slots[first].size(); ++sl) W(1 + sl / 2) |= (uint32_t)slots[first][sl] << (16 * (sl & 1));
+    base[l] = kadd[first] | (1u << 8);
+    for (int sl = 0; sl < cnt[first]; ++sl)
+      base[(1 + sl / 2) * 32 + l] |= (uint32_t)slot[(size_t)first * S + sl] << (16 * (sl & 1));
     pgid[(c * m + 0) * 32 + l] = gids[first];
     size_t step = 0;
     uint32_t e = 1;
     for (size_t x = pieces[pi].first + 1; x < pieces[pi].second; ++x) {
-      diff(ord[x - 1], ord[x], st);
-      for (size_t j = 0; j < st.size(); ++j, ++step)
-        prog[c * words * 32 + (1 + S / 2) * 32 + ((step / 2) * 32 + l) * 2 + step % 2] =
-            st[j].first | (j + 1 == st.size() ? 0x8000u : 0u) | ((uint32_t)st[j].second << 16);
+      const int k = diff(ord[x - 1], ord[x], add.data(), rem.data());
+      for (int j = 0; j < k; ++j, ++step)
+        base[(1 + S / 2) * 32 + ((step / 2) * 32 + l) * 2 + step % 2] =
+            add[j] | (j + 1 == k ? 0x8000u : 0u) | ((uint32_t)rem[j] << 16);
       pgid[(c * m + e) * 32 + l] = gids[ord[x]];
       ++e;
     }
   }
 }
 
-cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars) {
+void* pinned_acquire(cof_handle* h, size_t bytes, size_t* cap) {
+  constexpr size_t kUnit = 64ull << 20;
+  const size_t want = std::max<size_t>(kUnit, (bytes + kUnit - 1) / kUnit * kUnit);
+  {
+    std::lock_guard<std::mutex> lock(h->pinned_mu);
+    auto it = h->pinned_free.lower_bound(want);
+    if (it != h->pinned_free.end() && it->first <= 2 * want) {
+      void* p = it->second;
+      *cap = it->first;
+      h->pinned_pooled -= it->first;
+      h->pinned_free.erase(it);
+      return p;
+    }
+  }
+  void* p = nullptr;
+  if (cudaMallocHost(&p, want) != cudaSuccess) {
+    // Give the pool back to the system and try once more.
+    std::lock_guard<std::mutex> lock(h->pinned_mu);
+    for (auto& kv : h->pinned_free) cudaFreeHost(kv.second);
+    h->pinned_free.clear();
+    h->pinned_pooled = 0;
+    p = nullptr;
+    if (cudaMallocHost(&p, want) != cudaSuccess) return nullptr;
+  }
+  *cap = want;
+  return p;
+}
+
+void pinned_release(cof_handle* h, void* p, size_t cap) {
+  if (!p) return;
+  constexpr size_t kMaxPooled = 32ull << 30;
+  std::lock_guard<std::mutex> lock(h->pinned_mu);
+  h->pinned_free.emplace(cap, p);
+  h->pinned_pooled += cap;
+  while (h->pinned_pooled > kMaxPooled && !h->pinned_free.empty()) {
+    auto big = std::prev(h->pinned_free.end());
+    cudaFreeHost(big->second);
+    h->pinned_pooled -= big->first;
+    h->pinned_free.erase(big);
+  }
+}
+
+void build_group_host(bool force_popc, PatternGroup& g, const std::vector<const Variant*>& vars, GroupHost& gh) {
   const size_t V = vars.size();
   const size_t msz = g.nw == 1 ? sizeof(VariantMask<1>) : sizeof(VariantMask<2>);
-  std::vector<unsigned char> masks(std::max<size_t>(V, 1) * msz, 0);
+  gh.masks.assign(std::max<size_t>(V, 1) * msz, 0);
   int maxpos = 0;
   g.nonN_sum = 0;
   g.concrete_only = true;
   for (size_t i = 0; i < V; ++i) {
     const Variant& var = *vars[i];
-    if (g.nw == 1) fill_mask<1>(((VariantMask<1>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
-    else fill_mask<2>(((VariantMask<2>*)masks.data())[i], var.key, var.threshold, g.gids[i]);
+    if (g.nw == 1) fill_mask<1>(((VariantMask<1>*)gh.masks.data())[i], var.key, var.threshold, g.gids[i]);
+    else fill_mask<2>(((VariantMask<2>*)gh.masks.data())[i], var.key, var.threshold, g.gids[i]);
     int c = 0;
     for (char ch : var.key) {
       const uint32_t cls = bs_class_of((unsigned char)ch);
@@ -314,17 +367,32 @@ cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<
     }
     maxpos = std::max(maxpos, c);
   }
-  COF_CUDA(h, g.vmask.ensure(masks.size()));
-  COF_CUDA(h, cudaMemcpyAsync(g.vmask.p, masks.data(), masks.size(), cudaMemcpyHostToDevice, h->stream));
-  g.bs_slots = h->force_popc ? 0 : bs_slots_for(maxpos);
-  std::vector<uint32_t> prog, pgid;
+  g.bs_slots = force_popc ? 0 : bs_slots_for(maxpos);
+  gh.prog.clear();
+  gh.pgid.clear();
+  g.bs_chunks = 0;
+  g.bs_m = 1;
+  if (g.bs_slots)
+    build_bs_programs(vars, g.gids, g.bs_slots, (uint32_t)bs_row_for(g.L), gh.prog, gh.pgid, g.bs_chunks, g.bs_m);
+}
+
+cof_status upload_group(cof_handle* h, PatternGroup& g, const GroupHost& gh, cudaStream_t st) {
+  COF_CUDA(h, g.vmask.ensure(gh.masks.size()));
+  COF_CUDA(h, cudaMemcpyAsync(g.vmask.p, gh.masks.data(), gh.masks.size(), cudaMemcpyHostToDevice, st));
   if (g.bs_slots) {
-    build_bs_programs(vars, g.gids, g.bs_slots, (uint32_t)bs_row_for(g.L), prog, pgid, g.bs_chunks, g.bs_m);
-    COF_CUDA(h, g.bs_prog.ensure(prog.size() * 4));
-    COF_CUDA(h, g.bs_pgid.ensure(pgid.size() * 4));
-    COF_CUDA(h, cudaMemcpyAsync(g.bs_prog.p, prog.data(), prog.size() * 4, cudaMemcpyHostToDevice, h->stream));
-    COF_CUDA(h, cudaMemcpyAsync(g.bs_pgid.p, pgid.data(), pgid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, g.bs_prog.ensure(gh.prog.size() * 4));
+    COF_CUDA(h, g.bs_pgid.ensure(gh.pgid.size() * 4));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_prog.p, gh.prog.data(), gh.prog.size() * 4, cudaMemcpyHostToDevice, st));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_pgid.p, gh.pgid.data(), gh.pgid.size() * 4, cudaMemcpyHostToDevice, st));
   }
+  return COF_OK;
+}
+
+cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars) {
+  GroupHost gh;
+  build_group_host(h->force_popc, g, vars, gh);
+  cof_status st = upload_group(h, g, gh, h->stream);
+  if (st) return st;
   // The host vectors die on return: wait for the copies.
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
   return COF_OK;
@@ -538,6 +606,67 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   return COF_OK;
 }
 
+// Everything the captured passes depend on: buffers, sizes and each group's
+// launch parameters.
+std::string pass_graph_key(const cof_handle* h, uint64_t cap) {
+  std::string k;
+  auto put = [&](const void* p, size_t n) { k.append((const char*)p, n); };
+  auto put64 = [&](uint64_t v) { put(&v, 8); };
+  for (const void* p : {h->genome.hi.p, h->genome.lo.p, h->genome.ot.p, h->queue[0].p, h->queue[1].p, h->qcounts.p,
+                        h->hits.p, h->hit_count.p})
+    put64((uint64_t)p);
+  put64(h->genome.n);
+  put64(h->qcounts.cap);
+  put64(cap);
+  put64((uint64_t)h->sm_count);
+  for (const PatternGroup& g : h->groups) {
+    for (uint64_t v : {(uint64_t)g.L, (uint64_t)g.nw, (uint64_t)g.bs_slots, (uint64_t)g.bs_chunks, (uint64_t)g.bs_m,
+                       (uint64_t)g.concrete_only, (uint64_t)g.gids.size()})
+      put64(v);
+    for (const void* p : {g.bs_prog.p, g.bs_pgid.p, g.vmask.p}) put64((uint64_t)p);
+    put(&g.fpat, sizeof(g.fpat));
+  }
+  return k;
+}
+
+// run_passes through a CUDA graph: captured on first use (or when the key
+// changes), then one cudaGraphLaunch per search.
+cof_status run_passes_graph(cof_handle* h, uint64_t cap, uint64_t* nseg) {
+  // Buffers run_passes would allocate must exist before capture.
+  uint64_t max_words = 0;
+  for (const PatternGroup& g : h->groups) {
+    const uint64_t npos = h->genome.n >= g.L ? h->genome.n - g.L + 1 : 0;
+    max_words = std::max(max_words, (npos + 31) / 32);
+  }
+  const uint64_t ns = (max_words + kSegWords - 1) / kSegWords;
+  COF_CUDA(h, h->qcounts.ensure(std::max<uint64_t>(ns * h->groups.size(), 1) * 4));
+  const std::string key = pass_graph_key(h, cap);
+  if (!h->pass_graph || key != h->pass_key) {
+    if (h->pass_graph) cudaGraphExecDestroy(h->pass_graph);
+    h->pass_graph = nullptr;
+    std::vector<EventPair> none;
+    COF_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    const cof_status st = run_passes(h, cap, none, nseg);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    if (st || e != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return st ? st : fail(h, COF_ERR_CUDA, std::string("pass capture: ") + cudaGetErrorString(e));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&h->pass_graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      h->pass_graph = nullptr;
+      return fail(h, COF_ERR_CUDA, std::string("pass graph: ") + cudaGetErrorString(ei));
+    }
+    h->pass_key = key;
+    h->pass_nseg = *nseg;
+  }
+  *nseg = h->pass_nseg;
+  COF_CUDA(h, cudaGraphLaunch(h->pass_graph, h->stream));
+  return COF_OK;
+}
+
 cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   if (h->jobs.empty()) return fail(h, COF_ERR_STATE, "no input file has been read");
   if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
@@ -557,8 +686,12 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   COF_CUDA(h, h->hits.ensure(cap * 8));
   std::vector<EventPair> evs;
   uint64_t nseg = 0, nhits = 0;
+  // Profiled searches time each launch with events and a streamed upload
+  // waits on per-segment events: both run the passes directly.
+  const bool graph = h->use_graphs && !h->profiling && !h->upload_pending;
   for (;;) {
-    if ((st = run_passes(h, cap, evs, &nseg))) return st;
+    st = graph ? run_passes_graph(h, cap, &nseg) : run_passes(h, cap, evs, &nseg);
+    if (st) return st;
     COF_CUDA(h, cudaMemcpyAsync(&nhits, h->hit_count.p, 8, cudaMemcpyDeviceToHost, h->stream));
     COF_CUDA(h, cudaStreamSynchronize(h->stream));
     if (nhits <= cap) break;
@@ -746,6 +879,8 @@ void cof_close(cof_handle* h) {
   cudaEvent_t evs[7] = {h->timer_a, h->timer_b, h->ev_start, h->ev_found[0], h->ev_found[1], h->ev_used[0],
                         h->ev_used[1]};
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+  if (h->pass_graph) cudaGraphExecDestroy(h->pass_graph);
+  for (auto& kv : h->pinned_free) cudaFreeHost(kv.second);
   delete h;  // frees device buffers
   for (cudaEvent_t ev : evs)
     if (ev) cudaEventDestroy(ev);

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -22,16 +23,34 @@ constexpr uint64_t kSegWords = kSegPositions / 32;
 struct DevBuf {
   void* p = nullptr;
   size_t cap = 0;
-  ~DevBuf() {
-    if (p) cudaFree(p);
+  // With a stream set, allocation and release are stream-ordered
+  // (cudaMallocAsync / cudaFreeAsync on it): no device-wide synchronisation.
+  cudaStream_t st = nullptr;
+  DevBuf() = default;
+  explicit DevBuf(cudaStream_t s) : st(s) {}
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), cap(o.cap), st(o.st) { o.p = nullptr, o.cap = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p, cap = o.cap, st = o.st;
+      o.p = nullptr, o.cap = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) st ? cudaFreeAsync(p, st) : cudaFree(p);
+    p = nullptr;
+    cap = 0;
   }
   cudaError_t ensure(size_t bytes) {
     if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 1);
+    release();
+    cudaError_t e = st ? cudaMallocAsync(&p, bytes ? bytes : 1, st) : cudaMalloc(&p, bytes ? bytes : 1);
     if (e == cudaSuccess) cap = bytes;
+    else p = nullptr;
     return e;
   }
   template <typename T>
@@ -144,6 +163,16 @@ struct cof_handle {
   std::vector<uint64_t> job_byte0;  // row text of job j: [job_byte0[j], job_byte0[j+1]) of host_text
 
   bool profiling = false;
+  // Pinned host buffers for served results, reused across requests.
+  std::mutex pinned_mu;
+  std::multimap<size_t, void*> pinned_free;
+  size_t pinned_pooled = 0;
+  // CUDA graph of the finder / comparer passes of a search, replayed while
+  // everything its launches depend on (pass_key) is unchanged.
+  cudaGraphExec_t pass_graph = nullptr;
+  std::string pass_key;
+  uint64_t pass_nseg = 0;
+  bool use_graphs = true;
   std::map<std::string, KernelStat> stats;
   std::vector<cudaEvent_t> event_pool;  // reused timing events (profiling)
   cudaEvent_t timer_a = nullptr, timer_b = nullptr;
@@ -170,6 +199,23 @@ std::string revcomp(const std::string& s);
 void init_group(PatternGroup& g, const std::string& pattern);
 // Builds and uploads g's comparer tables for its variants `vars` (g.gids
 // already set, one id per variant).  Synchronizes h->stream.
+// Pool of pinned host buffers kept by the handle: acquire returns a buffer of
+// at least `bytes` (its size in *cap), or nullptr; release gives it back.
+// Thread-safe.
+void* pinned_acquire(cof_handle* h, size_t bytes, size_t* cap);
+void pinned_release(cof_handle* h, void* p, size_t cap);
+
+// Host side of a pattern group's comparer tables (built without the GPU).
+struct GroupHost {
+  std::vector<unsigned char> masks;  // popcount comparer (only when the bit-sliced one cannot run)
+  std::vector<uint32_t> prog, pgid;  // bit-sliced lane programs
+};
+// Fills g's host-side fields (slots, chunks, m, ...) and `gh` for `vars`
+// (ids g.gids).  Thread-safe: touches only its arguments.
+void build_group_host(bool force_popc, PatternGroup& g, const std::vector<const Variant*>& vars, GroupHost& gh);
+// Copies `gh` into g's device buffers on `st`; gh must stay alive until the
+// copies are done.
+cof_status upload_group(cof_handle* h, PatternGroup& g, const GroupHost& gh, cudaStream_t st);
 cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars);
 // Lane programs of the bit-sliced comparer for `vars` (ids `gids`), `S` slots,
 // class rows of `row` words; layout in kernels.cuh.

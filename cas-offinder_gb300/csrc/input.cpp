@@ -13,6 +13,9 @@
 #include <map>
 #include <sstream>
 #include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
 
 #include "cof_internal.h"
 
@@ -234,20 +237,41 @@ static RowShape shape_of(const Job& job, const Variant& v, const BulgeRecord& b,
 
 bool build_shapes(Job& job, std::string& err) {
   const size_t L = job.pattern.size();
+  const size_t V = job.variants.size();
   std::string win(L, '\0');
   for (size_t k = 0; k < L; ++k) win[k] = (char)(0x80 + k);
-  for (int s = 0; s < 2; ++s) {
-    job.shapes[s].assign(job.variants.size(), {});
-    for (size_t v = 0; v < job.variants.size(); ++v)
-      for (const BulgeRecord& b : job.variants[v].bulges) {
-        try {
-          job.shapes[s][v].push_back(shape_of(job, job.variants[v], b, s == 1, win));
-        } catch (const std::exception& e) {
-          err = std::string("row construction failed: ") + e.what();
-          return false;
+  for (int s = 0; s < 2; ++s) job.shapes[s].assign(V, {});
+  // Variants are independent: large inputs are split over a few threads.
+  // The first failure in variant order is the one reported.
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t T = V < 4096 ? 1 : std::min<size_t>(std::min<unsigned>(hw, 8u), V / 2048);
+  std::vector<size_t> bad(T, V);
+  std::vector<std::string> why(T);
+  auto work = [&](size_t t) {
+    for (size_t v = V * t / T; v < V * (t + 1) / T; ++v)
+      for (int s = 0; s < 2; ++s)
+        for (const BulgeRecord& b : job.variants[v].bulges) {
+          try {
+            job.shapes[s][v].push_back(shape_of(job, job.variants[v], b, s == 1, win));
+          } catch (const std::exception& e) {
+            bad[t] = v;
+            why[t] = e.what();
+            return;
+          }
         }
-      }
+  };
+  if (T == 1) {
+    work(0);
+  } else {
+    std::vector<std::thread> th;
+    for (size_t t = 0; t < T; ++t) th.emplace_back(work, t);
+    for (std::thread& x : th) x.join();
   }
+  for (size_t t = 0; t < T; ++t)
+    if (bad[t] < V) {
+      err = "row construction failed: " + why[t];
+      return false;
+    }
   return true;
 }
 

@@ -3,24 +3,40 @@
 // The reference runs one input file per process (main.cpp:72-157).  A server
 // keeps the packed genome resident and searches many requests (each one input
 // file) at once.  The genome is walked as a ring of segments; one step
-// processes one segment for every active request.  Requests are admitted at
-// any step boundary -- while others are already running -- as long as the
-// active compare variants fit the variant budget, and each request is complete
-// once it has seen every segment of the ring, wherever it joined.  Active
-// requests with the same padded pattern share one PAM scan and one comparer
-// launch per step, but keep their own variants, ids and thresholds, so every
-// request's rows are exactly those of a search of that input file alone.
+// processes one segment for every request in the current comparer tables.
+// Requests are admitted at any step boundary -- while others are already
+// running -- as long as the admitted compare variants fit the variant budget,
+// and each request is complete once it has seen every segment of the ring,
+// wherever it joined.  Requests with the same padded pattern share one PAM
+// scan and one comparer launch per step, but keep their own variants, ids and
+// thresholds, so every request's rows are exactly those of a search of that
+// input file alone.
 //
-// Threads: cof_server_submit / wait / release may be called from any host
-// thread; all device work runs on the server's worker thread, on the handle's
-// streams.  While a server runs, the handle must not be used for anything else.
+// Threads.  cof_server_submit / wait / release may be called from any host
+// thread (submit parses the input file on the caller's thread).  Three server
+// threads keep host work off the ring:
+//   worker    runs the ring steps on the handle's streams;
+//   builder   compiles the comparer tables of the admitted set (lane
+//             programs, masks) while the worker keeps stepping with the
+//             previous tables; the worker adopts a finished set at a step
+//             boundary, and a request counts steps only from then on;
+//   finisher  sorts and formats a completed request's hits on its own stream
+//             and copies the rows into a pinned host buffer taken from the
+//             handle's pool (returned on cof_server_release), so delivering
+//             GBs of rows touches no fresh pages once the pool is warm.
+// Device buffers that change with the request mix are stream-ordered
+// (cudaMallocAsync / cudaFreeAsync), so no step waits for a device-wide
+// synchronisation.  While a server runs, the handle must not be used for
+// anything else.
 #include <cub/cub.cuh>
 
 #include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <thread>
@@ -42,18 +58,38 @@ struct Request {
   Job job;
   uint32_t nvar = 0;
   double t_submit = 0, t_admit = 0, t_done = 0;
+  // worker-owned until handed to the finisher
   uint64_t steps_seen = 0;
-  uint32_t gid0 = 0;            // first id of its variants in the active tables
-  DevBuf hits;                  // device hit keys with request-local variant ids
+  bool ran = false;  // has completed the ring (or failed): no more hits
+  DevBuf hits;       // device hit keys with request-local variant ids
   uint64_t n_hits = 0;
+  cudaEvent_t last_append = nullptr;
+  // result, published under the server mutex with `done`
   bool done = false;
   cof_status status = COF_OK;
   std::string err;
-  std::string rows;
-  uint64_t n_rows = 0;
+  char* rows = nullptr;  // pinned buffer from the handle's pool (rows_cap bytes)
+  size_t rows_cap = 0;
+  uint64_t rows_len = 0, n_rows = 0;
+  cof_handle* pool = nullptr;  // returns `rows` to the pool on destruction
+  Request() = default;
+  Request(const Request&) = delete;
+  Request& operator=(const Request&) = delete;
+  ~Request() {
+    if (rows) pinned_release(pool, rows, rows_cap);
+  }
 };
 
 using ReqPtr = std::shared_ptr<Request>;
+
+// Comparer tables of one set of requests: ids request by request in set
+// order, groups keyed by padded pattern.
+struct TableSet {
+  std::vector<ReqPtr> reqs;
+  std::vector<uint32_t> gid0;
+  std::vector<PatternGroup> groups;
+  std::vector<GroupHost> host;  // upload source, kept with the set
+};
 
 }  // namespace
 
@@ -62,81 +98,127 @@ struct cof_server {
   uint64_t max_active_variants = 0;
   uint64_t hit_buffer_bytes = 0;
 
-  std::thread worker;
+  std::thread worker, builder, finisher;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work, cv_done, cv_build, cv_finish;
   bool stop = false;
   std::deque<ReqPtr> pending;
-  std::vector<ReqPtr> active;
+  std::vector<ReqPtr> active;  // admitted, not yet through the ring
   std::unordered_map<uint64_t, ReqPtr> tickets;
   uint64_t next_ticket = 1;
   std::string last_error;
   std::atomic<uint64_t> steps{0};
   uint64_t admitted = 0, completed = 0, max_active_seen = 0;
 
+  // builder hand-off (under mu)
+  bool build_wanted = false;
+  std::vector<ReqPtr> build_input;
+  std::unique_ptr<TableSet> built;
+  // finisher hand-off (under mu); the finisher drains until the worker is gone
+  std::deque<ReqPtr> to_finish;
+  bool worker_gone = false;
+
   // worker-only state
-  std::vector<PatternGroup> groups;
-  bool tables_dirty = true;
+  std::unique_ptr<TableSet> tables;
   uint64_t seg_words = kSegWords;  // plane words (32 start positions each) per ring segment
   uint64_t ring = 0, cur = 0;      // ring length in segments, current segment
-  DevBuf step_hits, step_sorted, step_count, step_bounds, step_gid0, sort_tmp, fmt_hits, fmt_bytes, fmt_off, fmt_cnt,
-      fmt_tmp, fmt_text, fmt_vf, fmt_sf, fmt_pool, fmt_small;
+  DevBuf step_hits, step_sorted, step_count, step_bounds, step_gid0, sort_tmp;
+  // finisher-only state
+  cudaStream_t fin_stream = nullptr;
+  DevBuf fmt_hits, fmt_bytes, fmt_off, fmt_cnt, fmt_tmp, fmt_text, fmt_vf, fmt_sf, fmt_pool, fmt_small;
 };
 
 namespace {
 
-// Rebuilds the comparer tables of the active set: ids are assigned request by
-// request in admission order, groups keyed by padded pattern.
-cof_status rebuild_tables(cof_server* s) {
-  cof_handle* h = s->h;
-  s->groups.clear();
-  std::map<std::string, size_t> group_of;
-  std::vector<std::vector<const Variant*>> vars;
-  uint32_t next = 0;
-  for (const ReqPtr& r : s->active) {
-    r->gid0 = next;
-    auto it = group_of.find(r->job.pattern);
-    if (it == group_of.end()) {
-      it = group_of.emplace(r->job.pattern, s->groups.size()).first;
-      s->groups.emplace_back();
-      init_group(s->groups.back(), r->job.pattern);
-      vars.emplace_back();
+// Builder thread: compiles the tables of the latest admitted set.
+void builder_main(cof_server* s) {
+  for (;;) {
+    std::vector<ReqPtr> reqs;
+    {
+      std::unique_lock<std::mutex> lock(s->mu);
+      s->cv_build.wait(lock, [&] { return s->stop || s->build_wanted; });
+      if (s->stop) return;
+      reqs = s->build_input;
+      s->build_wanted = false;
     }
-    for (size_t v = 0; v < r->job.variants.size(); ++v) {
-      s->groups[it->second].gids.push_back(next + (uint32_t)v);
-      vars[it->second].push_back(&r->job.variants[v]);
+    auto ts = std::make_unique<TableSet>();
+    ts->reqs = reqs;
+    std::map<std::string, size_t> group_of;
+    std::vector<std::vector<const Variant*>> vars;
+    uint32_t next = 0;
+    for (const ReqPtr& r : reqs) {
+      ts->gid0.push_back(next);
+      auto it = group_of.find(r->job.pattern);
+      if (it == group_of.end()) {
+        it = group_of.emplace(r->job.pattern, ts->groups.size()).first;
+        ts->groups.emplace_back();
+        init_group(ts->groups.back(), r->job.pattern);
+        vars.emplace_back();
+      }
+      for (size_t v = 0; v < r->job.variants.size(); ++v) {
+        ts->groups[it->second].gids.push_back(next + (uint32_t)v);
+        vars[it->second].push_back(&r->job.variants[v]);
+      }
+      next += r->nvar;
     }
-    next += r->nvar;
+    ts->host.resize(ts->groups.size());
+    for (size_t g = 0; g < ts->groups.size(); ++g)
+      build_group_host(s->h->force_popc, ts->groups[g], vars[g], ts->host[g]);
+    {
+      std::lock_guard<std::mutex> lock(s->mu);
+      s->built = std::move(ts);
+    }
+    s->cv_work.notify_all();
   }
-  for (size_t g = 0; g < s->groups.size(); ++g) {
-    cof_status st = build_group_tables(h, s->groups[g], vars[g]);
-    if (st) return st;
-  }
-  s->tables_dirty = false;
-  return COF_OK;
 }
 
-// One ring step: segment s->cur for every active group.  Appends each hit to
-// its request, with the request-local variant id.
+// Asks the builder for tables of the current admitted set (under mu).
+void want_build(cof_server* s) {
+  s->build_input = s->active;
+  s->build_wanted = true;
+  s->cv_build.notify_one();
+}
+
+// True when the front pending request fits the variant budget (under mu).
+bool admissible(const cof_server* s) {
+  if (s->pending.empty()) return false;
+  if (s->active.empty()) return true;
+  uint64_t used = 0;
+  for (const ReqPtr& r : s->active) used += r->nvar;
+  return used + s->pending.front()->nvar <= s->max_active_variants;
+}
+
+// True when the current tables hold a request still walking the ring.
+bool tables_live(const cof_server* s) {
+  if (!s->tables) return false;
+  for (const ReqPtr& r : s->tables->reqs)
+    if (!r->ran) return true;
+  return false;
+}
+
+// One ring step: segment s->cur for every group of the current tables.
+// Appends each hit to its request (request-local variant id) unless the
+// request has already completed the ring.
 cof_status run_step(cof_server* s) {
   cof_handle* h = s->h;
+  TableSet& T = *s->tables;
   const GenomeView gv = h->genome.view();
   const uint64_t n = h->genome.n;
   uint64_t cap = std::max<uint64_t>(s->step_hits.cap / 8, 1u << 16);
   COF_CUDA(h, s->step_hits.ensure(cap * 8));
   COF_CUDA(h, s->step_count.ensure(8));
-  COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(s->groups.size(), 1) * 4));
+  COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(T.groups.size(), 1) * 4));
   COF_CUDA(h, h->queue[0].ensure(2 * kSegPositions * 4));
   COF_CUDA(h, h->queue[1].ensure(2 * kSegPositions * 4));
   uint64_t count = 0;
   for (;;) {
-    COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<size_t>(s->groups.size(), 1) * 4, h->stream));
+    COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<size_t>(T.groups.size(), 1) * 4, h->stream));
     COF_CUDA(h, cudaMemsetAsync(s->step_count.p, 0, 8, h->stream));
     COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
     COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
     uint64_t pass = 0;
-    for (size_t gi = 0; gi < s->groups.size(); ++gi) {
-      const PatternGroup& g = s->groups[gi];
+    for (size_t gi = 0; gi < T.groups.size(); ++gi) {
+      const PatternGroup& g = T.groups[gi];
       const uint64_t npos = n >= g.L ? n - g.L + 1 : 0;
       const uint64_t words = (npos + 31) / 32;
       const uint64_t w0 = s->cur * s->seg_words, w1 = std::min(words, w0 + s->seg_words);
@@ -173,7 +255,7 @@ cof_status run_step(cof_server* s) {
   if (count) {
     // Sort the step's hits: each request's ids are one consecutive range, so
     // its hits become one run, appended to the request's own device buffer.
-    const size_t A = s->active.size();
+    const size_t A = T.reqs.size();
     COF_CUDA(h, s->step_sorted.ensure(count * 8));
     COF_CUDA(h, s->step_bounds.ensure((A + 1) * 8));
     COF_CUDA(h, s->step_gid0.ensure((A + 1) * 4));
@@ -184,9 +266,7 @@ cof_status run_step(cof_server* s) {
     tmp = s->sort_tmp.cap;
     COF_CUDA(h, cub::DeviceRadixSort::SortKeys(s->sort_tmp.p, tmp, s->step_hits.as<uint64_t>(),
                                                s->step_sorted.as<uint64_t>(), (int64_t)count, 0, 64, h->stream));
-    std::vector<uint32_t> gid0(A);
-    for (size_t a = 0; a < A; ++a) gid0[a] = s->active[a]->gid0;
-    COF_CUDA(h, cudaMemcpyAsync(s->step_gid0.p, gid0.data(), A * 4, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(s->step_gid0.p, T.gid0.data(), A * 4, cudaMemcpyHostToDevice, h->stream));
     launch_run_starts(s->step_sorted.as<uint64_t>(), count, s->step_gid0.as<uint32_t>(), (uint32_t)A,
                       s->step_bounds.as<uint64_t>(), h->stream);
     std::vector<uint64_t> start(A + 1);
@@ -194,20 +274,18 @@ cof_status run_step(cof_server* s) {
     COF_CUDA(h, cudaStreamSynchronize(h->stream));
     start[A] = count;
     for (size_t a = 0; a < A; ++a) {
-      Request& r = *s->active[a];
+      Request& r = *T.reqs[a];
       const uint64_t k = start[a + 1] - start[a];
-      if (!k) continue;
+      if (!k || r.ran) continue;
       if ((r.n_hits + k) * 8 > r.hits.cap) {  // grow by doubling, keeping the hits so far
-        DevBuf bigger;
+        DevBuf bigger(h->stream);
         COF_CUDA(h, bigger.ensure(std::max<uint64_t>((r.n_hits + k) * 8, 2 * r.hits.cap)));
         if (r.n_hits)
           COF_CUDA(h, cudaMemcpyAsync(bigger.p, r.hits.p, r.n_hits * 8, cudaMemcpyDeviceToDevice, h->stream));
-        COF_CUDA(h, cudaStreamSynchronize(h->stream));
-        std::swap(r.hits.p, bigger.p);
-        std::swap(r.hits.cap, bigger.cap);
+        r.hits = std::move(bigger);  // the old buffer is freed in stream order
       }
-      launch_rebase_hits(s->step_sorted.as<uint64_t>() + start[a], k, r.gid0, r.hits.as<uint64_t>() + r.n_hits,
-                         h->stream);
+      launch_rebase_hits(s->step_sorted.as<uint64_t>() + start[a], k, T.gid0[a],
+                         r.hits.as<uint64_t>() + r.n_hits, h->stream);
       r.n_hits += k;
     }
     COF_CUDA(h, cudaGetLastError());
@@ -216,65 +294,92 @@ cof_status run_step(cof_server* s) {
   return COF_OK;
 }
 
-// Sorts a finished request's hits and formats its rows on the device.
-cof_status format_request(cof_server* s, Request& r) {
+// CUDA check for the finisher: reports through `err`, not the handle.
+#define COF_FIN(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);                         \
+      return e_ == cudaErrorMemoryAllocation ? COF_ERR_NOMEM : COF_ERR_CUDA;            \
+    }                                                                                   \
+  } while (0)
+
+// Sorts a finished request's hits and formats its rows on the finisher's
+// stream, into a pinned host buffer from the handle's pool.
+cof_status format_request(cof_server* s, Request& r, std::string& err) {
   cof_handle* h = s->h;
+  cudaStream_t st = s->fin_stream;
+  if (r.last_append) COF_FIN(cudaStreamWaitEvent(st, r.last_append, 0));
   const uint64_t nh = r.n_hits;
   if (!nh) return COF_OK;
   std::vector<VariantFmt> vf;
   std::vector<ShapeFmt> sf;
   std::string pool;
   append_format_tables(r.job, vf, sf, pool);
-  COF_CUDA(h, s->fmt_vf.ensure(vf.size() * sizeof(VariantFmt)));
-  COF_CUDA(h, s->fmt_sf.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
-  COF_CUDA(h, s->fmt_pool.ensure(std::max<size_t>(pool.size(), 1)));
-  COF_CUDA(h, s->fmt_hits.ensure(nh * 8));
-  COF_CUDA(h, s->fmt_bytes.ensure(nh * 8));
-  COF_CUDA(h, s->fmt_off.ensure(nh * 8));
-  COF_CUDA(h, s->fmt_cnt.ensure(nh * 4));
-  COF_CUDA(h, s->fmt_small.ensure(16));
-  COF_CUDA(h, cudaMemcpyAsync(s->fmt_vf.p, vf.data(), vf.size() * sizeof(VariantFmt), cudaMemcpyHostToDevice, h->stream));
+  COF_FIN(s->fmt_vf.ensure(vf.size() * sizeof(VariantFmt)));
+  COF_FIN(s->fmt_sf.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
+  COF_FIN(s->fmt_pool.ensure(std::max<size_t>(pool.size(), 1)));
+  COF_FIN(s->fmt_hits.ensure(nh * 8));
+  COF_FIN(s->fmt_bytes.ensure(nh * 8));
+  COF_FIN(s->fmt_off.ensure(nh * 8));
+  COF_FIN(s->fmt_cnt.ensure(nh * 4));
+  COF_FIN(s->fmt_small.ensure(16));
+  COF_FIN(cudaMemcpyAsync(s->fmt_vf.p, vf.data(), vf.size() * sizeof(VariantFmt), cudaMemcpyHostToDevice, st));
   if (!sf.empty())
-    COF_CUDA(h, cudaMemcpyAsync(s->fmt_sf.p, sf.data(), sf.size() * sizeof(ShapeFmt), cudaMemcpyHostToDevice, h->stream));
-  if (!pool.empty())
-    COF_CUDA(h, cudaMemcpyAsync(s->fmt_pool.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, h->stream));
+    COF_FIN(cudaMemcpyAsync(s->fmt_sf.p, sf.data(), sf.size() * sizeof(ShapeFmt), cudaMemcpyHostToDevice, st));
+  if (!pool.empty()) COF_FIN(cudaMemcpyAsync(s->fmt_pool.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, st));
   size_t t0 = 0, t1 = 0, t2 = 0;
-  COF_CUDA(h, cub::DeviceRadixSort::SortKeys(nullptr, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
-                                             (int64_t)nh, 0, 64, h->stream));
-  COF_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
-                                            (int64_t)nh, h->stream));
-  COF_CUDA(h, cub::DeviceReduce::Sum(nullptr, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(), (int64_t)nh,
-                                     h->stream));
-  COF_CUDA(h, s->fmt_tmp.ensure(std::max(t0, std::max(t1, t2))));
+  COF_FIN(cub::DeviceRadixSort::SortKeys(nullptr, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(), (int64_t)nh,
+                                         0, 64, st));
+  COF_FIN(cub::DeviceScan::ExclusiveSum(nullptr, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
+                                        (int64_t)nh, st));
+  COF_FIN(cub::DeviceReduce::Sum(nullptr, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(), (int64_t)nh,
+                                 st));
+  COF_FIN(s->fmt_tmp.ensure(std::max(t0, std::max(t1, t2))));
   t0 = s->fmt_tmp.cap;
-  COF_CUDA(h, cub::DeviceRadixSort::SortKeys(s->fmt_tmp.p, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
-                                             (int64_t)nh, 0, 64, h->stream));
+  COF_FIN(cub::DeviceRadixSort::SortKeys(s->fmt_tmp.p, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
+                                         (int64_t)nh, 0, 64, st));
+  r.hits.st = st;  // freed in order after the sort on this stream
+  r.hits.release();
   const GenomeView gv = h->genome.view();
   FormatTables ft{s->fmt_vf.as<VariantFmt>(), s->fmt_sf.as<ShapeFmt>(), s->fmt_pool.as<char>()};
   launch_row_lengths(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_bytes.as<uint64_t>(), s->fmt_cnt.as<uint32_t>(),
-                     h->stream);
+                     st);
   t1 = s->fmt_tmp.cap;
-  COF_CUDA(h, cub::DeviceScan::ExclusiveSum(s->fmt_tmp.p, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
-                                            (int64_t)nh, h->stream));
+  COF_FIN(cub::DeviceScan::ExclusiveSum(s->fmt_tmp.p, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
+                                        (int64_t)nh, st));
   t2 = s->fmt_tmp.cap;
-  COF_CUDA(h, cub::DeviceReduce::Sum(s->fmt_tmp.p, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(),
-                                     (int64_t)nh, h->stream));
+  COF_FIN(cub::DeviceReduce::Sum(s->fmt_tmp.p, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(),
+                                 (int64_t)nh, st));
   uint64_t last[3] = {0, 0, 0};
-  COF_CUDA(h, cudaMemcpyAsync(&last[0], s->fmt_off.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, h->stream));
-  COF_CUDA(h, cudaMemcpyAsync(&last[1], s->fmt_bytes.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, h->stream));
-  COF_CUDA(h, cudaMemcpyAsync(&last[2], s->fmt_small.p, 8, cudaMemcpyDeviceToHost, h->stream));
-  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  COF_FIN(cudaMemcpyAsync(&last[0], s->fmt_off.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, st));
+  COF_FIN(cudaMemcpyAsync(&last[1], s->fmt_bytes.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, st));
+  COF_FIN(cudaMemcpyAsync(&last[2], s->fmt_small.p, 8, cudaMemcpyDeviceToHost, st));
+  COF_FIN(cudaStreamSynchronize(st));
   const uint64_t bytes = last[0] + last[1];
-  COF_CUDA(h, s->fmt_text.ensure(bytes + 1));
+  COF_FIN(s->fmt_text.ensure(bytes + 1));
   launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), bytes, s->fmt_text.as<char>(),
-                    h->stream);
-  COF_CUDA(h, cudaGetLastError());
-  r.rows.resize(bytes);
-  COF_CUDA(h, cudaMemcpyAsync(&r.rows[0], s->fmt_text.p, bytes, cudaMemcpyDeviceToHost, h->stream));
-  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+                    st);
+  COF_FIN(cudaGetLastError());
+  // Rows go straight to a pinned host buffer from the handle's pool.
+  size_t cap = 0;
+  char* dst = (char*)pinned_acquire(h, bytes + 1, &cap);
+  if (!dst) {
+    err = "no pinned host memory for " + std::to_string(bytes) + " bytes of rows";
+    return COF_ERR_NOMEM;
+  }
+  r.pool = h;
+  r.rows = dst;
+  r.rows_cap = cap;
+  COF_FIN(cudaMemcpyAsync(dst, s->fmt_text.p, bytes, cudaMemcpyDeviceToHost, st));
+  COF_FIN(cudaStreamSynchronize(st));
+  dst[bytes] = 0;
+  r.rows_len = bytes;
   r.n_rows = last[2];
   return COF_OK;
 }
+
+#undef COF_FIN
 
 void finish(cof_server* s, const ReqPtr& r, cof_status st, const std::string& err) {
   std::lock_guard<std::mutex> lock(s->mu);
@@ -286,53 +391,103 @@ void finish(cof_server* s, const ReqPtr& r, cof_status st, const std::string& er
   s->cv_done.notify_all();
 }
 
+// Finisher thread: formats completed requests in completion order.
+void finisher_main(cof_server* s) {
+  cudaSetDevice(s->h->device);
+  for (;;) {
+    ReqPtr r;
+    {
+      std::unique_lock<std::mutex> lock(s->mu);
+      s->cv_finish.wait(lock, [&] { return s->worker_gone || !s->to_finish.empty(); });
+      if (s->to_finish.empty()) return;  // the worker has stopped and everything is drained
+      r = s->to_finish.front();
+      s->to_finish.pop_front();
+    }
+    std::string err = r->err;
+    const cof_status st = r->status ? r->status : format_request(s, *r, err);
+    r->hits.st = s->fin_stream;
+    r->hits.release();
+    if (r->last_append) {
+      cudaEventDestroy(r->last_append);
+      r->last_append = nullptr;
+    }
+    finish(s, r, st, st ? err : std::string());
+  }
+}
+
 void worker_main(cof_server* s) {
   cof_handle* h = s->h;
   cudaSetDevice(h->device);
   const uint64_t words = (h->genome.n + 31) / 32;
   s->ring = std::max<uint64_t>(1, (words + s->seg_words - 1) / s->seg_words);
   for (;;) {
+    std::unique_ptr<TableSet> fresh;
     {
       std::unique_lock<std::mutex> lock(s->mu);
-      s->cv_work.wait(lock, [&] { return s->stop || !s->pending.empty() || !s->active.empty(); });
+      s->cv_work.wait(lock, [&] { return s->stop || admissible(s) || s->built || tables_live(s); });
       if (s->stop) break;
       // Admit waiting requests while the variant budget allows (always at
       // least one, so a request larger than the budget still runs alone).
-      uint64_t used = 0;
-      for (const ReqPtr& r : s->active) used += r->nvar;
-      while (!s->pending.empty()) {
-        const ReqPtr& r = s->pending.front();
-        if (!s->active.empty() && used + r->nvar > s->max_active_variants) break;
-        used += r->nvar;
-        r->t_admit = now_s();
-        r->steps_seen = 0;
-        s->active.push_back(r);
+      bool changed = false;
+      while (admissible(s)) {
+        const ReqPtr r = s->pending.front();
         s->pending.pop_front();
+        r->t_admit = now_s();
+        s->active.push_back(r);
         ++s->admitted;
-        s->tables_dirty = true;
+        changed = true;
       }
       s->max_active_seen = std::max<uint64_t>(s->max_active_seen, s->active.size());
+      if (changed) want_build(s);
+      fresh = std::move(s->built);
     }
-    cof_status st = COF_OK;
-    if (s->tables_dirty) st = rebuild_tables(s);
-    if (!st) st = run_step(s);
-    std::vector<ReqPtr> finished;
-    for (const ReqPtr& r : s->active)
-      if (st || ++r->steps_seen >= s->ring) finished.push_back(r);
-    for (const ReqPtr& r : finished) {
-      cof_status fs = st ? st : format_request(s, *r);
-      if (r->hits.p) {  // the request's device hits are no longer needed
-        cudaFree(r->hits.p);
-        r->hits.p = nullptr;
-        r->hits.cap = 0;
+    if (fresh) {
+      // Adopt the new tables at this step boundary: uploads on the worker's
+      // stream, ahead of the step's kernels; the old set's device buffers are
+      // freed in stream order.
+      cof_status st = COF_OK;
+      for (size_t g = 0; g < fresh->groups.size() && !st; ++g) {
+        PatternGroup& pg = fresh->groups[g];
+        pg.vmask.st = pg.bs_prog.st = pg.bs_pgid.st = h->stream;
+        st = upload_group(h, pg, fresh->host[g], h->stream);
       }
-      finish(s, r, fs, fs ? h->err : std::string());
+      s->tables = std::move(fresh);
+      if (st) {
+        std::lock_guard<std::mutex> lock(s->mu);
+        for (const ReqPtr& r : s->tables->reqs)
+          if (!r->ran) {
+            r->ran = true;
+            r->status = st;
+            r->err = h->err;
+            s->to_finish.push_back(r);
+          }
+        s->active.erase(std::remove_if(s->active.begin(), s->active.end(), [](const ReqPtr& r) { return r->ran; }),
+                        s->active.end());
+        s->cv_finish.notify_one();
+        continue;
+      }
     }
+    if (!tables_live(s)) continue;
+    const cof_status st = run_step(s);
+    std::vector<ReqPtr> finished;
+    for (const ReqPtr& r : s->tables->reqs)
+      if (!r->ran && (st || ++r->steps_seen >= s->ring)) finished.push_back(r);
     if (!finished.empty()) {
       std::lock_guard<std::mutex> lock(s->mu);
-      s->active.erase(std::remove_if(s->active.begin(), s->active.end(), [](const ReqPtr& r) { return r->done; }),
+      for (const ReqPtr& r : finished) {
+        r->ran = true;
+        if (st) {
+          r->status = st;
+          r->err = h->err;
+        } else if (cudaEventCreateWithFlags(&r->last_append, cudaEventDisableTiming) == cudaSuccess) {
+          cudaEventRecord(r->last_append, h->stream);
+        }
+        s->to_finish.push_back(r);
+      }
+      s->active.erase(std::remove_if(s->active.begin(), s->active.end(), [](const ReqPtr& r) { return r->ran; }),
                       s->active.end());
-      s->tables_dirty = true;
+      want_build(s);
+      s->cv_finish.notify_one();
     }
     s->cur = (s->cur + 1) % s->ring;
   }
@@ -340,19 +495,24 @@ void worker_main(cof_server* s) {
   std::vector<ReqPtr> left;
   {
     std::lock_guard<std::mutex> lock(s->mu);
-    left.insert(left.end(), s->active.begin(), s->active.end());
+    for (const ReqPtr& r : s->active)
+      if (!r->ran) left.push_back(r);
     left.insert(left.end(), s->pending.begin(), s->pending.end());
     s->active.clear();
     s->pending.clear();
   }
   for (const ReqPtr& r : left) {
-    if (r->hits.p) {
-      cudaFree(r->hits.p);
-      r->hits.p = nullptr;
-      r->hits.cap = 0;
-    }
+    r->ran = true;
+    r->hits.release();
     finish(s, r, COF_ERR_STATE, "server stopped");
   }
+  s->tables.reset();
+  cudaStreamSynchronize(h->stream);
+  {
+    std::lock_guard<std::mutex> lock(s->mu);
+    s->worker_gone = true;
+  }
+  s->cv_finish.notify_all();
 }
 
 }  // namespace
@@ -364,13 +524,28 @@ cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_
   if (!h || !out) return COF_ERR_ARG;
   *out = nullptr;
   if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
+  cudaSetDevice(h->device);
   cof_server* s = new cof_server();
   s->h = h;
   s->max_active_variants = max_active_variants ? max_active_variants : (1u << 17);
   if (s->max_active_variants >= (1u << 20)) s->max_active_variants = (1u << 20) - 1;
   s->hit_buffer_bytes = hit_buffer_bytes ? hit_buffer_bytes : (8ull << 30);
   if (segment_positions) s->seg_words = std::min<uint64_t>(kSegWords, std::max<uint64_t>(1, segment_positions / 32));
+  cudaError_t e = cudaStreamCreateWithFlags(&s->fin_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(h, COF_ERR_CUDA, std::string("server stream: ") + cudaGetErrorString(e));
+  }
+  // Buffers that grow with the request mix are stream-ordered on the stream
+  // that uses them (a plain cudaFree would wait for the whole device).
+  for (DevBuf* b : {&s->step_hits, &s->step_sorted, &s->step_count, &s->step_bounds, &s->step_gid0, &s->sort_tmp})
+    b->st = h->stream;
+  for (DevBuf* b : {&s->fmt_hits, &s->fmt_bytes, &s->fmt_off, &s->fmt_cnt, &s->fmt_tmp, &s->fmt_text, &s->fmt_vf,
+                    &s->fmt_sf, &s->fmt_pool, &s->fmt_small})
+    b->st = s->fin_stream;
   s->worker = std::thread(worker_main, s);
+  s->builder = std::thread(builder_main, s);
+  s->finisher = std::thread(finisher_main, s);
   *out = s;
   return COF_OK;
 }
@@ -378,6 +553,7 @@ cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_
 cof_status cof_server_submit(cof_server* s, const char* text, size_t len, uint64_t* ticket) {
   if (!s || (!text && len) || !ticket) return COF_ERR_ARG;
   auto r = std::make_shared<Request>();
+  r->hits.st = s->h->stream;
   std::string err;
   if (!parse_job(text ? text : "", len, r->job, err) || !build_shapes(r->job, err)) {
     std::lock_guard<std::mutex> lock(s->mu);
@@ -402,7 +578,7 @@ cof_status cof_server_submit(cof_server* s, const char* text, size_t len, uint64
     *ticket = r->ticket;
     s->tickets[r->ticket] = r;
     if (r->nvar == 0) {  // nothing to search: done at once
-      r->done = true;
+      r->done = r->ran = true;
       r->t_admit = r->t_done = r->t_submit;
       ++s->completed;
       s->cv_done.notify_all();
@@ -424,8 +600,8 @@ cof_status cof_server_wait(cof_server* s, uint64_t ticket, int timeout_ms, const
   auto ready = [&] { return r->done; };
   if (timeout_ms < 0) s->cv_done.wait(lock, ready);
   else if (!s->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), ready)) return COF_ERR_TIMEOUT;
-  if (rows) *rows = r->rows.data();
-  if (rows_len) *rows_len = r->rows.size();
+  if (rows) *rows = r->rows ? r->rows : "";
+  if (rows_len) *rows_len = r->rows_len;
   if (latency_ms) *latency_ms = (r->t_done - r->t_submit) * 1e3;
   if (r->status) s->last_error = r->err;
   return r->status;
@@ -466,9 +642,19 @@ void cof_server_stop(cof_server* s) {
     s->stop = true;
   }
   s->cv_work.notify_all();
+  s->cv_build.notify_all();
   if (s->worker.joinable()) s->worker.join();
+  if (s->builder.joinable()) s->builder.join();
+  // The finisher drains what the worker handed over, then exits.
+  if (s->finisher.joinable()) s->finisher.join();
   cudaSetDevice(s->h->device);
+  s->built.reset();
+  cudaStreamSynchronize(s->fin_stream);
+  cudaStreamSynchronize(s->h->stream);
+  cudaStream_t fs = s->fin_stream;
   delete s;
+  cudaStreamSynchronize(fs);
+  cudaStreamDestroy(fs);
 }
 
 }  // extern "C"

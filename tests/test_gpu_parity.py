@@ -72,10 +72,13 @@ def test_abi_search_matches_golden_and_repeats(P, built, tmp_path):
     with P.CasOFFinder(0) as eng:
         eng.read_input_path(inp)
         eng.load_genome_file(eng.chrdir)
-        first = eng.search()
-        second = eng.search()
+        first = eng.search()   # passes captured as a CUDA graph
+        second = eng.search()  # graph replayed
+        eng.set_profiling(True)
+        third = eng.search()   # profiled: passes launched directly
+        eng.set_profiling(False)
         assert P.HEADER.encode() + first == want
-        assert first == second
+        assert first == second == third
         nh, nr = eng.last_hit_count()
         assert nr == len(cases.rows_of(want))
 
@@ -127,6 +130,27 @@ def test_search_planes_streams_like_resident_search(P, built):
         assert got == want
         pinned[:] = 0  # the genome is resident: the host planes are no longer read
         assert eng.search() == want
+
+
+def test_hit_buffer_growth_with_captured_passes(P, built):
+    """More hits than the first hit buffer holds: the passes are captured
+    again for the larger buffer, and the rows equal the directly launched
+    (profiled) search's."""
+    seqs = [P.synth_record(5, 0, 15_000_000, gc=0.41)]
+    text, starts = P.reference_text(seqs)
+    hi, lo, ot, ep, eb = P.pack_text(text)
+    inp = "synthetic\n" + "N" * 20 + "NGG\n" + "ACGTACGTACGTACGTACGT" + "NNN 20\n"
+    with P.CasOFFinder(0) as eng:
+        eng.readInputFile(inp)
+        eng.load_genome_planes(hi, lo, ot, len(text), ep, eb, ["chr1"], starts)
+        a = eng.search()
+        nh, nr = eng.last_hit_count()
+        assert nh > (1 << 20)
+        eng.set_profiling(True)
+        b = eng.search()
+        eng.set_profiling(False)
+        assert a == b
+        assert eng.search() == a
 
 
 def read_fasta(path):
