@@ -75,6 +75,26 @@ def batched_jobs(seed=5, n=1024, genome_path="synthetic"):
     return texts
 
 
+PAM_SETS = [("NNGRRT", 21, False), ("NNNNGMTT", 24, False), ("NNAGAAW", 20, False), ("TTTV", 23, True)]
+
+
+def pam_variety_jobs(seed=7, per_set=256, genome_path="synthetic"):
+    """PAM and orientation variety: four input files of 256 random guides each
+    (NNGRRT with 21-nt spacers, NNNNGMTT with 24, NNAGAAW with 20, and the 5'
+    PAM TTTV with 23), max mismatches 4, DNA bulge 1, RNA bulge 1."""
+    import random
+    rng = random.Random(seed)
+    texts = []
+    for pam, spacer, pam5 in PAM_SETS:
+        pattern = (pam + "N" * spacer) if pam5 else ("N" * spacer + pam)
+        lines = [genome_path, pattern + " 1 1"]
+        for _ in range(per_set):
+            g = "".join(rng.choice("ACGT") for _ in range(spacer))
+            lines.append((("N" * len(pam) + g) if pam5 else (g + "N" * len(pam))) + " 4")
+        texts.append("\n".join(lines) + "\n")
+    return texts
+
+
 SERVED_PAMS = [("NGG", 20, False), ("NRG", 20, False), ("NNGRRT", 21, False), ("TTTV", 23, True)]
 
 
@@ -346,6 +366,9 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=2)
     ap.add_argument("--plain-sample", type=int, default=32, help="plain searches timed for the comparison")
     ap.add_argument("--no-served", action="store_true", help="skip the served request stream")
+    ap.add_argument("--no-pam-variety", action="store_true", help="skip the four 256-guide PAM sets")
+    ap.add_argument("--comparer", default="auto", choices=["auto", "popcount", "bitsliced"],
+                    help="comparer kernel for the plain search (default: bit-sliced where it fits)")
     ap.add_argument("--served-requests", type=int, default=12)
     ap.add_argument("--served-rates", type=float, nargs="+", default=[2.0, 20.0, 200.0])
     args = ap.parse_args()
@@ -375,6 +398,7 @@ def main():
     gen_s = time.time() - t0
 
     eng = P.CasOFFinder(local)
+    eng.set_comparer({"auto": 0, "popcount": 1, "bitsliced": 2}[args.comparer])
     eng.readInputFile(input_text("synthetic", guides))
     info = eng.input_info()
     eng.load_genome_planes(hi, lo, ot, n, None, None, names, starts)
@@ -463,6 +487,7 @@ def main():
     launches = args.steps * int(stats["finder"]["launches"] + stats["comparer"]["launches"] +
                                 3 * stats["format"]["launches"])
     batched = None if args.no_batched else run_batched(P, eng, lens, rates, args)
+    pam_variety = None if args.no_pam_variety else run_pam_variety(P, eng, lens, rates, args)
     served = None if args.no_served else run_served(P, eng, lens, args)
     if rank == 0:
         line = {
@@ -485,6 +510,7 @@ def main():
                                 else None, "basis": "0.375 B per genome position (3 bit planes)"},
             "kernel_ms_per_step": {k: v["ms"] for k, v in stats.items()},
             "batched": batched,
+            "pam_variety": pam_variety,
             "served": served,
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
@@ -534,6 +560,50 @@ def run_batched(P, eng, lens, rates, args):
         "steps": args.batched_steps, "variants": info["variants"], "hits": hits, "rows": rows,
         "plain_value": gbp / (plain_ms / 1e3), "plain_ms_per_input": plain_ms, "plain_sample_inputs": k,
         "speedup_vs_plain": (plain_ms * len(texts)) / ms,
+        "comparer_roofline": {"achieved": achieved, "peak": peak, "unit": "G base-comparisons/s",
+                              "frac": achieved / peak if peak else None},
+    }
+
+
+def run_pam_variety(P, eng, lens, rates, args):
+    """The four 256-guide PAM sets in one batched search of the resident
+    genome, against the four sets searched one after another."""
+    texts = pam_variety_jobs()
+    eng.batch_clear()
+    for t in texts:
+        eng.batch_add_input(t)
+    info = eng.input_info()
+    eng.search_view()  # warm-up
+    eng.synchronize()
+    eng.reset_stats()
+    eng.set_profiling(True)
+    eng.search_view()
+    eng.set_profiling(False)
+    cmp = eng.kernel_stats("comparer")
+    eng.timer_start()
+    for _ in range(args.batched_steps):
+        eng.search_view()
+    ms = eng.timer_stop() / args.batched_steps
+    hits, rows = eng.last_hit_count()
+    gbp = sum(lens) / 1e9
+    seq_ms = 0.0
+    for t in texts:
+        eng.readInputFile(t)
+        eng.search_view()
+        eng.synchronize()
+        eng.timer_start()
+        eng.search_view()
+        seq_ms += eng.timer_stop()
+    guides = 256 * len(texts)
+    achieved = cmp["units"] / (cmp["ms"] * 1e-3) / 1e9 if cmp["ms"] else 0.0
+    peak = rates["lop3"] * 16 / 1e9
+    return {
+        "workload": "4 input files x 256 guides: NNGRRT/21-nt, NNNNGMTT/24-nt, NNAGAAW/20-nt, 5'-TTTV/23-nt spacers, "
+                    "mm 4, DNA bulge 1, RNA bulge 1, on the same 3.1 Gbp genome",
+        "value": guides * gbp / (ms / 1e3), "unit": "guide-Gbp/s", "ms_per_step": ms, "steps": args.batched_steps,
+        "variants": info["variants"], "hits": hits, "rows": rows,
+        "sequential_value": guides * gbp / (seq_ms / 1e3), "sequential_ms": seq_ms,
+        "speedup_vs_sequential": seq_ms / ms,
         "comparer_roofline": {"achieved": achieved, "peak": peak, "unit": "G base-comparisons/s",
                               "frac": achieved / peak if peak else None},
     }

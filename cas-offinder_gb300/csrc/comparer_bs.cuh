@@ -238,7 +238,12 @@ __device__ __forceinline__ void build_pair(const RawWindow<NK>& ra, const RawWin
     const unsigned k = i * 32 + lane;
     if (k < (unsigned)ROW) {
       // One LOP3 of (h, l, o) each; truth tables over (0xF0, 0xCC, 0xAA).
-#define COF_ROW(r, LUT) pt[(r) * ROW + k] = make_uint2(lop3<LUT>(h0, l0, o0), lop3<LUT>(h1, l1, o1))
+      // Row r holds position k at column (k + r) mod ROW: classes rotate across
+      // the banks, so lanes reading different classes at nearby positions
+      // conflict less.
+#define COF_ROW(r, LUT)                                                           \
+  pt[(r) * ROW + (k + (r) < (unsigned)ROW ? k + (r) : k + (r) - ROW)] =           \
+      make_uint2(lop3<LUT>(h0, l0, o0), lop3<LUT>(h1, l1, o1))
       COF_ROW(1, 0xFE);  // T: h | l | o (mismatch unless T)
       COF_ROW(2, 0xFB);  // C: h | ~l | o
       COF_ROW(3, 0xEF);  // A: ~h | l | o

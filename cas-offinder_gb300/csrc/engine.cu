@@ -207,7 +207,7 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
     int c = 0;
     for (size_t k = 0; k < key.size() && c < S; ++k) {
       const uint32_t cl = bs_class_of((unsigned char)key[k]);
-      if (cl) sl[c++] = (uint16_t)((cl * row + (uint32_t)k) * 8);
+      if (cl) sl[c++] = (uint16_t)((cl * row + ((uint32_t)k + cl) % row) * 8);
     }
     std::sort(sl, sl + c);
     cnt[i] = (uint8_t)c;

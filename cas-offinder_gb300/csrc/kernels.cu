@@ -52,9 +52,27 @@ __device__ __forceinline__ uint32_t bits_at(uint32_t w0, uint32_t w1, uint32_t w
 constexpr int kFinderThreads = 128;
 constexpr int kFinderStage = 512;  // staged entries per warp; denser warps store directly
 
+// Device form of a FinderPattern: per pattern position that can mismatch its
+// window offset and the five class masks (T, C, A, G, other byte) as
+// all-ones / all-zeros words, so the scan does no decoding.
+struct FinderMasks {
+  uint32_t L, nf, nr;
+  uint8_t fk[kMaxL], rk[kMaxL];
+  uint32_t fm[kMaxL][5], rm[kMaxL][5];
+};
+
+// 32 consecutive bits starting at bit k of the window words x0|x1|x2 (NK = 1:
+// k < 32 and x2 unused).
+template <int NK>
+__device__ __forceinline__ uint32_t window_bits(uint32_t x0, uint32_t x1, uint32_t x2, unsigned k) {
+  if (NK == 1) return __funnelshift_r(x0, x1, k);
+  return bits_at(x0, x1, x2, k);
+}
+
+template <int NK>
 __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
-    uint64_t w_begin, uint64_t w_end, const __grid_constant__ FinderPattern pat, uint32_t* __restrict__ queue,
+    uint64_t w_begin, uint64_t w_end, const __grid_constant__ FinderMasks pat, uint32_t* __restrict__ queue,
     uint32_t* __restrict__ qcount) {
   __shared__ uint32_t stage[kFinderThreads / 32][kFinderStage];
   const unsigned lane = threadIdx.x & 31;
@@ -64,21 +82,22 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     const uint64_t w = wb + lane;
     uint32_t fwd = 0, rev = 0;
     if (w < w_end) {
-      const uint32_t h0 = hi[w], h1 = hi[w + 1], h2 = hi[w + 2];
-      const uint32_t l0 = lo[w], l1 = lo[w + 1], l2 = lo[w + 2];
-      const uint32_t o0 = ot[w], o1 = ot[w + 1], o2 = ot[w + 2];
+      // A window of L <= 32 starting in word w ends in word w + 1.
+      const uint32_t h0 = hi[w], h1 = hi[w + 1], h2 = NK == 1 ? 0u : hi[w + 2];
+      const uint32_t l0 = lo[w], l1 = lo[w + 1], l2 = NK == 1 ? 0u : lo[w + 2];
+      const uint32_t o0 = ot[w], o1 = ot[w + 1], o2 = NK == 1 ? 0u : ot[w + 2];
       uint32_t badf = 0, badr = 0;
       for (uint32_t j = 0; j < pat.nf; ++j) {
         const unsigned k = pat.fk[j];
-        const uint32_t m = pat.fm[j];
-        badf |= mismatch_word(bits_at(h0, h1, h2, k), bits_at(l0, l1, l2, k), bits_at(o0, o1, o2, k), 0u - (m & 1),
-                              0u - ((m >> 1) & 1), 0u - ((m >> 2) & 1), 0u - ((m >> 3) & 1), 0u - ((m >> 4) & 1));
+        badf |= mismatch_word(window_bits<NK>(h0, h1, h2, k), window_bits<NK>(l0, l1, l2, k),
+                              window_bits<NK>(o0, o1, o2, k), pat.fm[j][0], pat.fm[j][1], pat.fm[j][2],
+                              pat.fm[j][3], pat.fm[j][4]);
       }
       for (uint32_t j = 0; j < pat.nr; ++j) {
         const unsigned k = pat.rk[j];
-        const uint32_t m = pat.rm[j];
-        badr |= mismatch_word(bits_at(h0, h1, h2, k), bits_at(l0, l1, l2, k), bits_at(o0, o1, o2, k), 0u - (m & 1),
-                              0u - ((m >> 1) & 1), 0u - ((m >> 2) & 1), 0u - ((m >> 3) & 1), 0u - ((m >> 4) & 1));
+        badr |= mismatch_word(window_bits<NK>(h0, h1, h2, k), window_bits<NK>(l0, l1, l2, k),
+                              window_bits<NK>(o0, o1, o2, k), pat.rm[j][0], pat.rm[j][1], pat.rm[j][2],
+                              pat.rm[j][3], pat.rm[j][4]);
       }
       fwd = ~badf;
       rev = ~badr;
@@ -87,7 +106,7 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
         const uint32_t s0 = o0 & l0 & ~h0, s1 = o1 & l1 & ~h1, s2 = o2 & l2 & ~h2;
         if (s0 | s1 | s2) {
           uint32_t near = 0;
-          for (unsigned k = 0; k < pat.L; ++k) near |= bits_at(s0, s1, s2, k);
+          for (unsigned k = 0; k < pat.L; ++k) near |= window_bits<NK>(s0, s1, s2, k);
           fwd &= ~near;
           rev &= ~near;
         }
@@ -105,24 +124,28 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(qcount, total);
     base = __shfl_sync(kFull, base, 0);
-    const bool staged = total <= (uint32_t)kFinderStage;  // warp-uniform
-    uint32_t* dst = staged ? my : queue + base;
-    uint32_t at = incl - cnt;
     const uint32_t rel = (uint32_t)((w - w_begin) << 5);
-    while (fwd) {
-      const unsigned b = __ffs(fwd) - 1;
-      fwd &= fwd - 1;
-      dst[at++] = (rel + b) << 1;
-    }
-    while (rev) {
-      const unsigned b = __ffs(rev) - 1;
-      rev &= rev - 1;
-      dst[at++] = ((rel + b) << 1) | 1u;
-    }
-    if (staged) {
+    // Candidates in descending bit order (queue order does not matter).
+    auto emit = [&](uint32_t* dst) {
+      uint32_t at = incl - cnt;
+      while (fwd) {
+        const unsigned b = 31 - __clz(fwd);
+        fwd ^= 1u << b;
+        dst[at++] = (rel + b) << 1;
+      }
+      while (rev) {
+        const unsigned b = 31 - __clz(rev);
+        rev ^= 1u << b;
+        dst[at++] = ((rel + b) << 1) | 1u;
+      }
+    };
+    if (total <= (uint32_t)kFinderStage) {  // warp-uniform
+      emit(my);
       __syncwarp();
       for (uint32_t i = lane; i < total; i += 32) queue[base + i] = my[i];
       __syncwarp();
+    } else {
+      emit(queue + base);
     }
   }
 }
@@ -133,8 +156,24 @@ void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const 
   uint64_t blocks = (words + kFinderThreads - 1) / kFinderThreads;
   if (blocks > 65535ull * 8) blocks = 65535ull * 8;
   if (blocks == 0) return;
-  finder_kernel<<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, pat, queue,
-                                                                  qcount);
+  FinderMasks fm{};
+  fm.L = pat.L;
+  fm.nf = pat.nf;
+  fm.nr = pat.nr;
+  for (uint32_t j = 0; j < pat.nf; ++j) {
+    fm.fk[j] = pat.fk[j];
+    for (int c = 0; c < 5; ++c) fm.fm[j][c] = 0u - ((pat.fm[j] >> c) & 1u);
+  }
+  for (uint32_t j = 0; j < pat.nr; ++j) {
+    fm.rk[j] = pat.rk[j];
+    for (int c = 0; c < 5; ++c) fm.rm[j][c] = 0u - ((pat.rm[j] >> c) & 1u);
+  }
+  if (pat.L <= 32)
+    finder_kernel<1><<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, fm, queue,
+                                                                     qcount);
+  else
+    finder_kernel<2><<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, fm, queue,
+                                                                     qcount);
 }
 
 // ---------------------------------------------------------------- comparer
@@ -356,9 +395,24 @@ __device__ __forceinline__ void write_row(const GenomeView& g, const FormatTable
   const char* comp = ft.pool + vf.comp_off;
   // Oriented window with mismatches lower-cased (indicate_mismatches,
   // cas-offinder.cpp:299-317: byte += 32).
+  // The window's plane bits, 64 positions from h.pos (three words per plane
+  // cover any L <= 64 at any bit offset).
+  const uint64_t w0 = h.pos >> 5;
+  const unsigned b0 = (unsigned)(h.pos & 31);
+  auto bits64 = [&](const uint32_t* plane) {
+    const uint64_t lo64 = ((uint64_t)plane[w0 + 1] << 32) | plane[w0];
+    return b0 ? (lo64 >> b0) | ((uint64_t)plane[w0 + 2] << (64 - b0)) : lo64;
+  };
+  const uint64_t H = bits64(g.hi), Lo = bits64(g.lo), O = bits64(g.ot);
   unsigned char win[kMaxL];
   for (uint32_t k = 0; k < L; ++k) {
-    unsigned char c = h.strand ? dev_complement(genome_byte(g, h.pos + (L - 1 - k))) : genome_byte(g, h.pos + k);
+    const uint32_t q = h.strand ? L - 1 - k : k;  // window position of oriented position k
+    const unsigned hb = (unsigned)(H >> q) & 1u, lb = (unsigned)(Lo >> q) & 1u;
+    unsigned char c;
+    if (!((O >> q) & 1u)) c = (unsigned char)"TCAG"[hb * 2 + lb];
+    else if (!hb) c = lb ? ';' : 'N';
+    else c = genome_byte(g, h.pos + q);  // another byte: from the exception list
+    if (h.strand) c = dev_complement(c);
     if (dev_mismatch((unsigned char)comp[k], c)) c = (unsigned char)(c + 32);
     win[k] = c;
   }

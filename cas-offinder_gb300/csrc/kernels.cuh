@@ -114,7 +114,8 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
 //   word 0           bits 0-7: 2^NB - 1 - min(threshold, 2^NB - 1), NB =
 //                    bit_width(slots); bit 8: the first variant is real
 //   words 1..slots/2 the first variant's slots: u16 shared-memory byte
-//                    offsets (class * row + k) * 8, two per word, 0 = padding
+//                    offsets (class * row + (k + class) % row) * 8, two per
+//                    word, 0 = padding
 //   (these 1 + slots/2 words lane-minor: word w of lane l at w * 32 + l)
 //   then the m - 1 steps (padded to an even count with zero words) as pairs,
 //                    step s of lane l at (1 + slots/2) * 32 + ((s / 2) * 32

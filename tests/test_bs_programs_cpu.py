@@ -67,7 +67,7 @@ def replay(P, text):
     variants = r["variants"]
     assert sorted(seen) == list(range(len(variants))), "every variant exactly once"
     for gid, (key, thr) in enumerate(variants):
-        want = frozenset((CLASS[ch] * row + k) * 8 for k, ch in enumerate(key) if ch in CLASS)
+        want = frozenset((CLASS[ch] * row + (k + CLASS[ch]) % row) * 8 for k, ch in enumerate(key) if ch in CLASS)
         slots, k = seen[gid]
         assert slots == want, f"variant {gid} ({key}) counted over the wrong slots"
         assert len(want) <= S
