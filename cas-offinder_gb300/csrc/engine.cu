@@ -42,9 +42,25 @@ std::mutex g_open_mu;
 std::string g_open_err;
 
 // Uploads a packed genome into `dg` (copies are stream-ordered on h->stream).
-// With `streamed` the plane copies go to h->stream3 one segment at a time
-// (events in h->upload_ev) and the call returns before they finish: the host
-// planes must stay valid until the search that waits on them is done.
+// Queues the copies of streamed-upload chunks [issued, upto) on h->stream2,
+// the finders' stream: each finder follows the copies queued before it.
+cof_status issue_upload(cof_handle* h, size_t upto) {
+  upto = std::min(upto, h->upload_pending);
+  DevGenome& dg = h->genome;
+  const uint64_t W = h->upload_words;
+  for (; h->upload_issued < upto; ++h->upload_issued) {
+    const size_t c = h->upload_issued;
+    const uint64_t w0 = c * kSegWords, nw = std::min<uint64_t>(W - w0, kSegWords);
+    uint32_t* dst[3] = {dg.hi.as<uint32_t>(), dg.lo.as<uint32_t>(), dg.ot.as<uint32_t>()};
+    for (int p = 0; p < 3; ++p)
+      COF_CUDA(h, cudaMemcpyAsync(dst[p] + w0, h->upload_src[p] + w0, nw * 4, cudaMemcpyHostToDevice, h->stream2));
+  }
+  return COF_OK;
+}
+
+// With `streamed` the plane copies are left to the search (run_passes queues
+// them on the finders' stream two segments ahead of the scan): the host
+// planes must stay valid until that search is done.
 cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
                          uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
                          const std::vector<std::string>& names, const std::vector<uint64_t>& starts,
@@ -67,22 +83,12 @@ cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const
     COF_CUDA(h, cudaMemcpyAsync(dg.lo.p, lo, W * 4, cudaMemcpyHostToDevice, h->stream));
     COF_CUDA(h, cudaMemcpyAsync(dg.ot.p, ot, W * 4, cudaMemcpyHostToDevice, h->stream));
   } else {
-    // The copy stream starts after everything already queued on the handle.
-    COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
-    COF_CUDA(h, cudaStreamWaitEvent(h->stream3, h->ev_start, 0));
     const size_t chunks = (size_t)((W + kSegWords - 1) / kSegWords);
-    while (h->upload_ev.size() < chunks) {
-      cudaEvent_t e = nullptr;
-      COF_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-      h->upload_ev.push_back(e);
-    }
-    for (size_t c = 0; c < chunks; ++c) {
-      const uint64_t w0 = c * kSegWords, nw = std::min<uint64_t>(W - w0, kSegWords);
-      COF_CUDA(h, cudaMemcpyAsync(dg.hi.as<uint32_t>() + w0, hi + w0, nw * 4, cudaMemcpyHostToDevice, h->stream3));
-      COF_CUDA(h, cudaMemcpyAsync(dg.lo.as<uint32_t>() + w0, lo + w0, nw * 4, cudaMemcpyHostToDevice, h->stream3));
-      COF_CUDA(h, cudaMemcpyAsync(dg.ot.as<uint32_t>() + w0, ot + w0, nw * 4, cudaMemcpyHostToDevice, h->stream3));
-      COF_CUDA(h, cudaEventRecord(h->upload_ev[c], h->stream3));
-    }
+    h->upload_src[0] = hi;
+    h->upload_src[1] = lo;
+    h->upload_src[2] = ot;
+    h->upload_words = W;
+    h->upload_issued = 0;
     h->upload_pending = chunks;
   }
   COF_CUDA(h, dg.exc_pos.ensure(n_exc * 8));
@@ -556,7 +562,7 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
   COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
   COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
-  uint64_t pass = 0, waited_seg = ~0ull;
+  uint64_t pass = 0;
   for (uint64_t s = 0; s < nseg; ++s) {
     for (size_t gi = 0; gi < G; ++gi) {
       const PatternGroup& g = h->groups[gi];
@@ -568,11 +574,11 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       uint32_t* qc = h->qcounts.as<uint32_t>() + s * G + gi;
       uint32_t* q = h->queue[b].as<uint32_t>();
       if (pass >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
-      if (h->upload_pending && waited_seg != s) {
-        // Segment s reads plane words up to w1 + 2: chunks s and s + 1.
-        const size_t c = std::min<size_t>((size_t)s + 1, h->upload_pending - 1);
-        COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->upload_ev[c], 0));
-        waited_seg = s;
+      if (h->upload_pending) {
+        // Segment s reads plane words up to w1 + 2 (chunks s and s + 1); its
+        // finder follows the copies up to chunk s + 2 on the same stream.
+        cof_status st = issue_upload(h, (size_t)s + 3);
+        if (st) return st;
       }
       cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32, h->stream2);
       if (st) return st;
@@ -594,14 +600,17 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       ++pass;
     }
   }
+  // Row formatting reads the planes: the rest of a streamed upload goes
+  // before the join.
+  if (h->upload_pending) {
+    cof_status st = issue_upload(h, h->upload_pending);
+    if (st) return st;
+  }
   // Join stream2 into the main stream (it may end with a finder whose
-  // comparer was skipped; normally the last comparer already waited on it).
+  // comparer was skipped, or with copies; normally the last comparer already
+  // waited on it).
   COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream2));
   COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->ev_start, 0));
-  if (h->upload_pending) {
-    // Row formatting reads the planes: the whole upload must be in.
-    COF_CUDA(h, cudaStreamWaitEvent(h->stream, h->upload_ev[h->upload_pending - 1], 0));
-  }
   COF_CUDA(h, cudaGetLastError());
   return COF_OK;
 }
@@ -617,6 +626,10 @@ std::string pass_graph_key(const cof_handle* h, uint64_t cap) {
     put64((uint64_t)p);
   put64(h->genome.n);
   put64(h->qcounts.cap);
+  // A streamed upload's copies are part of the graph.
+  put64(h->upload_pending);
+  for (const uint32_t* p : h->upload_src) put64(h->upload_pending ? (uint64_t)p : 0);
+  put64(h->upload_pending ? h->upload_words : 0);
   put64(cap);
   put64((uint64_t)h->sm_count);
   for (const PatternGroup& g : h->groups) {
@@ -645,6 +658,7 @@ cof_status run_passes_graph(cof_handle* h, uint64_t cap, uint64_t* nseg) {
     if (h->pass_graph) cudaGraphExecDestroy(h->pass_graph);
     h->pass_graph = nullptr;
     std::vector<EventPair> none;
+    h->upload_issued = 0;  // a streamed upload is captured whole
     COF_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     const cof_status st = run_passes(h, cap, none, nseg);
     cudaGraph_t graph = nullptr;
@@ -664,6 +678,7 @@ cof_status run_passes_graph(cof_handle* h, uint64_t cap, uint64_t* nseg) {
   }
   *nseg = h->pass_nseg;
   COF_CUDA(h, cudaGraphLaunch(h->pass_graph, h->stream));
+  h->upload_issued = h->upload_pending;  // the graph copies every chunk
   return COF_OK;
 }
 
@@ -686,9 +701,9 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   COF_CUDA(h, h->hits.ensure(cap * 8));
   std::vector<EventPair> evs;
   uint64_t nseg = 0, nhits = 0;
-  // Profiled searches time each launch with events and a streamed upload
-  // waits on per-segment events: both run the passes directly.
-  const bool graph = h->use_graphs && !h->profiling && !h->upload_pending;
+  // Profiled searches time each launch with events, and copies from pageable
+  // host memory cannot be graph nodes: both run the passes directly.
+  const bool graph = h->use_graphs && !h->profiling && (!h->upload_pending || h->upload_pinned);
   for (;;) {
     st = graph ? run_passes_graph(h, cap, &nseg) : run_passes(h, cap, evs, &nseg);
     if (st) return st;
@@ -853,7 +868,6 @@ cof_status cof_open(int device, cof_handle** out) {
   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device);
   e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream3, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming);
   for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
     e = cudaEventCreateWithFlags(&h->ev_found[i], cudaEventDisableTiming);
@@ -873,9 +887,7 @@ void cof_close(cof_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
-  if (h->stream3) cudaStreamSynchronize(h->stream3);
-  cudaStream_t s = h->stream, s2 = h->stream2, s3 = h->stream3;
-  for (cudaEvent_t e : h->upload_ev) cudaEventDestroy(e);
+  cudaStream_t s = h->stream, s2 = h->stream2;
   cudaEvent_t evs[7] = {h->timer_a, h->timer_b, h->ev_start, h->ev_found[0], h->ev_found[1], h->ev_used[0],
                         h->ev_used[1]};
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
@@ -886,7 +898,6 @@ void cof_close(cof_handle* h) {
     if (ev) cudaEventDestroy(ev);
   if (s) cudaStreamDestroy(s);
   if (s2) cudaStreamDestroy(s2);
-  if (s3) cudaStreamDestroy(s3);
 }
 
 const char* cof_last_error(const cof_handle* h) { return h ? h->err.c_str() : "null handle"; }
@@ -1040,11 +1051,20 @@ cof_status cof_search_planes(cof_handle* h, const uint32_t* hi, const uint32_t* 
     st.push_back(starts[i]);
   }
   cof_status r = upload_genome(h, h->genome, hi, lo, ot, n, exc_pos, exc_byte, n_exc, nm, st, true);
+  h->upload_pinned = true;
+  for (const uint32_t* p : {hi, lo, ot}) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess || a.type != cudaMemoryTypeHost) h->upload_pinned = false;
+  }
+  cudaGetLastError();  // an unregistered pointer is not an error here
   if (r == COF_OK) r = do_search(h, rows, rows_len);
-  // The host planes are not read after this call returns.
+  // The whole genome stays resident (also when the search stopped early) and
+  // the host planes are not read after this call returns.
   if (h->upload_pending) {
-    const cudaError_t e = cudaStreamSynchronize(h->stream3);
-    h->upload_pending = 0;
+    const cof_status ri = issue_upload(h, h->upload_pending);
+    const cudaError_t e = cudaStreamSynchronize(h->stream2);
+    h->upload_pending = h->upload_issued = 0;
+    if (ri && r == COF_OK) return ri;
     if (e != cudaSuccess && r == COF_OK) return fail(h, COF_ERR_CUDA, cudaGetErrorString(e));
   }
   return r;

@@ -135,11 +135,13 @@ struct cof_handle {
   cudaStream_t stream = nullptr;   // comparer, formatting, copies
   cudaStream_t stream2 = nullptr;  // finder passes, one segment ahead of the comparer
   cudaEvent_t ev_start = nullptr, ev_found[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
-  // Streamed upload (cof_search_planes): plane copies per segment on stream3,
-  // upload_ev[c] recorded after chunk c; finders wait for their chunks.
-  cudaStream_t stream3 = nullptr;
-  std::vector<cudaEvent_t> upload_ev;
+  // Streamed upload (cof_search_planes): plane copies per segment, queued on
+  // stream2 ahead of the finders that read them.
   size_t upload_pending = 0;  // chunks of the current streamed upload (0: none)
+  size_t upload_issued = 0;   // chunks whose copies are queued so far
+  bool upload_pinned = false;  // the host planes are page-locked (copies can be graph nodes)
+  const uint32_t* upload_src[3] = {nullptr, nullptr, nullptr};  // host planes (valid during the call)
+  uint64_t upload_words = 0;
   std::string err;
 
   // The batch: one or more parsed input files ("jobs").  Variant ids are
