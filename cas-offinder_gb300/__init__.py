@@ -32,7 +32,7 @@ HEADER = ("##Generated by Cas-OFFinder 3.0.0\n"
 # Every entry point include/cof.h declares (checked by the CPU tests).
 EXPORTS = [
     "cof_open", "cof_close", "cof_last_error", "cof_open_error", "cof_read_input", "cof_genome_path",
-    "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes", "cof_search_planes",
+    "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes", "cof_search_planes", "cof_search_stream",
     "cof_genome_info", "cof_search", "cof_last_hit_count", "cof_set_summary", "cof_summary_text",
     "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
     "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
@@ -40,8 +40,11 @@ EXPORTS = [
     "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
     "cof_server_start", "cof_server_submit", "cof_server_wait", "cof_server_release", "cof_server_stats",
     "cof_server_last_error", "cof_server_stop",
-    "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table", "cofx_bs_programs",
+    "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table", "cofx_bs_programs", "cofx_genome_text",
 ]
+
+# cof_write_fn: int (*)(void* ctx, const char* data, size_t len)
+WRITE_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t)
 
 _lib = None
 
@@ -87,6 +90,7 @@ def lib():
                                             c.POINTER(c.c_uint64), u32, c.POINTER(c.c_void_p), c.POINTER(sz)]),
             "cof_genome_info": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u32)]),
             "cof_search": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
+            "cof_search_stream": (c.c_int, [vp, WRITE_FN, vp, c.POINTER(u64)]),
             "cof_last_hit_count": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u64)]),
             "cof_set_summary": (c.c_int, [vp, c.c_int]),
             "cof_summary_text": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
@@ -124,6 +128,7 @@ def lib():
                                           c.POINTER(c.c_double)]),
             "cofx_mismatch_table": (None, [vp]),
             "cofx_bs_programs": (c.c_int, [c.c_char_p, sz, vp, vp, sz, vp, sz, vp, sz]),
+            "cofx_genome_text": (c.c_int, [c.c_char_p, vp, u64, c.POINTER(u64)]),
             "cofx_synth_record": (u64, [u64, u32, u64, c.c_double, c.c_double, u32, c.c_double, u32, u32, vp]),
         }
         for name, (res, args) in sig.items():
@@ -149,6 +154,18 @@ def mismatch_table():
     out = np.zeros(65536, np.uint8)
     lib().cofx_mismatch_table(_ptr(out))
     return out.reshape(256, 256)
+
+
+def genome_text(path):
+    """The reference's genome string for a FASTA / 2BIT file as the engine's
+    loaders read it (host only), or None when the file is neither."""
+    n = ctypes.c_uint64()
+    p = os.fsencode(path)
+    if lib().cofx_genome_text(p, None, 0, ctypes.byref(n)) != 0:
+        return None
+    out = ctypes.create_string_buffer(max(n.value, 1))
+    lib().cofx_genome_text(p, out, n.value, ctypes.byref(n))
+    return out.raw[:n.value]
 
 
 def bs_programs(text):
@@ -292,6 +309,21 @@ class CasOFFinder:
             self._h, _ptr(hi), _ptr(lo), _ptr(ot), n, _ptr(exc_pos), _ptr(exc_byte),
             0 if exc_pos is None else exc_pos.size, arr_n, arr_s, len(names), ctypes.byref(p), ctypes.byref(m)))
         return p.value, m.value
+
+    def search_stream(self, write):
+        """cof_search_stream: write(bytes) is called with the rows, chunk by
+        chunk, in order; returns the total bytes written.  A write that
+        raises stops the search (COF_ERR_IO)."""
+        def cb(ctx, data, n):
+            try:
+                write(_bytes_at(data, n))
+                return 0
+            except Exception:
+                return 1
+        fn = WRITE_FN(cb)
+        total = ctypes.c_uint64()
+        self._check(self._L.cof_search_stream(self._h, fn, None, ctypes.byref(total)))
+        return total.value
 
     def search_view(self):
         """(address, length) of the rows in the engine's pinned buffer, without a copy."""

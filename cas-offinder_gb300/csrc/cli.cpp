@@ -131,16 +131,15 @@ int main(int argc, char** argv) {
       failed = 1;
       return;
     }
-    const char* rows = nullptr;
-    size_t len = 0;
-    if ((st = cof_search(h, &rows, &len)) != COF_OK) {
-      std::cerr << "Search failed on " << path << ": " << cof_last_error(h) << std::endl;
+    // Rows are written as they come off the GPU, chunk by chunk.
+    cof_write_fn writer = [](void* ctx, const char* data, size_t n) -> int {
+      return write_all((FILE*)ctx, data, n) ? 0 : 1;
+    };
+    if ((st = cof_search_stream(h, writer, out, nullptr)) != COF_OK) {
+      if (st == COF_ERR_IO) std::cerr << "Write error on " << pos[2] << std::endl;
+      else std::cerr << "Search failed on " << path << ": " << cof_last_error(h) << std::endl;
       failed = 1;
       return;
-    }
-    if (!write_all(out, rows, len)) {
-      std::cerr << "Write error on " << pos[2] << std::endl;
-      failed = 1;
     }
     fflush(out);
     if (!summary_path.empty()) {

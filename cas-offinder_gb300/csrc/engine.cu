@@ -656,6 +656,8 @@ cof_status run_passes_graph(cof_handle* h, uint64_t cap, uint64_t* nseg) {
   const std::string key = pass_graph_key(h, cap);
   if (!h->pass_graph || key != h->pass_key) {
     if (h->pass_graph) cudaGraphExecDestroy(h->pass_graph);
+  for (cudaEvent_t e : h->stream_ev)
+    if (e) cudaEventDestroy(e);
     h->pass_graph = nullptr;
     std::vector<EventPair> none;
     h->upload_issued = 0;  // a streamed upload is captured whole
@@ -682,7 +684,14 @@ cof_status run_passes_graph(cof_handle* h, uint64_t cap, uint64_t* nseg) {
   return COF_OK;
 }
 
-cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
+// Where cof_search_stream sends the rows.
+struct StreamSink {
+  cof_write_fn fn;
+  void* ctx;
+  uint64_t written;
+};
+
+cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamSink* sink = nullptr) {
   if (h->jobs.empty()) return fail(h, COF_ERR_STATE, "no input file has been read");
   if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
   cof_status st = upload_jobs(h);
@@ -784,15 +793,58 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
   if (bytes > (nrows + 1) * (uint64_t)(1 << 20))
     return fail(h, COF_ERR_DEVICE, "row text of " + std::to_string(bytes) + " bytes for " + std::to_string(nrows) +
                                        " rows (" + std::to_string(nhits) + " hits)");
-  COF_CUDA(h, h->text.ensure(bytes + 1));
-  launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), bytes,
-                    h->text.as<char>(), h->stream);
-  if ((st = record_stop(h, evs, h->stream))) return st;
-  COF_CUDA(h, cudaGetLastError());
-  COF_CUDA(h, h->host_text.ensure(bytes + 1));
-  COF_CUDA(h, cudaMemcpyAsync(h->host_text.p, h->text.p, bytes, cudaMemcpyDeviceToHost, h->stream));
-  COF_CUDA(h, cudaStreamSynchronize(h->stream));
-  ((char*)h->host_text.p)[bytes] = 0;
+  if (!sink) {
+    COF_CUDA(h, h->text.ensure(bytes + 1));
+    launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), 0, bytes,
+                      h->text.as<char>(), h->stream);
+    if ((st = record_stop(h, evs, h->stream))) return st;
+    COF_CUDA(h, cudaGetLastError());
+    COF_CUDA(h, h->host_text.ensure(bytes + 1));
+    COF_CUDA(h, cudaMemcpyAsync(h->host_text.p, h->text.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    COF_CUDA(h, cudaStreamSynchronize(h->stream));
+    ((char*)h->host_text.p)[bytes] = 0;
+  } else {
+    // Rows in chunks of kBatch hits: chunk k+1 is formatted and copied while
+    // the caller writes chunk k (two device and two pinned host buffers).
+    if ((st = record_stop(h, evs, h->stream))) return st;
+    constexpr uint64_t kBatch = 1ull << 20;
+    const uint64_t nb = (nhits + kBatch - 1) / kBatch;
+    std::vector<uint64_t> cut(nb + 1, 0);
+    for (uint64_t k = 0; k < nb; ++k)
+      COF_CUDA(h, cudaMemcpyAsync(&cut[k], h->row_offsets.as<uint64_t>() + k * kBatch, 8, cudaMemcpyDeviceToHost,
+                                  h->stream));
+    COF_CUDA(h, cudaStreamSynchronize(h->stream));
+    cut[nb] = bytes;
+    uint64_t most = 0;
+    for (uint64_t k = 0; k < nb; ++k) most = std::max(most, cut[k + 1] - cut[k]);
+    for (int b = 0; b < 2; ++b) {
+      COF_CUDA(h, h->stream_dev[b].ensure(most + 16));
+      COF_CUDA(h, h->stream_host[b].ensure(most + 16));
+      if (!h->stream_ev[b]) COF_CUDA(h, cudaEventCreateWithFlags(&h->stream_ev[b], cudaEventDisableTiming));
+    }
+    for (uint64_t k = 0; k <= nb; ++k) {
+      if (k < nb) {
+        const int b = (int)(k & 1);
+        const uint64_t i0 = k * kBatch, i1 = std::min(nhits, i0 + kBatch);
+        launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>() + i0, i1 - i0, h->row_offsets.as<uint64_t>() + i0,
+                          cut[k], cut[k + 1], h->stream_dev[b].as<char>(), h->stream);
+        COF_CUDA(h, cudaGetLastError());
+        COF_CUDA(h, cudaMemcpyAsync(h->stream_host[b].p, h->stream_dev[b].p, cut[k + 1] - cut[k],
+                                    cudaMemcpyDeviceToHost, h->stream));
+        COF_CUDA(h, cudaEventRecord(h->stream_ev[b], h->stream));
+      }
+      if (k >= 1) {
+        const int pb = (int)((k - 1) & 1);
+        const uint64_t len = cut[k] - cut[k - 1];
+        COF_CUDA(h, cudaEventSynchronize(h->stream_ev[pb]));
+        if (len && sink->fn(sink->ctx, (const char*)h->stream_host[pb].p, len) != 0) {
+          cudaStreamSynchronize(h->stream);
+          return fail(h, COF_ERR_IO, "the row writer failed after " + std::to_string(sink->written) + " bytes");
+        }
+        sink->written += len;
+      }
+    }
+  }
   collect(h, evs);
   h->last_rows = nrows;
   if (h->summary_on) {
@@ -810,8 +862,10 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len) {
       }
     }
   }
-  *rows = (const char*)h->host_text.p;
-  *rows_len = bytes;
+  if (!sink) {
+    *rows = (const char*)h->host_text.p;
+    *rows_len = bytes;
+  }
   return COF_OK;
 }
 
@@ -892,6 +946,8 @@ void cof_close(cof_handle* h) {
                         h->ev_used[1]};
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
   if (h->pass_graph) cudaGraphExecDestroy(h->pass_graph);
+  for (cudaEvent_t e : h->stream_ev)
+    if (e) cudaEventDestroy(e);
   for (auto& kv : h->pinned_free) cudaFreeHost(kv.second);
   delete h;  // frees device buffers
   for (cudaEvent_t ev : evs)
@@ -1033,6 +1089,18 @@ cof_status cof_search(cof_handle* h, const char** rows, size_t* rows_len) {
   h->err.clear();
   cudaSetDevice(h->device);
   return do_search(h, rows, rows_len);
+}
+
+cof_status cof_search_stream(cof_handle* h, cof_write_fn write, void* ctx, uint64_t* bytes_written) {
+  if (!h || !write) return COF_ERR_ARG;
+  h->err.clear();
+  cudaSetDevice(h->device);
+  StreamSink sink{write, ctx, 0};
+  const char* rows = "";
+  size_t len = 0;
+  const cof_status st = do_search(h, &rows, &len, &sink);
+  if (bytes_written) *bytes_written = sink.written;
+  return st;
 }
 
 cof_status cof_search_planes(cof_handle* h, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot, uint64_t n,

@@ -158,6 +158,9 @@ struct cof_handle {
   DevBuf queue[2], qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small,
       job_start, job_bytes;
   HostPinned host_text;
+  DevBuf stream_dev[2];  // cof_search_stream: row chunks on the device / in pinned memory
+  HostPinned stream_host[2];
+  cudaEvent_t stream_ev[2] = {nullptr, nullptr};
   std::string summary_text;
   std::vector<std::map<std::string, unsigned long long>> summaries;  // per job
   bool summary_on = false;

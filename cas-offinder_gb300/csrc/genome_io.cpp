@@ -6,15 +6,20 @@
 //                lines give record names (text after '>'); sequence lines are
 //                upper-cased (soft mask dropped) and appended; a ';' separates
 //                consecutive records; symlinks are resolved with readlink.
-//   load_twobit  read_twobit (read_twobit.cpp:44-131): host-order magic
-//                0x1A412743, version 0 only, the index offsets are ignored and
-//                records are read back to back, N blocks become 'N', mask
-//                blocks are skipped, ';' between records.
+//   load_twobit  read_twobit (read_twobit.cpp:44-131): magic 0x1A412743,
+//                N blocks become 'N', mask blocks are skipped, ';' between
+//                records.  Beyond the reference (which reads host-order
+//                version 0 files and ignores the index offsets, reading the
+//                records back to back): each record is read at its index
+//                offset (the same bytes for files laid out back to back),
+//                version 1 files (64-bit offsets) and files of the other byte
+//                order are accepted.
 // 2BIT data is converted code for code (its T,C,A,G = 0..3 is the plane code),
 // without expanding to one byte per base.
 #include <unistd.h>
 
 #include <climits>
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <thread>
@@ -218,23 +223,43 @@ void mark_other(PackedGenome& g, uint64_t p, uint64_t cnt, bool sep) {
 int load_twobit(const std::string& path, PackedGenome& g) {
   FILE* f = fopen(resolve(path).c_str(), "rb");
   if (!f) return 1;
-  auto u32 = [&](uint32_t& v) { return fread(&v, 4, 1, f) == 1; };
-  uint32_t magic = 0, version = 1, count = 0, reserved = 0;
-  if (!u32(magic) || magic != 0x1A412743u || !u32(version) || version != 0) {
+  bool swap = false;  // file written on a machine of the other byte order
+  auto u32 = [&](uint32_t& v) {
+    if (fread(&v, 4, 1, f) != 1) return false;
+    if (swap) v = __builtin_bswap32(v);
+    return true;
+  };
+  uint32_t magic = 0, version = 2, count = 0, reserved = 0;
+  if (!u32(magic) || (magic != 0x1A412743u && magic != 0x4327411Au)) {
+    fclose(f);
+    return 1;
+  }
+  swap = magic == 0x4327411Au;
+  if (!u32(version) || version > 1) {
     fclose(f);
     return 1;
   }
   g = PackedGenome();
   u32(count);
   u32(reserved);
+  // Index: name and file offset of each record (32-bit in version 0, 64-bit
+  // in version 1).  The reference reads records back to back after the index
+  // and knows version 0 only; honouring the offsets reads the same bytes for
+  // files laid out that way and the right ones for any other layout.
+  std::vector<uint64_t> offset(count, 0);
   for (uint32_t i = 0; i < count; ++i) {
     unsigned char nlen = 0;
     char name[256];
     if (fread(&nlen, 1, 1, f) != 1) nlen = 0;
     const size_t got = fread(name, 1, nlen, f);
     g.names.emplace_back(name, got);
-    uint32_t off;
-    u32(off);
+    uint32_t lo32 = 0, hi32 = 0;
+    u32(lo32);
+    if (version == 1) {
+      u32(hi32);
+      if (swap) std::swap(lo32, hi32);
+    }
+    offset[i] = ((uint64_t)hi32 << 32) | lo32;
   }
   struct Rec {
     uint32_t len;
@@ -246,6 +271,7 @@ int load_twobit(const std::string& path, PackedGenome& g) {
   uint64_t total = 0;
   for (uint32_t r = 0; r < count; ++r) {
     Rec& R = recs[r];
+    if (offset[r] && fseeko(f, (off_t)offset[r], SEEK_SET) != 0) break;
     uint32_t nb = 0, mb = 0;
     R.len = 0;
     u32(R.len);
@@ -255,7 +281,7 @@ int load_twobit(const std::string& path, PackedGenome& g) {
     for (auto& v : R.nstart) u32(v);
     for (auto& v : R.nsize) u32(v);
     u32(mb);
-    fseek(f, (long)mb * 8 + 4, SEEK_CUR);
+    fseeko(f, (off_t)mb * 8 + 4, SEEK_CUR);
     R.packed.assign(((uint64_t)R.len + 3) / 4, 0);
     const size_t got = fread(R.packed.data(), 1, R.packed.size(), f);
     (void)got;  // a short file leaves zeros (T), like the reference's unread buffer
@@ -312,3 +338,27 @@ int load_twobit(const std::string& path, PackedGenome& g) {
 }
 
 }  // namespace cof
+
+// Test hook (include/cof_tools.h): the reference's genome string as the
+// loaders produce it, decoded back from the planes.
+extern "C" int cofx_genome_text(const char* path, char* out, uint64_t cap, uint64_t* n) {
+  cof::PackedGenome g;
+  const std::string p = path ? path : "";
+  if (cof::load_fasta(p, g) != 0 && cof::load_twobit(p, g) != 0) return 1;
+  if (n) *n = g.n;
+  if (!out || cap < g.n) return 0;
+  size_t e = 0;
+  for (uint64_t q = 0; q < g.n; ++q) {
+    const unsigned b = q & 31;
+    const unsigned h = (g.hi[q >> 5] >> b) & 1, l = (g.lo[q >> 5] >> b) & 1, o = (g.ot[q >> 5] >> b) & 1;
+    char c;
+    if (!o) c = "TCAG"[h * 2 + l];
+    else if (!h) c = l ? ';' : 'N';
+    else {
+      while (e < g.exc_pos.size() && g.exc_pos[e] < q) ++e;
+      c = (e < g.exc_pos.size() && g.exc_pos[e] == q) ? (char)g.exc_byte[e] : 'N';
+    }
+    out[q] = c;
+  }
+  return 0;
+}

@@ -449,15 +449,18 @@ constexpr uint32_t kRowStage = 32768;
 
 __global__ void __launch_bounds__(kRowThreads) write_rows_kernel(GenomeView g, FormatTables ft,
                                                                  const uint64_t* __restrict__ hits, uint64_t n_hits,
-                                                                 const uint64_t* __restrict__ offsets, uint64_t total,
+                                                                 const uint64_t* __restrict__ offsets,
+                                                                 uint64_t out_base, uint64_t total,
                                                                  char* __restrict__ out) {
   __shared__ __align__(16) char stage[kRowStage];
   const uint64_t i0 = (uint64_t)blockIdx.x * kRowThreads, i = i0 + threadIdx.x;
   const uint64_t i1 = min(i0 + kRowThreads, n_hits);
-  const uint64_t base = offsets[i0], end = i1 < n_hits ? offsets[i1] : total;
+  // Byte positions relative to `out` (offsets - out_base).
+  const uint64_t base = offsets[i0] - out_base, end = (i1 < n_hits ? offsets[i1] : total) - out_base;
   const uint64_t a0 = base & ~15ull;  // stage[0] holds output byte a0
   const bool staged = end - a0 <= kRowStage;
-  if (i < n_hits) write_row(g, ft, hits[i], staged ? stage + (offsets[i] - a0) : out + offsets[i]);
+  if (i < n_hits)
+    write_row(g, ft, hits[i], staged ? stage + (offsets[i] - out_base - a0) : out + (offsets[i] - out_base));
   if (!staged) return;  // the same for the whole block
   __syncthreads();
   for (uint64_t c = a0 + 16 * threadIdx.x; c < end; c += 16 * kRowThreads) {
@@ -478,10 +481,10 @@ void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint6
 }
 
 void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
-                       const uint64_t* offsets, uint64_t total, char* out, cudaStream_t stream) {
+                       const uint64_t* offsets, uint64_t base, uint64_t end, char* out, cudaStream_t stream) {
   if (!n_hits) return;
   write_rows_kernel<<<(unsigned)((n_hits + kRowThreads - 1) / kRowThreads), kRowThreads, 0, stream>>>(
-      g, ft, hits, n_hits, offsets, total, out);
+      g, ft, hits, n_hits, offsets, base, end, out);
 }
 
 // Byte offset of each job's first row: job j's hits start at the first sorted

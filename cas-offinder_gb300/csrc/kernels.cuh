@@ -137,10 +137,11 @@ uint32_t bs_class_of(unsigned char p);  // class row of a pattern byte (0: never
 // Row byte counts per sorted hit (and rows per hit).
 void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
                         uint64_t* row_bytes, uint32_t* row_count, cudaStream_t stream);
-// Writes the rows of every hit at `offsets` (exclusive scan of row_bytes;
-// `total` = all rows' bytes).
+// Writes the rows of hits [0, n_hits) at out + (offsets[i] - base) (offsets:
+// exclusive scan of row_bytes; `end` = the byte offset just past the last
+// hit's rows).
 void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
-                       const uint64_t* offsets, uint64_t total, char* out, cudaStream_t stream);
+                       const uint64_t* offsets, uint64_t base, uint64_t end, char* out, cudaStream_t stream);
 
 // Per job (global variant ids job_gid0[j] .. job_gid0[j+1]), the byte offset
 // of its first row in the formatted text; out[njobs] = total bytes.

@@ -358,8 +358,8 @@ cof_status format_request(cof_server* s, Request& r, std::string& err) {
   COF_FIN(cudaStreamSynchronize(st));
   const uint64_t bytes = last[0] + last[1];
   COF_FIN(s->fmt_text.ensure(bytes + 1));
-  launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), bytes, s->fmt_text.as<char>(),
-                    st);
+  launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), 0, bytes,
+                    s->fmt_text.as<char>(), st);
   COF_FIN(cudaGetLastError());
   // Rows go straight to a pinned host buffer from the handle's pool.
   size_t cap = 0;

@@ -36,7 +36,7 @@ enum {
   COF_ERR_ARG = 2,         /* a bad argument (null pointer, size out of range) */
   COF_ERR_NOMEM = 3,       /* device or host allocation failed */
   COF_ERR_INPUT = 4,       /* malformed input file; message = the reference's text */
-  COF_ERR_IO = 5,          /* a file could not be read */
+  COF_ERR_IO = 5,          /* a file could not be read, or the caller's row writer failed */
   COF_ERR_STATE = 6,       /* call out of order (no input or no genome loaded) */
   COF_ERR_UNSUPPORTED = 7, /* pattern longer than COF_MAX_PATTERN */
   COF_ERR_NOT_GENOME = 8,  /* file is neither FASTA nor 2BIT ("Skipping non-acceptable file") */
@@ -103,6 +103,16 @@ cof_status cof_genome_info(const cof_handle* h, uint64_t* n, uint32_t* n_records
  *      `*rows` points into a buffer owned by the handle, valid until the next
  *      search or cof_close. */
 cof_status cof_search(cof_handle* h, const char** rows, size_t* rows_len);
+/* Receives row text: returns 0 to go on, anything else to stop (the search
+ * then returns COF_ERR_IO). */
+typedef int (*cof_write_fn)(void* ctx, const char* data, size_t len);
+/* cof_search with the rows streamed to `write` in order, in chunks of about
+ * 10^6 hits, instead of one buffer (the reference writes rows as it formats
+ * them, cas-offinder.cpp:450-455): chunk k+1 is formatted and copied to host
+ * memory while the caller writes chunk k, and memory use stays bounded for
+ * searches with billions of bytes of rows.  *bytes_written (may be null)
+ * = total bytes handed to `write`.  Summary counts as after cof_search. */
+cof_status cof_search_stream(cof_handle* h, cof_write_fn write, void* ctx, uint64_t* bytes_written);
 /* Load + search in one call, for a genome that lives in host memory (the
  * reference's per-file loop: setChrData, then loadNextChunk / findPattern /
  * compareAll per chunk, cas-offinder.cpp:175-297, 330-469).  Arguments as

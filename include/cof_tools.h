@@ -36,6 +36,12 @@ void cofx_mismatch_table(uint8_t* out);
  * roofline.  Takes about a second.  Returns 0 on success. */
 int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd);
 
+/* Test hook: loads a FASTA or 2BIT file with the engine's loaders (no GPU
+ * needed) and writes the reference's genome string (records joined by ';')
+ * to `out` when `cap` suffices; *n = its length.  Returns 0, or 1 when the
+ * file is neither format. */
+int cofx_genome_text(const char* path, char* out, uint64_t cap, uint64_t* n);
+
 /* Test hook: parses one input file (the whole text) and builds the lane
  * programs of the bit-sliced comparer for its compare variants (layout in
  * cas-offinder_gb300/csrc/kernels.cuh, launch_comparer_bs).  info[0..5] =

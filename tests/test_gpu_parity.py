@@ -151,6 +151,17 @@ def test_hit_buffer_growth_with_captured_passes(P, built):
         eng.set_profiling(False)
         assert a == b
         assert eng.search() == a
+        # The same rows streamed in chunks of 2^20 hits (two chunks here).
+        parts = []
+        assert eng.search_stream(parts.append) == len(a)
+        assert len(parts) == 2 and b"".join(parts) == a
+
+        def refuse(chunk):
+            raise IOError("disk full")
+        with pytest.raises(P.CofError) as e:
+            eng.search_stream(refuse)
+        assert e.value.status == 5  # COF_ERR_IO
+        assert eng.search() == a    # the handle stays usable
 
 
 def read_fasta(path):
