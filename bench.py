@@ -409,6 +409,7 @@ def main():
     for _ in range(args.warmup):
         addr, rows_len = eng.search_view()
     nh, nrows = eng.last_hit_count()
+    schedule = eng.schedule().strip()
 
     # ---- per-kernel times (CUDA events around every launch): one profiled
     # search, outside the timed region
@@ -498,7 +499,7 @@ def main():
                                    "NNNNNNNNNNNNNNNNNNNNNRG dna 2 rna 1, 4 random 20-nt guides + NNN, mm 5",
                        "genome_bp": n, "variants": info["variants"], "pattern_len": info["pattern_len"],
                        "hits": nh, "rows": nrows, "l2": "no flush: inputs (1.16 GB planes) exceed L2",
-                       "genome_gen_s": round(gen_s, 1)},
+                       "genome_gen_s": round(gen_s, 1), "comparer_schedule": schedule},
             "e2e": {"value": e2e_value, "unit": "guide-Gbp/s", "h2d_bytes_per_step": h2d_bytes,
                     "d2h_bytes_per_step": rows_len + 16, "ms_per_step": e2e_ms},
             "roofline": {"bound": "int-pipe", "kernel": "comparer", "achieved": achieved, "peak": peak,
@@ -529,7 +530,8 @@ def run_batched(P, eng, lens, rates, args):
     for t in texts:
         eng.batch_add_input(t)
     info = eng.input_info()
-    eng.search_view()  # warm-up (sizes every buffer)
+    eng.search_view()  # warm-up (sizes every buffer, tunes the comparer)
+    schedule = eng.schedule().strip()
     eng.synchronize()
     eng.reset_stats()
     eng.set_profiling(True)
@@ -559,7 +561,7 @@ def run_batched(P, eng, lens, rates, args):
         "value": len(texts) * gbp / (ms / 1e3), "unit": "guide-Gbp/s", "ms_per_step": ms,
         "steps": args.batched_steps, "variants": info["variants"], "hits": hits, "rows": rows,
         "plain_value": gbp / (plain_ms / 1e3), "plain_ms_per_input": plain_ms, "plain_sample_inputs": k,
-        "speedup_vs_plain": (plain_ms * len(texts)) / ms,
+        "speedup_vs_plain": (plain_ms * len(texts)) / ms, "comparer_schedule": schedule,
         "comparer_roofline": {"achieved": achieved, "peak": peak, "unit": "G base-comparisons/s",
                               "frac": achieved / peak if peak else None},
     }
@@ -573,7 +575,8 @@ def run_pam_variety(P, eng, lens, rates, args):
     for t in texts:
         eng.batch_add_input(t)
     info = eng.input_info()
-    eng.search_view()  # warm-up
+    eng.search_view()  # warm-up (tunes the comparer)
+    schedule = eng.schedule().strip()
     eng.synchronize()
     eng.reset_stats()
     eng.set_profiling(True)
@@ -603,7 +606,7 @@ def run_pam_variety(P, eng, lens, rates, args):
         "value": guides * gbp / (ms / 1e3), "unit": "guide-Gbp/s", "ms_per_step": ms, "steps": args.batched_steps,
         "variants": info["variants"], "hits": hits, "rows": rows,
         "sequential_value": guides * gbp / (seq_ms / 1e3), "sequential_ms": seq_ms,
-        "speedup_vs_sequential": seq_ms / ms,
+        "speedup_vs_sequential": seq_ms / ms, "comparer_schedule": schedule,
         "comparer_roofline": {"achieved": achieved, "peak": peak, "unit": "G base-comparisons/s",
                               "frac": achieved / peak if peak else None},
     }

@@ -32,7 +32,7 @@ HEADER = ("##Generated by Cas-OFFinder 3.0.0\n"
 # Every entry point include/cof.h declares (checked by the CPU tests).
 EXPORTS = [
     "cof_open", "cof_close", "cof_last_error", "cof_open_error", "cof_read_input", "cof_genome_path",
-    "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes", "cof_search_planes", "cof_search_stream",
+    "cof_input_info", "cof_genome_load_file", "cof_genome_load_text", "cof_genome_load_planes", "cof_search_planes", "cof_search_stream", "cof_set_autotune", "cof_schedule_text",
     "cof_genome_info", "cof_search", "cof_last_hit_count", "cof_set_summary", "cof_summary_text",
     "cof_header_text", "cof_finder_chunk", "cof_comparer_chunk", "cof_plane_words", "cof_pack_text",
     "cof_set_profiling", "cof_kernel_stats", "cof_reset_stats", "cof_timer_start", "cof_timer_stop",
@@ -91,6 +91,8 @@ def lib():
             "cof_genome_info": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u32)]),
             "cof_search": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
             "cof_search_stream": (c.c_int, [vp, WRITE_FN, vp, c.POINTER(u64)]),
+            "cof_set_autotune": (c.c_int, [vp, c.c_int]),
+            "cof_schedule_text": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
             "cof_last_hit_count": (c.c_int, [vp, c.POINTER(u64), c.POINTER(u64)]),
             "cof_set_summary": (c.c_int, [vp, c.c_int]),
             "cof_summary_text": (c.c_int, [vp, c.POINTER(c.c_void_p), c.POINTER(sz)]),
@@ -396,6 +398,16 @@ class CasOFFinder:
     def set_comparer(self, kind):
         """0 auto (bit-sliced when it fits), 1 popcount, 2 bit-sliced."""
         self._check(self._L.cof_set_comparer(self._h, kind))
+
+    def set_autotune(self, on=True):
+        self._check(self._L.cof_set_autotune(self._h, 1 if on else 0))
+
+    def schedule(self):
+        """Per pattern group: pattern, variants, slots, program length m,
+        chunks and the autotuner's timings (one line each)."""
+        p, n = ctypes.c_void_p(), ctypes.c_size_t()
+        self._check(self._L.cof_schedule_text(self._h, ctypes.byref(p), ctypes.byref(n)))
+        return _bytes_at(p.value, n.value).decode()
 
     def comparer_info(self):
         k, sl = ctypes.c_int(), ctypes.c_int()

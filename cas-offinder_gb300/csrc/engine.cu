@@ -200,7 +200,7 @@ void init_group(PatternGroup& g, const std::string& pattern) {
 // (m - 1) are chosen to minimise the work of the resulting 32-lane chunks.
 void build_bs_programs(const std::vector<const Variant*>& vars, const std::vector<uint32_t>& gids, int S,
                        uint32_t row, std::vector<uint32_t>& prog, std::vector<uint32_t>& pgid, uint32_t& chunks,
-                       uint32_t& m_out) {
+                       uint32_t& m_out, uint32_t force_m, std::vector<uint32_t>* ranked) {
   const size_t V = vars.size();
   const int NB = [&] { int b = 1; while ((1 << b) <= S) ++b; return b; }();  // bit_width(S)
   // Slots of each variant as sorted u16 offsets, S per variant (cnt used).
@@ -274,14 +274,25 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
   // full count ~(4.6 S + 26), a step ~37.
   uint32_t best_m = 1;
   double best = 1e300;
+  std::vector<std::pair<double, uint32_t>> costs;
   for (uint32_t m = 1; m <= 24; ++m) {
     const size_t pieces = cut(m, nullptr);
     const double cost = (double)((pieces + 31) / 32) * (4.6 * S + 26 + 37.0 * (m - 1));
+    costs.emplace_back(cost, m);
     if (cost < best * 0.999) {
       best = cost;
       best_m = m;
     }
   }
+  if (ranked) {
+    // Candidates for the autotuner: the model's best and the next cheapest
+    // lengths within 1.5x of it (at most three).
+    std::stable_sort(costs.begin(), costs.end());
+    ranked->assign(1, best_m);
+    for (const auto& c : costs)
+      if (ranked->size() < 3 && c.second != best_m && c.first <= 1.5 * best) ranked->push_back(c.second);
+  }
+  if (force_m >= 1 && force_m <= 24) best_m = force_m;
   std::vector<std::pair<size_t, size_t>> pieces;
   cut(best_m, &pieces);
   const uint32_t m = best_m;
@@ -379,7 +390,8 @@ void build_group_host(bool force_popc, PatternGroup& g, const std::vector<const 
   g.bs_chunks = 0;
   g.bs_m = 1;
   if (g.bs_slots)
-    build_bs_programs(vars, g.gids, g.bs_slots, (uint32_t)bs_row_for(g.L), gh.prog, gh.pgid, g.bs_chunks, g.bs_m);
+    build_bs_programs(vars, g.gids, g.bs_slots, (uint32_t)bs_row_for(g.L), gh.prog, gh.pgid, g.bs_chunks, g.bs_m, 0,
+                      &g.bs_candidates);
 }
 
 cof_status upload_group(cof_handle* h, PatternGroup& g, const GroupHost& gh, cudaStream_t st) {
@@ -444,6 +456,89 @@ using namespace cof::eng;
 
 // Builds the pattern groups and uploads every variant's comparer and
 // formatting tables for the current batch.
+// Autotuner of the lane-program length m: the comparer is timed on one full
+// genome segment for each of the cost model's candidates (twice each, the
+// faster run counts) and the fastest is kept.  Runs once per job set, on the
+// first search; groups whose genome is shorter than two segments keep the
+// model's choice.
+cof_status autotune_group(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars) {
+  g.bs_tuned.clear();
+  if (!g.bs_slots || g.bs_candidates.size() < 2) return COF_OK;
+  const DevGenome& dg = h->genome;
+  const uint64_t npos = dg.n >= g.L ? dg.n - g.L + 1 : 0;
+  const uint64_t words = (npos + 31) / 32;
+  if (words < 2 * kSegWords) return COF_OK;
+  const uint64_t w0 = (words / kSegWords / 2) * kSegWords, w1 = std::min(words, w0 + kSegWords);
+  COF_CUDA(h, h->queue[0].ensure(2 * kSegPositions * 4));
+  COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(h->qcounts.cap, 4)));
+  COF_CUDA(h, h->hit_count.ensure(8));
+  const uint64_t cap = std::max<uint64_t>(h->hits.cap / 8, 1u << 20);
+  COF_CUDA(h, h->hits.ensure(cap * 8));
+  const GenomeView gv = dg.view();
+  uint32_t* q = h->queue[0].as<uint32_t>();
+  uint32_t* qc = h->qcounts.as<uint32_t>();
+  COF_CUDA(h, cudaMemsetAsync(qc, 0, 4, h->stream));
+  launch_finder(gv, w0, w1, g.fpat, q, qc, h->stream);
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  for (cudaEvent_t& e : ev) COF_CUDA(h, cudaEventCreate(&e));
+  const uint32_t row = (uint32_t)bs_row_for(g.L);
+  float best_us = 1e30f;
+  uint32_t best_m = g.bs_m, best_chunks = g.bs_chunks;
+  std::vector<uint32_t> best_prog, best_pgid;
+  cof_status st = COF_OK;
+  for (uint32_t m : g.bs_candidates) {
+    std::vector<uint32_t> prog, pgid;
+    uint32_t chunks = 0, mm = 0;
+    build_bs_programs(vars, g.gids, g.bs_slots, row, prog, pgid, chunks, mm, m, nullptr);
+    DevBuf dprog, dpgid;
+    float us = 1e30f;
+    auto run = [&]() -> cof_status {
+      COF_CUDA(h, dprog.ensure(prog.size() * 4));
+      COF_CUDA(h, dpgid.ensure(pgid.size() * 4));
+      COF_CUDA(h, cudaMemcpyAsync(dprog.p, prog.data(), prog.size() * 4, cudaMemcpyHostToDevice, h->stream));
+      COF_CUDA(h, cudaMemcpyAsync(dpgid.p, pgid.data(), pgid.size() * 4, cudaMemcpyHostToDevice, h->stream));
+      for (int rep = 0; rep < 2; ++rep) {
+        COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
+        COF_CUDA(h, cudaEventRecord(ev[0], h->stream));
+        launch_comparer_bs(gv, q, qc, w0 * 32, dprog.as<uint32_t>(), dpgid.as<uint32_t>(), chunks, mm, g.bs_slots,
+                           g.L, g.concrete_only, h->hits.as<uint64_t>(), h->hit_count.as<unsigned long long>(), cap,
+                           h->sm_count, h->stream);
+        COF_CUDA(h, cudaEventRecord(ev[1], h->stream));
+        COF_CUDA(h, cudaEventSynchronize(ev[1]));
+        float ms = 0;
+        COF_CUDA(h, cudaEventElapsedTime(&ms, ev[0], ev[1]));
+        us = std::min(us, ms * 1e3f);
+      }
+      COF_CUDA(h, cudaGetLastError());
+      return COF_OK;
+    };
+    if ((st = run())) break;
+    g.bs_tuned.emplace_back(mm, us);
+    if (us < best_us) {
+      best_us = us;
+      best_m = mm;
+      best_chunks = chunks;
+      best_prog.swap(prog);
+      best_pgid.swap(pgid);
+    }
+  }
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
+  if (st) return st;
+  if (best_m != g.bs_m) {
+    COF_CUDA(h, g.bs_prog.ensure(best_prog.size() * 4));
+    COF_CUDA(h, g.bs_pgid.ensure(best_pgid.size() * 4));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_prog.p, best_prog.data(), best_prog.size() * 4, cudaMemcpyHostToDevice,
+                                h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(g.bs_pgid.p, best_pgid.data(), best_pgid.size() * 4, cudaMemcpyHostToDevice,
+                                h->stream));
+    COF_CUDA(h, cudaStreamSynchronize(h->stream));
+    g.bs_m = best_m;
+    g.bs_chunks = best_chunks;
+  }
+  return COF_OK;
+}
+
 cof_status upload_jobs(cof_handle* h) {
   if (h->jobs_on_device) return COF_OK;
   h->groups.clear();
@@ -483,6 +578,13 @@ cof_status upload_jobs(cof_handle* h) {
     cof_status st = build_group_tables(h, h->groups[gi], group_vars[gi]);
     if (st) return st;
   }
+  // The planes of a streamed upload are not resident yet: such a search
+  // keeps the cost model's choice.
+  if (h->autotune && !h->upload_pending)
+    for (size_t gi = 0; gi < h->groups.size(); ++gi) {
+      cof_status st = autotune_group(h, h->groups[gi], group_vars[gi]);
+      if (st) return st;
+    }
   COF_CUDA(h, h->vfmt.ensure(std::max<size_t>(total, 1) * sizeof(VariantFmt)));
   COF_CUDA(h, h->sfmt.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
   COF_CUDA(h, h->pool.ensure(std::max<size_t>(pool.size(), 1)));
@@ -1307,7 +1409,7 @@ int cofx_bs_programs(const char* input, size_t len, uint32_t* info, uint32_t* pr
   const uint32_t row = (uint32_t)bs_row_for((uint32_t)job.pattern.size());
   std::vector<uint32_t> pv, gv;
   uint32_t chunks = 0, m = 1;
-  build_bs_programs(vars, gids, S, row, pv, gv, chunks, m);
+  build_bs_programs(vars, gids, S, row, pv, gv, chunks, m, 0, nullptr);
   std::string kt;
   for (const Variant& v : job.variants) kt += v.key + "\t" + std::to_string(v.threshold) + "\n";
   info[0] = chunks;
@@ -1352,6 +1454,41 @@ cof_status cof_set_comparer(cof_handle* h, int kind) {
   if (!h || kind < 0 || kind > 2) return COF_ERR_ARG;
   h->force_popc = kind == 1;
   h->jobs_on_device = false;  // rebuild the comparer tables on the next search
+  return COF_OK;
+}
+
+cof_status cof_set_autotune(cof_handle* h, int enable) {
+  if (!h) return COF_ERR_ARG;
+  h->autotune = enable != 0;
+  h->jobs_on_device = false;  // choose again on the next search
+  return COF_OK;
+}
+
+cof_status cof_schedule_text(cof_handle* h, const char** text, size_t* len) {
+  if (!h || !text || !len) return COF_ERR_ARG;
+  std::string t;
+  for (const PatternGroup& g : h->groups) {
+    char line[256];
+    snprintf(line, sizeof line, "%s variants=%zu slots=%d", g.pattern.c_str(), g.gids.size(), g.bs_slots);
+    t += line;
+    if (g.bs_slots) {
+      snprintf(line, sizeof line, " m=%u chunks=%u", g.bs_m, g.bs_chunks);
+      t += line;
+      if (!g.bs_tuned.empty()) {
+        t += " tuned:";
+        for (const auto& x : g.bs_tuned) {
+          snprintf(line, sizeof line, " m=%u %.1fus", x.first, x.second);
+          t += line;
+        }
+      }
+    } else {
+      t += " popcount";
+    }
+    t += "\n";
+  }
+  h->summary_text = t;
+  *text = h->summary_text.c_str();
+  *len = h->summary_text.size();
   return COF_OK;
 }
 

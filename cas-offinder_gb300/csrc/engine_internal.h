@@ -120,6 +120,8 @@ struct PatternGroup {
   // Bit-sliced comparer programs (layout in kernels.cuh): bs_chunks chunks of
   // 32 lane programs, each a first variant and bs_m - 1 update steps.
   uint32_t bs_chunks = 0, bs_m = 1;
+  std::vector<uint32_t> bs_candidates;             // lengths m worth timing (cost model's best first)
+  std::vector<std::pair<uint32_t, float>> bs_tuned;  // (m, comparer µs per segment) measured by the autotuner
   DevBuf vmask, bs_prog, bs_pgid;
 };
 
@@ -178,6 +180,7 @@ struct cof_handle {
   std::string pass_key;
   uint64_t pass_nseg = 0;
   bool use_graphs = true;
+  bool autotune = true;  // time the lane-program lengths on the first search of a job set
   std::map<std::string, KernelStat> stats;
   std::vector<cudaEvent_t> event_pool;  // reused timing events (profiling)
   cudaEvent_t timer_a = nullptr, timer_b = nullptr;
@@ -224,9 +227,11 @@ cof_status upload_group(cof_handle* h, PatternGroup& g, const GroupHost& gh, cud
 cof_status build_group_tables(cof_handle* h, PatternGroup& g, const std::vector<const Variant*>& vars);
 // Lane programs of the bit-sliced comparer for `vars` (ids `gids`), `S` slots,
 // class rows of `row` words; layout in kernels.cuh.
+// force_m (1-24) replaces the cost model's choice of m; `ranked` (may be
+// null) receives the model's best m and up to two runners-up.
 void build_bs_programs(const std::vector<const Variant*>& vars, const std::vector<uint32_t>& gids, int S,
                        uint32_t row, std::vector<uint32_t>& prog, std::vector<uint32_t>& pgid, uint32_t& chunks,
-                       uint32_t& m);
+                       uint32_t& m, uint32_t force_m, std::vector<uint32_t>* ranked);
 // Row shapes of `vars` (variant i gets id first_gid + i) appended to the
 // formatting tables vf (indexed by id), sf and pool.
 void append_format_tables(const Job& job, std::vector<VariantFmt>& vf, std::vector<ShapeFmt>& sf, std::string& pool);

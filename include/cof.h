@@ -243,6 +243,15 @@ uint64_t cof_pack_text(const char* seq, uint64_t n, uint32_t* hi, uint32_t* lo, 
  * popcount comparer; 1: always the popcount comparer; 2: bit-sliced where
  * possible (same as 0).  Both give identical hits. */
 cof_status cof_set_comparer(cof_handle* h, int kind);
+/* Autotuner of the bit-sliced comparer's lane-program length (variants per
+ * lane program): on by default; on the first search of a job set it times the
+ * comparer on one genome segment for the cost model's best lengths and keeps
+ * the fastest.  Off: the cost model alone chooses. */
+cof_status cof_set_autotune(cof_handle* h, int enable);
+/* One line per pattern group of the last search: pattern, variants, slots,
+ * chosen program length m and chunk count, and the autotuner's timings.
+ * Valid until the next call that returns text. */
+cof_status cof_schedule_text(cof_handle* h, const char** text, size_t* len);
 /* Comparer used by the last search: *kind 1 popcount, 2 bit-sliced; *slots =
  * the bit-sliced slot count (mismatchable positions per variant, padded). */
 cof_status cof_comparer_info(const cof_handle* h, int* kind, int* slots);

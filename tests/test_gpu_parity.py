@@ -119,6 +119,14 @@ def test_search_planes_streams_like_resident_search(P, built):
         eng.load_genome_planes(hi, lo, ot, len(text), ep, eb, names, starts)
         want = eng.search()
         assert len(cases.rows_of(want)) > 100
+        # The first search timed the candidate program lengths on a segment;
+        # the rows do not depend on the choice.
+        sched = eng.schedule()
+        assert "tuned:" in sched, sched
+        eng.set_autotune(False)
+        assert eng.search() == want
+        assert "tuned:" not in eng.schedule()
+        eng.set_autotune(True)
         got = P._bytes_at(*eng.search_planes_view(hi, lo, ot, len(text), ep, eb, names, starts))
         assert got == want
         torch = pytest.importorskip("torch")
