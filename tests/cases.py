@@ -141,3 +141,43 @@ def rows_of(text: bytes):
 
 def np_seed(seed):
     return np.random.default_rng(seed)
+
+
+IUPAC_SETS = {"A": "A", "C": "C", "G": "G", "T": "T", "R": "AG", "Y": "CT", "K": "GT", "M": "AC", "S": "CG",
+              "W": "AT", "B": "CGT", "D": "AGT", "H": "ACT", "V": "ACG", "N": "ACGT"}
+
+
+def shown_mismatch(p, g):
+    """Whether the reference lower-cases genome base g under pattern byte p
+    (cas-offinder.cpp:299-317): a non-ACGT genome byte only under a concrete
+    base, otherwise when g is outside p's IUPAC set."""
+    if p == "N" or p not in IUPAC_SETS:
+        return False
+    if g not in "ACGT":
+        return p in "ACGT"
+    return g not in IUPAC_SETS[p]
+
+
+def row_problems(row: str):
+    """Checks of one output row that need no genome: lower case exactly where
+    an aligned crRNA letter mismatches, and the lower-case count equals the
+    mismatch column.  A DNA-bulge base is compared with the pattern base the
+    crRNA column shows as '-', so it counts without an aligned letter; a '-'
+    strand RNA-bulge row's columns end short of the compared window
+    (cas-offinder.cpp:441-442), so there the count is only a lower bound.
+    Returns a list of problems (empty when the row passes)."""
+    f = row.split("\t")
+    crrna, dna, strand, mm = f[2], f[3], f[6], int(f[7])
+    bases = [c for c in dna if c != "-"]
+    crb = [c for c, d in zip(crrna, dna) if d != "-"]
+    out = []
+    for i, (p, g) in enumerate(zip(crb, bases)):
+        if p != "-" and g.islower() != shown_mismatch(p.upper(), g.upper()):
+            out.append(f"case of base {i}")
+    low = sum(c.islower() for c in bases)
+    if f[1] == "RNA" and strand == "-":
+        if low > mm:
+            out.append(f"{low} lower-case > {mm}")
+    elif low != mm:
+        out.append(f"{low} lower-case != {mm}")
+    return out

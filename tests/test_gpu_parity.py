@@ -47,6 +47,10 @@ RANDOM_CASES = [
     dict(seed=205, lens=[70000], pattern="N" * 24 + "NNNNGMTT", dna=1, rna=1, mm=5, per_guide=40),
     dict(seed=206, lens=[50000, 50000], pattern="N" * 20 + "NNAGAAW", dna=1, rna=1, mm=4, per_guide=40),
     dict(seed=207, lens=[30000], pattern="N" * 40 + "NGG", dna=2, rna=2, mm=8, per_guide=40),
+    # The CPU-runnable configuration's shape: 4 FASTA records, 10 Mbp, NGG
+    # without bulges, 4 guides at mm 4 (and one at 6), planted sites.
+    dict(seed=208, lens=[3000000, 2600000, 2400000, 2000000], pattern="N" * 21 + "GG", mm=[4, 4, 4, 6],
+         per_guide=60, n_frac=0.01),
 ]
 
 

@@ -87,3 +87,17 @@ def test_mismatch_predicate_exhaustive(P, built, oracle, tmp_path):
     assert (ora == golden).all()
     assert (eng == golden).all()
     assert golden.sum() == 1036  # 4 concrete bases x 255 + 6 two-base codes x 2 + 4 three-base codes x 1
+
+
+def test_golden_rows_obey_the_row_rules():
+    """The genome-free row checks that the full-scale GPU test applies to
+    sampled rows hold on every row the reference wrote in the fixtures."""
+    n = 0
+    for case in golden_cases():
+        path = os.path.join(GOLDEN, case, "expected.tsv")
+        if not os.path.exists(path):
+            continue
+        for row in cases.rows_of(open(path, "rb").read()):
+            assert not cases.row_problems(row.decode()), (case, row)
+            n += 1
+    assert n > 4000
