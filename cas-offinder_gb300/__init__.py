@@ -40,6 +40,8 @@ EXPORTS = [
     "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
     "cof_server_start", "cof_server_submit", "cof_server_wait", "cof_server_release", "cof_server_stats",
     "cof_server_last_error", "cof_server_stop",
+    "cof_router_open", "cof_router_add_genome", "cof_router_drop_genome", "cof_router_genomes", "cof_router_submit",
+    "cof_router_wait", "cof_router_release", "cof_router_last_error", "cof_router_close",
     "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table", "cofx_bs_programs", "cofx_genome_text",
 ]
 
@@ -119,6 +121,16 @@ def lib():
             "cof_server_stats": (c.c_int, [vp] + [c.POINTER(u64)] * 6),
             "cof_server_last_error": (c.c_char_p, [vp]),
             "cof_server_stop": (None, [vp]),
+            "cof_router_open": (c.c_int, [c.c_int, u64, u64, u64, c.c_int, c.POINTER(vp)]),
+            "cof_router_add_genome": (c.c_int, [vp, c.c_char_p, c.POINTER(u32)]),
+            "cof_router_drop_genome": (c.c_int, [vp, c.c_char_p]),
+            "cof_router_genomes": (c.c_int, [vp, c.POINTER(u32), c.POINTER(u32)]),
+            "cof_router_submit": (c.c_int, [vp, c.c_char_p, sz, c.POINTER(u64)]),
+            "cof_router_wait": (c.c_int, [vp, u64, c.c_int, c.POINTER(c.c_void_p), c.POINTER(sz),
+                                          c.POINTER(c.c_double)]),
+            "cof_router_release": (c.c_int, [vp, u64]),
+            "cof_router_last_error": (c.c_char_p, [vp]),
+            "cof_router_close": (None, [vp]),
             "cof_batch_add_input": (c.c_int, [vp, c.c_char_p, sz, c.POINTER(u32)]),
             "cof_batch_size": (c.c_int, [vp, c.POINTER(u32)]),
             "cof_job_rows": (c.c_int, [vp, u32, c.POINTER(c.c_void_p), c.POINTER(sz)]),
@@ -506,6 +518,75 @@ class Server:
 
     def __exit__(self, *exc):
         self.stop()
+
+
+class Router:
+    """Served mode over several resident genomes (see include/cof.h): each
+    request goes to the genome its input file's first line names."""
+
+    def __init__(self, device=0, max_active_variants=0, hit_buffer_bytes=0, segment_positions=0, auto_load=False):
+        self._L = lib()
+        r = ctypes.c_void_p()
+        st = self._L.cof_router_open(device, max_active_variants, hit_buffer_bytes, segment_positions,
+                                     1 if auto_load else 0, ctypes.byref(r))
+        if st != COF_OK:
+            raise CofError(st, "cof_router_open failed")
+        self._r = r
+
+    def _err(self, st):
+        return CofError(st, self._L.cof_router_last_error(self._r).decode())
+
+    def add_genome(self, path):
+        """Loads a genome file or directory; returns the number of genome files kept."""
+        n = ctypes.c_uint32()
+        st = self._L.cof_router_add_genome(self._r, os.fsencode(path), ctypes.byref(n))
+        if st != COF_OK:
+            raise self._err(st)
+        return n.value
+
+    def drop_genome(self, path):
+        st = self._L.cof_router_drop_genome(self._r, os.fsencode(path))
+        if st != COF_OK:
+            raise self._err(st)
+
+    def genomes(self):
+        """(resident genomes, resident genome files)."""
+        a, b = ctypes.c_uint32(), ctypes.c_uint32()
+        self._L.cof_router_genomes(self._r, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def submit(self, text):
+        if isinstance(text, str):
+            text = text.encode()
+        t = ctypes.c_uint64()
+        st = self._L.cof_router_submit(self._r, text, len(text), ctypes.byref(t))
+        if st != COF_OK:
+            raise self._err(st)
+        return t.value
+
+    def wait(self, ticket, timeout_ms=-1):
+        """(rows bytes, latency ms), or None on timeout; releases the ticket."""
+        p, n, lat = ctypes.c_void_p(), ctypes.c_size_t(), ctypes.c_double()
+        st = self._L.cof_router_wait(self._r, ticket, timeout_ms, ctypes.byref(p), ctypes.byref(n),
+                                     ctypes.byref(lat))
+        if st == 11:
+            return None
+        if st != COF_OK:
+            raise self._err(st)
+        rows = _bytes_at(p.value, n.value)
+        self._L.cof_router_release(self._r, ticket)
+        return rows, lat.value
+
+    def close(self):
+        if self._r:
+            self._L.cof_router_close(self._r)
+            self._r = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def pipe_rates(device=0):

@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
 CU_SOURCES = ["kernels.cu", "comparer_bs.cu", "engine.cu", "server.cu", "pipe_rates.cu", "noalloc.cu"]
-CPP_SOURCES = ["input.cpp", "genome_io.cpp", "synth.cpp"]
+CPP_SOURCES = ["input.cpp", "genome_io.cpp", "synth.cpp", "router.cpp"]
 # comparer_bs_inst.cu is compiled once per (table row words, window words,
 # concrete-only) instance set of the bit-sliced comparer.
 BS_INSTANCES = [(row, nk, conc) for row, nk in ((36, 1), (36, 2), (68, 2)) for conc in (1, 0)]

@@ -793,6 +793,42 @@ struct StreamSink {
   uint64_t written;
 };
 
+// Summary table (cas-offinder.cpp:451-454): each row of a hit counts once
+// under (id, bulge type, bulge size, mismatches).  The device counts hits per
+// (variant, strand, mismatches); the host spreads each count over the row
+// shapes of that variant and strand.
+cof_status summarise(cof_handle* h, uint64_t nhits) {
+  const uint32_t G = h->job_gid0.back();
+  uint32_t levels = 1;
+  for (const Job& job : h->jobs)
+    for (const Variant& v : job.variants) levels = std::max<uint32_t>(levels, (uint32_t)v.threshold + 1);
+  levels = std::min<uint32_t>(levels, 128);
+  const size_t ncount = (size_t)G * 2 * levels;
+  COF_CUDA(h, h->summary_counts.ensure(ncount * 4));
+  COF_CUDA(h, cudaMemsetAsync(h->summary_counts.p, 0, ncount * 4, h->stream));
+  launch_hit_histogram(h->hits_sorted.as<uint64_t>(), nhits, levels, h->summary_counts.as<uint32_t>(), h->stream);
+  COF_CUDA(h, cudaGetLastError());
+  std::vector<uint32_t> counts(ncount);
+  COF_CUDA(h, cudaMemcpyAsync(counts.data(), h->summary_counts.p, ncount * 4, cudaMemcpyDeviceToHost, h->stream));
+  COF_CUDA(h, cudaStreamSynchronize(h->stream));
+  size_t j = 0;
+  for (uint32_t gid = 0; gid < G; ++gid) {
+    while (gid >= h->job_gid0[j + 1]) ++j;
+    const Variant& var = h->jobs[j].variants[gid - h->job_gid0[j]];
+    for (uint32_t strand = 0; strand < 2; ++strand)
+      for (uint32_t mm = 0; mm < levels; ++mm) {
+        const uint32_t c = counts[((size_t)gid * 2 + strand) * levels + mm];
+        if (!c) continue;
+        for (const RowShape& r : h->jobs[j].shapes[strand][gid - h->job_gid0[j]]) {
+          char key[10000];
+          snprintf(key, sizeof key, "%s,%s,%d,%d", var.id.c_str(), r.type.c_str(), (int)r.bulge_size, (int)mm);
+          h->summaries[j][key] += c;
+        }
+      }
+  }
+  return COF_OK;
+}
+
 cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamSink* sink = nullptr) {
   if (h->jobs.empty()) return fail(h, COF_ERR_STATE, "no input file has been read");
   if (!h->genome.loaded) return fail(h, COF_ERR_STATE, "no genome is loaded");
@@ -949,21 +985,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
   }
   collect(h, evs);
   h->last_rows = nrows;
-  if (h->summary_on) {
-    std::vector<uint64_t> keys(nhits);
-    COF_CUDA(h, cudaMemcpy(keys.data(), h->hits_sorted.p, nhits * 8, cudaMemcpyDeviceToHost));
-    for (uint64_t k : keys) {
-      const uint32_t gid = (uint32_t)(k >> 44), strand = (uint32_t)((k >> 7) & 1), mm = (uint32_t)(k & 0x7F);
-      const size_t j = (size_t)(std::upper_bound(h->job_gid0.begin(), h->job_gid0.end(), gid) - h->job_gid0.begin()) - 1;
-      const uint32_t v = gid - h->job_gid0[j];
-      const Variant& var = h->jobs[j].variants[v];
-      for (const RowShape& r : h->jobs[j].shapes[strand][v]) {
-        char key[10000];
-        snprintf(key, sizeof key, "%s,%s,%d,%d", var.id.c_str(), r.type.c_str(), (int)r.bulge_size, (int)mm);
-        ++h->summaries[j][key];
-      }
-    }
-  }
+  if (h->summary_on && (st = summarise(h, nhits))) return st;
   if (!sink) {
     *rows = (const char*)h->host_text.p;
     *rows_len = bytes;

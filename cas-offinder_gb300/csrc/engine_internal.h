@@ -157,7 +157,7 @@ struct cof_handle {
   DevBuf vfmt, sfmt, pool;           // row formatting tables over all variants
   DevGenome genome, scratch;
 
-  DevBuf queue[2], qcounts, hits, hits_sorted, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small,
+  DevBuf queue[2], qcounts, hits, hits_sorted, summary_counts, hit_count, sort_tmp, row_bytes, row_offsets, row_count, text, small,
       job_start, job_bytes;
   HostPinned host_text;
   DevBuf stream_dev[2];  // cof_search_stream: row chunks on the device / in pinned memory

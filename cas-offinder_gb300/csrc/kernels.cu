@@ -514,6 +514,29 @@ void launch_job_bounds(const uint64_t* sorted, uint64_t n, const uint32_t* job_g
   job_bounds_kernel<<<(njobs + 1 + 127) / 128, 128, 0, stream>>>(sorted, n, job_gid0, njobs, offsets, row_bytes, out);
 }
 
+__global__ void hit_histogram_kernel(const uint64_t* __restrict__ keys, uint64_t n, uint32_t levels,
+                                     uint32_t* __restrict__ counts) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  // Whole warps walk the keys together so that every lane joins the match.
+  const uint64_t span = (n + 31) & ~(uint64_t)31;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < span; i += stride) {
+    uint32_t idx = 0xFFFFFFFFu;
+    if (i < n) {
+      const uint64_t k = keys[i];
+      idx = ((uint32_t)(k >> 44) * 2 + (uint32_t)((k >> 7) & 1)) * levels + (uint32_t)(k & 0x7F);
+    }
+    const uint32_t same = __match_any_sync(0xFFFFFFFFu, idx);
+    if (idx != 0xFFFFFFFFu && (threadIdx.x & 31) == (uint32_t)(__ffs(same) - 1))
+      atomicAdd(&counts[idx], (uint32_t)__popc(same));
+  }
+}
+
+void launch_hit_histogram(const uint64_t* keys, uint64_t n, uint32_t levels, uint32_t* counts, cudaStream_t stream) {
+  if (!n) return;
+  const uint64_t blocks = std::min<uint64_t>((n + 255) / 256, 152 * 8);
+  hit_histogram_kernel<<<(unsigned)blocks, 256, 0, stream>>>(keys, n, levels, counts);
+}
+
 // For each request a (ids from gid0[a]), the index of its first hit in the
 // sorted keys; gid0 has one sentinel entry past the last request.
 __global__ void run_starts_kernel(const uint64_t* __restrict__ sorted, uint64_t n, const uint32_t* __restrict__ gid0,

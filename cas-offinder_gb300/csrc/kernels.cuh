@@ -148,6 +148,12 @@ void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64
 void launch_job_bounds(const uint64_t* sorted, uint64_t n, const uint32_t* job_gid0, uint32_t njobs,
                        const uint64_t* offsets, const uint64_t* row_bytes, uint64_t* out, cudaStream_t stream);
 
+// Summary table counts: counts[(gid * 2 + strand) * levels + mm] += 1 for
+// each hit key (levels = largest mismatch limit + 1; counts zeroed by the
+// caller).  Keys of one (gid, strand, mm) sit next to each other once sorted,
+// so each warp adds one atomic per distinct counter it holds.
+void launch_hit_histogram(const uint64_t* keys, uint64_t n, uint32_t levels, uint32_t* counts, cudaStream_t stream);
+
 // Served mode: first index of each of m requests' id ranges (ids from
 // gid0[a]) in sorted hit keys, and a copy of a run of keys with the request's
 // first id subtracted.

@@ -208,8 +208,9 @@ cof_status run_step(cof_server* s) {
   COF_CUDA(h, s->step_hits.ensure(cap * 8));
   COF_CUDA(h, s->step_count.ensure(8));
   COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(T.groups.size(), 1) * 4));
-  COF_CUDA(h, h->queue[0].ensure(2 * kSegPositions * 4));
-  COF_CUDA(h, h->queue[1].ensure(2 * kSegPositions * 4));
+  // at most two oriented candidates per start position of a segment
+  COF_CUDA(h, h->queue[0].ensure(2 * s->seg_words * 32 * 4));
+  COF_CUDA(h, h->queue[1].ensure(2 * s->seg_words * 32 * 4));
   uint64_t count = 0;
   for (;;) {
     COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<size_t>(T.groups.size(), 1) * 4, h->stream));

@@ -172,6 +172,39 @@ const char* cof_server_last_error(cof_server* s);
 /* Stops the worker; requests not finished end with COF_ERR_STATE. */
 void cof_server_stop(cof_server* s);
 
+/* ---- served mode over several resident genomes.  No counterpart in the
+ * reference, which searches the genome named on line 1 of its input file: one
+ * file, or every file of a directory in readdir order with rows written file
+ * by file (main.cpp:133-147).  A router keeps such genomes resident on one
+ * device, one handle and one server (as cof_server_start) per genome file,
+ * and routes each request to the genome its input file's line 1 names; the
+ * request's rows are the rows of each file of that genome in its file order,
+ * as the CLI writes them (without the header).  Genomes are keyed by their
+ * resolved path. */
+typedef struct cof_router cof_router;
+/* Server settings as cof_server_start, for every genome file.  With auto_load
+ * a request naming a genome that is not resident loads it first; without,
+ * such a request is refused with COF_ERR_STATE. */
+cof_status cof_router_open(int device, uint64_t max_active_variants, uint64_t hit_buffer_bytes,
+                           uint64_t segment_positions, int auto_load, cof_router** out);
+/* Loads a genome (file or directory) and starts its servers; *n_files (may be
+ * NULL) = the genome files kept (files that are neither FASTA nor 2BIT are
+ * skipped, as the CLI does).  A genome already resident is not reloaded. */
+cof_status cof_router_add_genome(cof_router* r, const char* path, uint32_t* n_files);
+/* Stops a genome's servers and frees its device memory; COF_ERR_STATE while
+ * requests for it are not released. */
+cof_status cof_router_drop_genome(cof_router* r, const char* path);
+cof_status cof_router_genomes(cof_router* r, uint32_t* n_genomes, uint32_t* n_files);
+/* As cof_server_submit / wait / release; thread-safe.  *latency_ms = submit
+ * to completion of the genome's last file. */
+cof_status cof_router_submit(cof_router* r, const char* text, size_t len, uint64_t* ticket);
+cof_status cof_router_wait(cof_router* r, uint64_t ticket, int timeout_ms, const char** rows, size_t* rows_len,
+                           double* latency_ms);
+cof_status cof_router_release(cof_router* r, uint64_t ticket);
+const char* cof_router_last_error(cof_router* r);
+/* Stops every server; requests not finished end. */
+void cof_router_close(cof_router* r);
+
 /* Hit count of the last search (hits = (variant, position, strand) triples
  * with mismatches <= threshold, before expansion into bulge rows). */
 cof_status cof_last_hit_count(const cof_handle* h, uint64_t* n_hits, uint64_t* n_rows);

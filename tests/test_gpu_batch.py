@@ -50,25 +50,29 @@ def test_batch_matches_single_job_oracle(P, built, oracle, tmp_path):
         guides = [l.split()[0] for l in lines[2:]]
         cases.plant_sites(rng, seqs, pat[0], guides, 25, 6, dna, rna)
     P.write_fasta(genome, ["chr1", "chr2"], seqs)
-    want = []
+    want, want_summ = [], []
     for j, t in enumerate(texts):
         path = str(tmp_path / f"job{j}.txt")
         open(path, "w").write(t)
         out = str(tmp_path / f"job{j}.tsv")
-        r = cases.run_cli(oracle, path, out, threads=4)
+        summ = str(tmp_path / f"job{j}_summary.txt")
+        r = cases.run_cli(oracle, path, out, threads=4, summary=summ)
         assert r.returncode == 0, r.stderr.decode()
         want.append(open(out, "rb").read())
+        want_summ.append(open(summ, "rb").read())
         assert len(cases.rows_of(want[-1])) > 0, f"job {j} has no hits"
     with P.CasOFFinder(0) as eng:
         eng.load_genome_file(genome)
         for t in texts:
             eng.batch_add_input(t)
         assert eng.batch_size() == len(texts)
+        eng.set_summary(True)
         allrows = eng.search()
         got = [eng.job_rows(j) for j in range(len(texts))]
         assert b"".join(got) == allrows
         for j in range(len(texts)):
             assert P.HEADER.encode() + got[j] == want[j], f"job {j}"
+            assert eng.job_summary(j) == want_summ[j], f"job {j} summary"
         # A second search of the same batch gives the same rows.
         assert eng.search() == allrows
         # Single-job API after a batch: replaces the batch.

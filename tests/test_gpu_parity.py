@@ -58,13 +58,16 @@ RANDOM_CASES = [
 def test_cli_matches_oracle_random(spec, P, built, oracle, tmp_path):
     inp, _ = cases.make_case(str(tmp_path), **spec)
     a, b = str(tmp_path / "ora.tsv"), str(tmp_path / "gpu.tsv")
-    ra = cases.run_cli(oracle, inp, a, threads=4)
-    rb = cases.run_cli(P.CLI_PATH, inp, b, device="G0")
+    sa, sb = str(tmp_path / "ora_summary.txt"), str(tmp_path / "gpu_summary.txt")
+    ra = cases.run_cli(oracle, inp, a, threads=4, summary=sa)
+    rb = cases.run_cli(P.CLI_PATH, inp, b, device="G0", summary=sb)
     assert ra.returncode == 0, ra.stderr.decode()
     assert rb.returncode == 0, rb.stderr.decode()
     ta, tb = open(a, "rb").read(), open(b, "rb").read()
     assert len(cases.rows_of(ta)) > 0
     assert ta == tb
+    # summary table: counts per (id, bulge type, bulge size, mismatches)
+    assert open(sa, "rb").read() == open(sb, "rb").read()
 
 
 def test_abi_search_matches_golden_and_repeats(P, built, tmp_path):

@@ -87,3 +87,65 @@ def test_server_rejects_bad_input_and_times_out_cleanly(P, built, tmp_path):
             if r is None:
                 r = srv.wait(t)
             assert r is not None
+
+
+def test_router_keeps_genome_sets_resident(P, built, oracle, tmp_path):
+    """Requests for two genomes -- a directory of a FASTA file, a 2BIT file and
+    a file that is neither, and a single FASTA file -- sent through one router
+    from two threads: each request's rows are the oracle's for its input file
+    (the directory's files in readdir order, the non-genome file skipped)."""
+    rng = random.Random(66)
+    seqs_a = [P.synth_record(613, r, n, n_frac=0.01, n_run_min=50, n_run_max=500)
+              for r, n in enumerate([120000, 60000, 90000])]
+    seqs_b = [P.synth_record(614, r, n, n_frac=0.01, n_run_min=50, n_run_max=500)
+              for r, n in enumerate([150000, 40000])]
+    dir_a = tmp_path / "genome_a"
+    dir_a.mkdir()
+    file_b = str(tmp_path / "genome_b.fa")
+    texts = []
+    for genome, seqs in ((str(dir_a), seqs_a), (file_b, seqs_b)):
+        for t in batch_inputs(rng, genome):
+            lines = t.strip().split("\n")
+            pat = lines[1].split()
+            dna = int(pat[1]) if len(pat) == 3 else 0
+            rna = int(pat[2]) if len(pat) == 3 else 0
+            cases.plant_sites(rng, seqs, pat[0], [l.split()[0] for l in lines[2:]], 15, 6, dna, rna)
+            texts.append(t)
+    P.write_fasta(str(dir_a / "part1.fa"), ["chr1", "chr2"], seqs_a[:2])
+    cases.write_genome(str(dir_a / "part2.2bit"), "2bit", ["chr3"], seqs_a[2:])
+    (dir_a / "notes.txt").write_text("not a genome\n")
+    P.write_fasta(file_b, ["chrB1", "chrB2"], seqs_b)
+    want = oracle_rows(oracle, tmp_path, texts)
+    assert all(len(cases.rows_of(w)) > 0 for w in want)
+    order = list(range(len(texts)))
+    rng.shuffle(order)
+    with P.Router(0, max_active_variants=300, segment_positions=1 << 15, auto_load=True) as router:
+        assert router.add_genome(str(dir_a)) == 2  # notes.txt skipped
+        tickets = {}
+
+        def client(js):
+            for j in js:
+                tickets[j] = router.submit(texts[j])  # genome_b loads on its first request
+
+        ths = [threading.Thread(target=client, args=(order[k::2],)) for k in range(2)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        got = {j: router.wait(t) for j, t in tickets.items()}
+        assert router.genomes() == (2, 3)
+        for j in range(len(texts)):
+            rows, lat = got[j]
+            assert lat >= 0
+            assert P.HEADER.encode() + rows == want[j], f"request {j}"
+        # A genome with no requests outstanding can be dropped, and comes back
+        # on the next request that names it.
+        router.drop_genome(file_b)
+        assert router.genomes() == (1, 2)
+        j = len(texts) - 1
+        rows, _ = router.wait(router.submit(texts[j]))
+        assert P.HEADER.encode() + rows == want[j]
+    with P.Router(0) as router:  # without auto_load an unknown genome is refused
+        with pytest.raises(P.CofError) as e:
+            router.submit(texts[0])
+        assert e.value.status == 6 and "not resident" in e.value.message
