@@ -386,21 +386,24 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
         emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
         emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
       }
-      uint32_t e = 32;  // gid index of the lane's next tested variant, x 32
-      auto step = [&](uint32_t w) {
+      // Step st tests its variant when it emits (bit 15); the variant's id is
+      // entry st + 1 of the lane's id list.  A candidate passes while the top
+      // plane is clear, so a step has hits when the flag is set and some
+      // candidate of the pair has that plane clear.
+      auto step = [&](uint32_t w, uint32_t st) {
         uint32_t a0, a1, b0, b1;
         lds64<kImm>(tbase + (w & 0x7FFFu), a0, a1);
         lds64<kImm>(tbase + (w >> 16), b0, b1);
         step_update<NB + 1>(pa, a0, b0);
         step_update<NB + 1>(pb, a1, b1);
-        const uint32_t on = (w & 0x8000u) ? kFull : 0u;
-        const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
-        if (__any_sync(kFull, ha | hb)) {
-          const uint32_t gid = (ha | hb) ? __ldg(gids + e) : 0u;
+        const bool any = (w & 0x8000u) && (pa[NB] & pb[NB]) != kFull;
+        if (__any_sync(kFull, any)) {
+          const uint32_t on = any ? kFull : 0u;
+          const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
+          const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
           emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
           emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
         }
-        e += on & 32u;
       };
       // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
       const uint32_t sp = m / 2;
@@ -408,8 +411,8 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
       for (uint32_t j = 0; j < sp; ++j) {
         const uint2 w2 = wn;
         if (j + 1 < sp) wn = __ldg(steps + (j + 1) * 32);
-        step(w2.x);
-        step(w2.y);
+        step(w2.x, 2 * j);
+        step(w2.y, 2 * j + 1);
       }
     }
     run_program<P + 1, S, ROW, CONC>(addr, kmask, kadd, first_on, steps, gids, m, tbase, W, ents, seg_pos0, hits,

@@ -74,6 +74,14 @@ cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const
   if (n > 0 && (starts.empty() || starts[0] != 0)) return fail(h, COF_ERR_ARG, "first record must start at 0");
   for (size_t i = 1; i < starts.size(); ++i)
     if (starts[i] < starts[i - 1] || starts[i] > n) return fail(h, COF_ERR_ARG, "record starts must be sorted");
+  // Each later record follows a ';' (read_fasta.cpp:41): windows holding it
+  // are dropped, so the planes must mark it (other byte, lo set, hi clear).
+  for (size_t i = 1; i < starts.size(); ++i) {
+    const uint64_t p = starts[i] - 1, w = p >> 5;
+    const uint32_t b = 1u << (p & 31);
+    if (starts[i] == 0 || !(ot[w] & b) || !(lo[w] & b) || (hi[w] & b))
+      return fail(h, COF_ERR_ARG, "no ';' separator before record " + std::to_string(i) + " in the planes");
+  }
   COF_CUDA(h, dg.hi.ensure(W * 4));
   COF_CUDA(h, dg.lo.ensure(W * 4));
   COF_CUDA(h, dg.ot.ensure(W * 4));
@@ -308,16 +316,16 @@ void build_bs_programs(const std::vector<const Variant*>& vars, const std::vecto
     base[l] = kadd[first] | (1u << 8);
     for (int sl = 0; sl < cnt[first]; ++sl)
       base[(1 + sl / 2) * 32 + l] |= (uint32_t)slot[(size_t)first * S + sl] << (16 * (sl & 1));
+    // Ids: entry 0 = the first variant, entry st + 1 = the variant that step
+    // st emits (steps that only lead to the next variant have none).
     pgid[(c * m + 0) * 32 + l] = gids[first];
     size_t step = 0;
-    uint32_t e = 1;
     for (size_t x = pieces[pi].first + 1; x < pieces[pi].second; ++x) {
       const int k = diff(ord[x - 1], ord[x], add.data(), rem.data());
       for (int j = 0; j < k; ++j, ++step)
         base[(1 + S / 2) * 32 + ((step / 2) * 32 + l) * 2 + step % 2] =
             add[j] | (j + 1 == k ? 0x8000u : 0u) | ((uint32_t)rem[j] << 16);
-      pgid[(c * m + e) * 32 + l] = gids[ord[x]];
-      ++e;
+      pgid[(c * m + step) * 32 + l] = gids[ord[x]];  // emitted by step - 1
     }
   }
 }

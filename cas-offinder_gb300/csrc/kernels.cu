@@ -72,8 +72,8 @@ __device__ __forceinline__ uint32_t window_bits(uint32_t x0, uint32_t x1, uint32
 template <int NK>
 __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
-    uint64_t w_begin, uint64_t w_end, const __grid_constant__ FinderMasks pat, uint32_t* __restrict__ queue,
-    uint32_t* __restrict__ qcount) {
+    uint64_t w_begin, uint64_t w_end, uint64_t pos_end, const __grid_constant__ FinderMasks pat,
+    uint32_t* __restrict__ queue, uint32_t* __restrict__ qcount) {
   __shared__ uint32_t stage[kFinderThreads / 32][kFinderStage];
   const unsigned lane = threadIdx.x & 31;
   uint32_t* my = stage[threadIdx.x >> 5];
@@ -101,6 +101,14 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
       }
       fwd = ~badf;
       rev = ~badr;
+      // Only windows that end inside the genome: start < n - L + 1, whatever
+      // the plane bits past the end hold.
+      const uint64_t p0 = w << 5;
+      if (p0 + 32 > pos_end) {
+        const uint32_t keep = p0 >= pos_end ? 0u : (0xFFFFFFFFu >> (32 - (unsigned)(pos_end - p0)));
+        fwd &= keep;
+        rev &= keep;
+      }
       if (fwd | rev) {
         // Drop windows holding a record separator (cas-offinder.cl:64-67).
         const uint32_t s0 = o0 & l0 & ~h0, s1 = o1 & l1 & ~h1, s2 = o2 & l2 & ~h2;
@@ -156,6 +164,7 @@ void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const 
   uint64_t blocks = (words + kFinderThreads - 1) / kFinderThreads;
   if (blocks > 65535ull * 8) blocks = 65535ull * 8;
   if (blocks == 0) return;
+  const uint64_t pos_end = g.n >= pat.L ? g.n - pat.L + 1 : 0;
   FinderMasks fm{};
   fm.L = pat.L;
   fm.nf = pat.nf;
@@ -169,11 +178,11 @@ void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const 
     for (int c = 0; c < 5; ++c) fm.rm[j][c] = 0u - ((pat.rm[j] >> c) & 1u);
   }
   if (pat.L <= 32)
-    finder_kernel<1><<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, fm, queue,
-                                                                     qcount);
+    finder_kernel<1><<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, pos_end, fm,
+                                                                     queue, qcount);
   else
-    finder_kernel<2><<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, fm, queue,
-                                                                     qcount);
+    finder_kernel<2><<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, pos_end, fm,
+                                                                     queue, qcount);
 }
 
 // ---------------------------------------------------------------- comparer

@@ -95,8 +95,9 @@ struct FormatTables {
 };
 
 // ---- launchers (kernels.cu).  All run on `stream`, none synchronizes.
-// Scans start positions [32*w_begin, 32*w_end) and appends oriented candidate
-// entries (position - 32*w_begin) << 1 | strand to `queue`.
+// Scans start positions [32*w_begin, 32*w_end) below g.n - L + 1 (windows
+// inside the genome) and appends oriented candidate entries
+// (position - 32*w_begin) << 1 | strand to `queue`.
 void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const FinderPattern& pat, uint32_t* queue,
                    uint32_t* qcount, cudaStream_t stream);
 // Tests every entry of `queue` (count read on the device) against `nvar`
@@ -122,8 +123,9 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
 //                    + l) * 2 + s % 2: bits 0-14 offset of the word added,
 //                    bit 15 a variant ends with this step (test it), bits
 //                    16-30 offset of the word removed (offset 0 = nothing)
-// `pgid[(c * m + e) * 32 + l]` is the global id of lane l's e-th tested
-// variant.  Returns false if no kernel instance fits (then use
+// `pgid[(c * m + e) * 32 + l]` is the global id of lane l's first variant
+// (e = 0) and of the variant that its step e - 1 tests (e >= 1; none for a
+// step without bit 15).  Returns false if no kernel instance fits (then use
 // launch_comparer).  `concrete_only`: no variant uses a degenerate IUPAC code
 // (only the four concrete-base class rows are built).
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,

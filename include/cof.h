@@ -85,8 +85,11 @@ cof_status cof_genome_load_text(cof_handle* h, const char* seq, uint64_t n, cons
                                 const uint64_t* starts, uint32_t n_records);
 /* Pre-packed genome (what cof_pack_text produces, e.g. from pinned memory).
  * Plane word w bit b describes position 32*w+b; each plane has
- * cof_plane_words(n) words.  `exc_pos`/`exc_byte` list, in ascending position
- * order, the bytes that are not A/C/G/T/N/';' (n_exc entries). */
+ * cof_plane_words(n) words; bits past position n - 1 are ignored.  The byte
+ * before each record start but the first must be the ';' separator, as in the
+ * reference's genome string (COF_ERR_ARG otherwise).  `exc_pos`/`exc_byte`
+ * list, in ascending position order, the bytes that are not A/C/G/T/N/';'
+ * (n_exc entries). */
 cof_status cof_genome_load_planes(cof_handle* h, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
                                   uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
                                   const char* const* names, const uint64_t* starts, uint32_t n_records);

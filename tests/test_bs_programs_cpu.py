@@ -37,11 +37,9 @@ def replay(P, text):
                         assert off not in cur
                         cur.add(off)
             kadd = hdr & 0xFF
-            e = 0
             out = []
             if hdr & 0x100:
                 out.append((int(pgid[c, 0, lane]), frozenset(cur), kadd))
-                e = 1
             else:
                 assert not cur
             for st in range(2 * (m // 2)):
@@ -59,8 +57,7 @@ def replay(P, text):
                 # the biased counter never overflows its NB + 1 planes
                 assert len(cur) <= S + 1
                 if emit:
-                    out.append((int(pgid[c, e, lane]), frozenset(cur), kadd))
-                    e += 1
+                    out.append((int(pgid[c, st + 1, lane]), frozenset(cur), kadd))
             for gid, slots, k in out:
                 assert gid not in seen, f"variant {gid} tested twice"
                 seen[gid] = (slots, k)

@@ -242,3 +242,55 @@ def test_both_comparers_identical(spec, P, built, oracle, tmp_path):
         for kind in (1, 2, 0):
             eng.set_comparer(kind)
             assert P.HEADER.encode() + eng.search() == want, f"comparer {kind}"
+
+
+def test_positions_past_2_to_the_32(P, built, oracle, tmp_path):
+    """A genome longer than 2^32 bytes: a first record of N up to just below
+    2^32, then a 1 Mbp record with planted sites on both sides of position
+    2^32.  Rows carry record-relative locations, so the GPU rows must equal
+    the oracle's rows for the second record searched alone."""
+    import random
+    rng = random.Random(232)
+    pattern, dna, rna = "N" * 21 + "RG", 1, 1
+    guides = [("".join(rng.choice("ACGT") for _ in range(20)) + "NNN", 5) for _ in range(3)]
+    rec = P.synth_record(232, 0, 1_000_000, n_frac=0.01, n_run_min=50, n_run_max=500)
+    cases.plant_sites(rng, [rec], pattern, [g for g, _ in guides], 60, 5, dna, rna)
+    start = (1 << 32) - (1 << 19)  # word-aligned start of the second record
+    n = start + len(rec)
+    W = P.plane_words(n)
+    hi, lo, ot = (np.zeros(W, np.uint32) for _ in range(3))
+    ot[:start // 32] = 0xFFFFFFFF  # the N record ...
+    sep = start - 1
+    lo[sep // 32] |= np.uint32(1 << (sep % 32))  # ... and the ';' before chrX
+    rh, rl, ro, rexc, _ = P.pack_text(bytes(rec))
+    assert rexc.size == 0
+    k = (len(rec) + 31) // 32
+    hi[start // 32:start // 32 + k], lo[start // 32:start // 32 + k], ot[start // 32:start // 32 + k] = \
+        rh[:k], rl[:k], ro[:k]
+    fa = str(tmp_path / "rec.fa")
+    P.write_fasta(fa, ["chrX"], [bytes(rec)])
+    text = f"{fa}\n{pattern} {dna} {rna}\n" + "".join(f"{g} {mm}\n" for g, mm in guides)
+    inp = str(tmp_path / "in.txt")
+    open(inp, "w").write(text)
+    out = str(tmp_path / "ora.tsv")
+    r = cases.run_cli(oracle, inp, out, threads=4)
+    assert r.returncode == 0, r.stderr.decode()
+    want = open(out, "rb").read()
+    rows = cases.rows_of(want)
+    assert len(rows) > 50
+    locs = [int(x.split(b"\t")[5]) for x in rows]
+    assert min(locs) < (1 << 19) < max(locs)  # hits on both sides of 2^32
+    # The plane words past the end hold zeros (bases T): the scan must stop
+    # at the genome's end by itself.
+    assert not ot[n // 32 + 1:].any()
+    with P.CasOFFinder(0) as eng:
+        eng.readInputFile(text)
+        eng.load_genome_planes(hi, lo, ot, n, None, None, ["big", "chrX"], [0, start])
+        assert eng.genome_info() == (n, 2)
+        got = eng.search()
+        assert P.HEADER.encode() + got == want
+        # Planes without the separator before a record are refused.
+        lo[sep // 32] &= np.uint32(~(1 << (sep % 32)) & 0xFFFFFFFF)
+        with pytest.raises(P.CofError) as e:
+            eng.load_genome_planes(hi, lo, ot, n, None, None, ["big", "chrX"], [0, start])
+        assert e.value.status == 2 and "separator" in e.value.message
