@@ -8,8 +8,9 @@ namespace bs {
 // Launches the instance for `slots` (8..32); false when none fits.
 template <int ROW, int NK, bool CONC>
 bool dispatch_s(int slots, const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L, uint64_t* hits,
-                unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
+                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L,
+                uint32_t* tile_ctr, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
+                cudaStream_t stream);
 }  // namespace bs
 using bs::dispatch_s;
 
@@ -43,14 +44,14 @@ uint32_t bs_class_of(unsigned char p) {
 
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                         const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
-                        uint32_t L, bool concrete_only, uint64_t* hits, unsigned long long* hit_count,
-                        uint64_t hit_cap, int sm_count, cudaStream_t stream) {
+                        uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,
+                        unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
   if (chunks == 0) return true;
 #define COF_BS_ROW(ROWV, NKV)                                                                                       \
   return concrete_only ? dispatch_s<ROWV, NKV, true>(slots, g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L,  \
-                                                      hits, hit_count, hit_cap, sm_count, stream)                   \
+                                                      tile_ctr, hits, hit_count, hit_cap, sm_count, stream)         \
                        : dispatch_s<ROWV, NKV, false>(slots, g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, \
-                                                       hits, hit_count, hit_cap, sm_count, stream);
+                                                       tile_ctr, hits, hit_count, hit_cap, sm_count, stream);
   if (L <= 32) COF_BS_ROW(36, 1)
   if (L <= 36) COF_BS_ROW(36, 2)
   if (L <= 64) COF_BS_ROW(68, 2)

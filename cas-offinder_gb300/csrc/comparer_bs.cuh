@@ -440,7 +440,8 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
     const uint32_t* __restrict__ queue, const uint32_t* __restrict__ qcount, uint64_t seg_pos0,
     const uint32_t* __restrict__ prog, const uint32_t* __restrict__ pgid, uint32_t chunks, uint32_t m, uint32_t L,
-    uint64_t* __restrict__ hits, unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+    uint32_t* __restrict__ tile_ctr, uint64_t* __restrict__ hits, unsigned long long* __restrict__ hit_count,
+    uint64_t hit_cap) {
   constexpr int NB = bit_width(S);
   constexpr int kPairWords = TableRows<CONC>::kRows * ROW;  // uint2 per pair
   const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -466,7 +467,16 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
 
   const uint32_t n = *qcount;
   const uint32_t ntiles = (n + tile_n - 1) / tile_n;
-  uint32_t t = blockIdx.x;
+  // Tiles: blockIdx.x and blockIdx.x + gridDim.x first, then tiles claimed
+  // from *tile_ctr (zeroed by the caller), so CTAs whose warps are issued
+  // less often take fewer tiles instead of finishing last.  A claim is made
+  // two tiles ahead and published to the CTA through claimed[] (one slot
+  // per parity of the step, written before the step's barrier, read after
+  // it); a CTA's tiles increase, so it stops at the first one past the end.
+  __shared__ uint32_t claimed[2];
+  uint32_t t = blockIdx.x, tn = blockIdx.x + gridDim.x;
+  uint32_t claim = 0;
+  if (threadIdx.x == 0) claim = 2 * gridDim.x + atomicAdd(tile_ctr, 1u);
   const uint32_t ca = warp * 64 + lane, cb = ca + 32;  // this lane's candidates within a tile
   // With one chunk per warp the lane's program stays in registers for the
   // whole kernel; its addresses follow the current buffer.
@@ -478,8 +488,8 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   uint32_t ea = load_entry(queue, t * tile_n + ca, n), eb = load_entry(queue, t * tile_n + cb, n);
   stage_planes<NK>(stage_a, kS * 4, hi, lo, ot, ea, seg_pos0);
   stage_planes<NK>(stage_b, kS * 4, hi, lo, ot, eb, seg_pos0);
-  uint32_t na = load_entry(queue, (t + gridDim.x) * tile_n + ca, n);
-  uint32_t nb = load_entry(queue, (t + gridDim.x) * tile_n + cb, n);
+  uint32_t na = load_entry(queue, tn * tile_n + ca, n);
+  uint32_t nb = load_entry(queue, tn * tile_n + cb, n);
   cp_async_wait_all();
   if (t < ntiles) {
     RawWindow<NK> ra, rb;
@@ -487,18 +497,20 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     unstage<NK>(rb, stage + Stage<NK>::kSlots * kS, kS, eb);
     build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + warp * kPairWords, ents_all + warp * 64);
   }
+  if (threadIdx.x == 0) claimed[0] = claim;
   __syncthreads();
   // One tile per step: count the tile in buffer `cur` while the next tile's
   // words are in flight, then build the next tile into buffer cur ^ 1.
-  unsigned cur = 0;
+  unsigned cur = 0, par = 0;
   while (t < ntiles) {
-    const uint32_t tn = t + gridDim.x;
+    const uint32_t tnn = claimed[par];  // the tile after tn
+    if (threadIdx.x == 0) claim = 2 * gridDim.x + atomicAdd(tile_ctr, 1u);
     ea = na;
     eb = nb;
     stage_planes<NK>(stage_a, kS * 4, hi, lo, ot, ea, seg_pos0);
     stage_planes<NK>(stage_b, kS * 4, hi, lo, ot, eb, seg_pos0);
-    na = load_entry(queue, (tn + gridDim.x) * tile_n + ca, n);
-    nb = load_entry(queue, (tn + gridDim.x) * tile_n + cb, n);
+    na = load_entry(queue, tnn * tile_n + ca, n);
+    nb = load_entry(queue, tnn * tile_n + cb, n);
     const uint32_t* ents = ents_all + cur * (W * 64);
     const uint32_t tbase = table_base + cur * kBufBytes;
     for (uint32_t c = warp; c < chunks; c += W) {
@@ -517,6 +529,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
       build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + (cur ^ 1) * kBufWords + warp * kPairWords,
                                 ents_all + (cur ^ 1) * (W * 64) + warp * 64);
     }
+    if (threadIdx.x == 0) claimed[par ^ 1] = claim;
     __syncthreads();
     if (resident) {
       const uint32_t d = cur ? 0u - kBufBytes : kBufBytes;
@@ -524,7 +537,9 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
       for (int s = 0; s < S; ++s) addr[s] += d;
     }
     cur ^= 1;
+    par ^= 1;
     t = tn;
+    tn = tnn;
   }
 }
 
@@ -545,8 +560,9 @@ inline unsigned bs_warps(uint32_t chunks) {
 
 template <int S, int ROW, int NK, bool CONC>
 void launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-               const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L, uint64_t* hits,
-               unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
+               const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L,
+               uint32_t* tile_ctr, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
+               cudaStream_t stream) {
   const unsigned warps = bs_warps(chunks);
   const int threads = 32 * (int)warps;
   const size_t smem = bs_smem_bytes<ROW, NK, CONC>(warps);
@@ -558,19 +574,20 @@ void launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcoun
       per_sm < 1)
     per_sm = 1;
   comparer_bs_kernel<S, ROW, NK, CONC><<<sm_count * per_sm, threads, smem, stream>>>(
-      g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, hits, hit_count, hit_cap);
+      g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, tile_ctr, hits, hit_count, hit_cap);
 }
 
 }  // namespace
 
 template <int ROW, int NK, bool CONC>
 bool dispatch_s(int slots, const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L, uint64_t* hits,
-                unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
-#define COF_BS_CASE(SV)                                                                                            \
-  case SV:                                                                                                         \
-    launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, hits, hit_count, hit_cap, \
-                                 sm_count, stream);                                                                \
+                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L,
+                uint32_t* tile_ctr, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
+                cudaStream_t stream) {
+#define COF_BS_CASE(SV)                                                                                  \
+  case SV:                                                                                               \
+    launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, tile_ctr, hits,  \
+                                 hit_count, hit_cap, sm_count, stream);                                  \
     return true;
   switch (slots) {
     COF_BS_CASE(8)

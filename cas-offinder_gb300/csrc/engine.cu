@@ -478,7 +478,7 @@ cof_status autotune_group(cof_handle* h, PatternGroup& g, const std::vector<cons
   if (words < 2 * kSegWords) return COF_OK;
   const uint64_t w0 = (words / kSegWords / 2) * kSegWords, w1 = std::min(words, w0 + kSegWords);
   COF_CUDA(h, h->queue[0].ensure(2 * kSegPositions * 4));
-  COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(h->qcounts.cap, 4)));
+  COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(h->qcounts.cap, 8)));  // count, tile counter
   COF_CUDA(h, h->hit_count.ensure(8));
   const uint64_t cap = std::max<uint64_t>(h->hits.cap / 8, 1u << 20);
   COF_CUDA(h, h->hits.ensure(cap * 8));
@@ -507,10 +507,11 @@ cof_status autotune_group(cof_handle* h, PatternGroup& g, const std::vector<cons
       COF_CUDA(h, cudaMemcpyAsync(dpgid.p, pgid.data(), pgid.size() * 4, cudaMemcpyHostToDevice, h->stream));
       for (int rep = 0; rep < 2; ++rep) {
         COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
+        COF_CUDA(h, cudaMemsetAsync(qc + 1, 0, 4, h->stream));
         COF_CUDA(h, cudaEventRecord(ev[0], h->stream));
         launch_comparer_bs(gv, q, qc, w0 * 32, dprog.as<uint32_t>(), dpgid.as<uint32_t>(), chunks, mm, g.bs_slots,
-                           g.L, g.concrete_only, h->hits.as<uint64_t>(), h->hit_count.as<unsigned long long>(), cap,
-                           h->sm_count, h->stream);
+                           g.L, g.concrete_only, qc + 1, h->hits.as<uint64_t>(),
+                           h->hit_count.as<unsigned long long>(), cap, h->sm_count, h->stream);
         COF_CUDA(h, cudaEventRecord(ev[1], h->stream));
         COF_CUDA(h, cudaEventSynchronize(ev[1]));
         float ms = 0;
@@ -666,9 +667,10 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   }
   const uint64_t nseg = (max_words + kSegWords - 1) / kSegWords;
   *seg_count = nseg;
+  // qcounts: candidate counts per pass, then the comparer's tile counters.
   const uint64_t nq = std::max<uint64_t>(nseg * G, 1);
-  COF_CUDA(h, h->qcounts.ensure(nq * 4));
-  COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, nq * 4, h->stream));
+  COF_CUDA(h, h->qcounts.ensure(2 * nq * 4));
+  COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, 2 * nq * 4, h->stream));
   COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
   COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
   COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
@@ -701,8 +703,9 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       const uint32_t V = (uint32_t)g.gids.size();
       if (!g.bs_slots ||
           !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_prog.as<uint32_t>(), g.bs_pgid.as<uint32_t>(),
-                              g.bs_chunks, g.bs_m, g.bs_slots, g.L, g.concrete_only, h->hits.as<uint64_t>(),
-                              h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream))
+                              g.bs_chunks, g.bs_m, g.bs_slots, g.L, g.concrete_only, qc + nq,
+                              h->hits.as<uint64_t>(), h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count,
+                              h->stream))
         launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, h->hits.as<uint64_t>(),
                         h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count, h->stream);
       if ((st = record_stop(h, evs, h->stream))) return st;
@@ -762,12 +765,10 @@ cof_status run_passes_graph(cof_handle* h, uint64_t cap, uint64_t* nseg) {
     max_words = std::max(max_words, (npos + 31) / 32);
   }
   const uint64_t ns = (max_words + kSegWords - 1) / kSegWords;
-  COF_CUDA(h, h->qcounts.ensure(std::max<uint64_t>(ns * h->groups.size(), 1) * 4));
+  COF_CUDA(h, h->qcounts.ensure(2 * std::max<uint64_t>(ns * h->groups.size(), 1) * 4));
   const std::string key = pass_graph_key(h, cap);
   if (!h->pass_graph || key != h->pass_key) {
     if (h->pass_graph) cudaGraphExecDestroy(h->pass_graph);
-  for (cudaEvent_t e : h->stream_ev)
-    if (e) cudaEventDestroy(e);
     h->pass_graph = nullptr;
     std::vector<EventPair> none;
     h->upload_issued = 0;  // a streamed upload is captured whole

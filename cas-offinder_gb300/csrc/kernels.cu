@@ -45,12 +45,16 @@ __device__ __forceinline__ uint32_t bits_at(uint32_t w0, uint32_t w1, uint32_t w
 }  // namespace
 
 // ---------------------------------------------------------------- finder
-// One thread = 32 consecutive start positions (one plane word).  A warp's
-// candidates (up to kFinderStage) are staged in shared memory in scan order,
-// then written to the queue with one atomic reservation and coalesced stores;
-// a warp with more candidates (dense patterns) stores them directly.
+// One warp = 32 x kFinderWords consecutive plane words (32 start positions
+// each); lane `l` takes words l, l + 32, ... so every load is coalesced, and
+// all of a lane's words are loaded before any is tested, to keep many loads
+// in flight.  A warp's candidates (up to kFinderStage) are staged in shared
+// memory in scan order, then written to the queue with one atomic
+// reservation and coalesced stores; a warp with more candidates (dense
+// patterns) stores them directly.
 constexpr int kFinderThreads = 128;
-constexpr int kFinderStage = 512;  // staged entries per warp; denser warps store directly
+constexpr int kFinderWords = 4;     // plane words per lane per pass
+constexpr int kFinderStage = 1024;  // staged entries per warp; denser warps store directly
 
 // Device form of a FinderPattern: per pattern position that can mismatch its
 // window offset and the five class masks (T, C, A, G, other byte) as
@@ -74,77 +78,117 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
     uint64_t w_begin, uint64_t w_end, uint64_t pos_end, const __grid_constant__ FinderMasks pat,
     uint32_t* __restrict__ queue, uint32_t* __restrict__ qcount) {
+  constexpr int K = kFinderWords;
   __shared__ uint32_t stage[kFinderThreads / 32][kFinderStage];
   const unsigned lane = threadIdx.x & 31;
   uint32_t* my = stage[threadIdx.x >> 5];
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t wb = w_begin + (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wb < w_end; wb += stride) {
-    const uint64_t w = wb + lane;
-    uint32_t fwd = 0, rev = 0;
-    if (w < w_end) {
-      // A window of L <= 32 starting in word w ends in word w + 1.
-      const uint32_t h0 = hi[w], h1 = hi[w + 1], h2 = NK == 1 ? 0u : hi[w + 2];
-      const uint32_t l0 = lo[w], l1 = lo[w + 1], l2 = NK == 1 ? 0u : lo[w + 2];
-      const uint32_t o0 = ot[w], o1 = ot[w + 1], o2 = NK == 1 ? 0u : ot[w + 2];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * K;
+  for (uint64_t wb = w_begin + ((uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) * K; wb < w_end;
+       wb += stride) {
+    // A window of L <= 32 starting in word w ends in word w + 1 (L <= 64: w + 2).
+    uint32_t h[K][NK + 1], l[K][NK + 1], o[K][NK + 1];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint64_t w = wb + 32 * k + lane;
+      const bool in = w < w_end;
+#pragma unroll
+      for (int i = 0; i <= NK; ++i) {
+        h[k][i] = in ? hi[w + i] : 0u;
+        l[k][i] = in ? lo[w + i] : 0u;
+        o[k][i] = in ? ot[w + i] : 0u;
+      }
+    }
+    static_assert(K % 2 == 0, "counts are scanned two per word");
+    uint32_t fwd[K], rev[K], cnt[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const uint32_t h0 = h[k][0], h1 = h[k][1], h2 = NK == 1 ? 0u : h[k][NK];
+      const uint32_t l0 = l[k][0], l1 = l[k][1], l2 = NK == 1 ? 0u : l[k][NK];
+      const uint32_t o0 = o[k][0], o1 = o[k][1], o2 = NK == 1 ? 0u : o[k][NK];
       uint32_t badf = 0, badr = 0;
       for (uint32_t j = 0; j < pat.nf; ++j) {
-        const unsigned k = pat.fk[j];
-        badf |= mismatch_word(window_bits<NK>(h0, h1, h2, k), window_bits<NK>(l0, l1, l2, k),
-                              window_bits<NK>(o0, o1, o2, k), pat.fm[j][0], pat.fm[j][1], pat.fm[j][2],
+        const unsigned q = pat.fk[j];
+        badf |= mismatch_word(window_bits<NK>(h0, h1, h2, q), window_bits<NK>(l0, l1, l2, q),
+                              window_bits<NK>(o0, o1, o2, q), pat.fm[j][0], pat.fm[j][1], pat.fm[j][2],
                               pat.fm[j][3], pat.fm[j][4]);
       }
       for (uint32_t j = 0; j < pat.nr; ++j) {
-        const unsigned k = pat.rk[j];
-        badr |= mismatch_word(window_bits<NK>(h0, h1, h2, k), window_bits<NK>(l0, l1, l2, k),
-                              window_bits<NK>(o0, o1, o2, k), pat.rm[j][0], pat.rm[j][1], pat.rm[j][2],
+        const unsigned q = pat.rk[j];
+        badr |= mismatch_word(window_bits<NK>(h0, h1, h2, q), window_bits<NK>(l0, l1, l2, q),
+                              window_bits<NK>(o0, o1, o2, q), pat.rm[j][0], pat.rm[j][1], pat.rm[j][2],
                               pat.rm[j][3], pat.rm[j][4]);
       }
-      fwd = ~badf;
-      rev = ~badr;
-      // Only windows that end inside the genome: start < n - L + 1, whatever
-      // the plane bits past the end hold.
-      const uint64_t p0 = w << 5;
+      uint32_t f = ~badf, r = ~badr;
+      // Words past w_end (loaded as zeros) test nothing; and only windows
+      // that end inside the genome count: start < n - L + 1, whatever the
+      // plane bits past the end hold.
+      if (wb + 32 * k + lane >= w_end) f = r = 0;
+      const uint64_t p0 = (wb + 32 * k + lane) << 5;
       if (p0 + 32 > pos_end) {
         const uint32_t keep = p0 >= pos_end ? 0u : (0xFFFFFFFFu >> (32 - (unsigned)(pos_end - p0)));
-        fwd &= keep;
-        rev &= keep;
+        f &= keep;
+        r &= keep;
       }
-      if (fwd | rev) {
+      if (f | r) {
         // Drop windows holding a record separator (cas-offinder.cl:64-67).
         const uint32_t s0 = o0 & l0 & ~h0, s1 = o1 & l1 & ~h1, s2 = o2 & l2 & ~h2;
         if (s0 | s1 | s2) {
           uint32_t near = 0;
-          for (unsigned k = 0; k < pat.L; ++k) near |= window_bits<NK>(s0, s1, s2, k);
-          fwd &= ~near;
-          rev &= ~near;
+          for (unsigned q = 0; q < pat.L; ++q) near |= window_bits<NK>(s0, s1, s2, q);
+          f &= ~near;
+          r &= ~near;
         }
       }
+      fwd[k] = f;
+      rev[k] = r;
+      cnt[k] = __popc(f) + __popc(r);
     }
-    const uint32_t cnt = __popc(fwd) + __popc(rev);
-    uint32_t incl = cnt;
+    // Queue order = word order (pass k's 32 words, then pass k + 1's): the
+    // comparer gathers the windows of consecutive entries together, so
+    // nearby entries should be nearby in the genome.  Per-pass offsets come
+    // from one scan of two 16-bit counts per word (a warp pass has at most
+    // 32 x 64 candidates).
+    uint32_t incl[K / 2], tot[K];
 #pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t t = __shfl_up_sync(kFull, incl, d);
-      if (lane >= (unsigned)d) incl += t;
+    for (int k = 0; k < K; k += 2) {
+      uint32_t x = cnt[k] | (cnt[k + 1] << 16);
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(kFull, x, d);
+        if (lane >= (unsigned)d) x += t;
+      }
+      incl[k / 2] = x;
+      const uint32_t all = __shfl_sync(kFull, x, 31);
+      tot[k] = all & 0xFFFFu;
+      tot[k + 1] = all >> 16;
     }
-    const uint32_t total = __shfl_sync(kFull, incl, 31);
+    uint32_t total = 0;
+#pragma unroll
+    for (int k = 0; k < K; ++k) total += tot[k];
     if (total == 0) continue;  // warp-uniform
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(qcount, total);
     base = __shfl_sync(kFull, base, 0);
-    const uint32_t rel = (uint32_t)((w - w_begin) << 5);
-    // Candidates in descending bit order (queue order does not matter).
+    // Within a word: descending bit order, '+' before '-'.
     auto emit = [&](uint32_t* dst) {
-      uint32_t at = incl - cnt;
-      while (fwd) {
-        const unsigned b = 31 - __clz(fwd);
-        fwd ^= 1u << b;
-        dst[at++] = (rel + b) << 1;
-      }
-      while (rev) {
-        const unsigned b = 31 - __clz(rev);
-        rev ^= 1u << b;
-        dst[at++] = ((rel + b) << 1) | 1u;
+      uint32_t pass0 = 0;  // entries of the earlier passes
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const uint32_t mine = (k & 1) ? incl[k / 2] >> 16 : incl[k / 2] & 0xFFFFu;
+        uint32_t at = pass0 + mine - cnt[k];
+        pass0 += tot[k];
+        const uint32_t rel = (uint32_t)((wb + 32 * k + lane - w_begin) << 5);
+        uint32_t f = fwd[k], r = rev[k];
+        while (f) {
+          const unsigned b = 31 - __clz(f);
+          f ^= 1u << b;
+          dst[at++] = (rel + b) << 1;
+        }
+        while (r) {
+          const unsigned b = 31 - __clz(r);
+          r ^= 1u << b;
+          dst[at++] = ((rel + b) << 1) | 1u;
+        }
       }
     };
     if (total <= (uint32_t)kFinderStage) {  // warp-uniform
@@ -161,7 +205,7 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
 void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const FinderPattern& pat, uint32_t* queue,
                    uint32_t* qcount, cudaStream_t stream) {
   const uint64_t words = w_end - w_begin;
-  uint64_t blocks = (words + kFinderThreads - 1) / kFinderThreads;
+  uint64_t blocks = (words + kFinderThreads * kFinderWords - 1) / (kFinderThreads * kFinderWords);
   if (blocks > 65535ull * 8) blocks = 65535ull * 8;
   if (blocks == 0) return;
   const uint64_t pos_end = g.n >= pat.L ? g.n - pat.L + 1 : 0;

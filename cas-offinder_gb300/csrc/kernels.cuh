@@ -127,11 +127,12 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
 // (e = 0) and of the variant that its step e - 1 tests (e >= 1; none for a
 // step without bit 15).  Returns false if no kernel instance fits (then use
 // launch_comparer).  `concrete_only`: no variant uses a degenerate IUPAC code
-// (only the four concrete-base class rows are built).
+// (only the four concrete-base class rows are built).  `tile_ctr`: a u32 the
+// caller zeroes before each launch (CTAs claim tiles from it).
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                         const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
-                        uint32_t L, bool concrete_only, uint64_t* hits, unsigned long long* hit_count,
-                        uint64_t hit_cap, int sm_count, cudaStream_t stream);
+                        uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,
+                        unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
 int bs_slots_for(int max_positions);  // 0 when more than 32 positions can mismatch
 int bs_row_for(uint32_t L);           // words per class row of the shared table
 uint32_t bs_class_of(unsigned char p);  // class row of a pattern byte (0: never mismatches)

@@ -207,13 +207,15 @@ cof_status run_step(cof_server* s) {
   uint64_t cap = std::max<uint64_t>(s->step_hits.cap / 8, 1u << 16);
   COF_CUDA(h, s->step_hits.ensure(cap * 8));
   COF_CUDA(h, s->step_count.ensure(8));
-  COF_CUDA(h, h->qcounts.ensure(std::max<size_t>(T.groups.size(), 1) * 4));
+  // candidate counts per group, then the comparer's tile counters
+  const size_t nq = std::max<size_t>(T.groups.size(), 1);
+  COF_CUDA(h, h->qcounts.ensure(2 * nq * 4));
   // at most two oriented candidates per start position of a segment
   COF_CUDA(h, h->queue[0].ensure(2 * s->seg_words * 32 * 4));
   COF_CUDA(h, h->queue[1].ensure(2 * s->seg_words * 32 * 4));
   uint64_t count = 0;
   for (;;) {
-    COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, std::max<size_t>(T.groups.size(), 1) * 4, h->stream));
+    COF_CUDA(h, cudaMemsetAsync(h->qcounts.p, 0, 2 * nq * 4, h->stream));
     COF_CUDA(h, cudaMemsetAsync(s->step_count.p, 0, 8, h->stream));
     COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
     COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
@@ -234,8 +236,9 @@ cof_status run_step(cof_server* s) {
       const uint32_t V = (uint32_t)g.gids.size();
       if (!g.bs_slots ||
           !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_prog.as<uint32_t>(), g.bs_pgid.as<uint32_t>(),
-                              g.bs_chunks, g.bs_m, g.bs_slots, g.L, g.concrete_only, s->step_hits.as<uint64_t>(),
-                              s->step_count.as<unsigned long long>(), cap, h->sm_count, h->stream))
+                              g.bs_chunks, g.bs_m, g.bs_slots, g.L, g.concrete_only, qc + nq,
+                              s->step_hits.as<uint64_t>(), s->step_count.as<unsigned long long>(), cap, h->sm_count,
+                              h->stream))
         launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, s->step_hits.as<uint64_t>(),
                         s->step_count.as<unsigned long long>(), cap, h->sm_count, h->stream);
       COF_CUDA(h, cudaEventRecord(h->ev_used[b], h->stream));

@@ -294,3 +294,37 @@ def test_positions_past_2_to_the_32(P, built, oracle, tmp_path):
         with pytest.raises(P.CofError) as e:
             eng.load_genome_planes(hi, lo, ot, n, None, None, ["big", "chrX"], [0, start])
         assert e.value.status == 2 and "separator" in e.value.message
+
+
+def test_cli_directory_matches_oracle(P, built, oracle, tmp_path):
+    """Line 1 naming a directory: every genome file in readdir order (a FASTA
+    file, a 2BIT file, a file that is neither), rows written file by file,
+    the summary counted over all files -- as the reference's main.cpp walks
+    it.  Each file replaces the resident genome, so each search recaptures
+    its passes and streams its rows again."""
+    import random
+    rng = random.Random(77)
+    pattern, dna, rna = "N" * 21 + "RG", 1, 1
+    guides = ["".join(rng.choice("ACGT") for _ in range(20)) + "NNN" for _ in range(3)]
+    recs = [P.synth_record(177, r, n, n_frac=0.01, n_run_min=50, n_run_max=500)
+            for r, n in enumerate([300000, 80000, 200000, 5000])]
+    cases.plant_sites(rng, recs, pattern, guides, 40, 5, dna, rna)
+    d = tmp_path / "genome"
+    d.mkdir()
+    P.write_fasta(str(d / "a.fa"), ["chr1", "chr2"], [bytes(r) for r in recs[:2]])
+    cases.write_genome(str(d / "b.2bit"), "2bit", ["chr3", "chr4"], recs[2:])
+    (d / "readme.txt").write_text("not a genome\n")
+    (d / "c.fa").write_text(">empty\n")
+    inp = str(tmp_path / "in.txt")
+    open(inp, "w").write(f"{d}\n{pattern} {dna} {rna}\n" + "".join(f"{g} 5\n" for g in guides))
+    a, b = str(tmp_path / "ora.tsv"), str(tmp_path / "gpu.tsv")
+    sa, sb = str(tmp_path / "ora_summary.txt"), str(tmp_path / "gpu_summary.txt")
+    ra = cases.run_cli(oracle, inp, a, threads=4, summary=sa)
+    rb = cases.run_cli(P.CLI_PATH, inp, b, device="G0", summary=sb)
+    assert ra.returncode == 0, ra.stderr.decode()
+    assert rb.returncode == 0, rb.stderr.decode()
+    ta = open(a, "rb").read()
+    chroms = {r.split(b"\t")[4] for r in cases.rows_of(ta)}
+    assert {b"chr1", b"chr3"} <= chroms  # rows from both genome files
+    assert ta == open(b, "rb").read()
+    assert open(sa, "rb").read() == open(sb, "rb").read()
