@@ -340,10 +340,17 @@ __device__ __forceinline__ void step_update(uint32_t (&p)[NP], uint32_t a, uint3
   }
 }
 
+// Registers per thread: 72 lets four 224-thread (or seven 128-thread) CTAs
+// share an SM; wider slot lists get more.
+template <int S, int NK>
+struct MaxRegs {
+  static constexpr int value = (S > 16 && S <= 20 && NK == 1) ? 72 : (S <= 20 ? 80 : S <= 28 ? 96 : 104);
+};
+
 // Runs one lane program on pairs P.. W-1 of the current tile (`addr` points
 // at pair 0 of the current buffer, `tbase` is that buffer's base; the pair
 // index is a compile-time constant, so every load is [register + immediate]).
-template <int P, int S, int ROW, bool CONC>
+template <int P, int S, int ROW, int NK, bool CONC>
 __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
                                             uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
                                             const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase, unsigned W,
@@ -390,10 +397,7 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
       // entry st + 1 of the lane's id list.  A candidate passes while the top
       // plane is clear, so a step has hits when the flag is set and some
       // candidate of the pair has that plane clear.
-      auto step = [&](uint32_t w, uint32_t st) {
-        uint32_t a0, a1, b0, b1;
-        lds64<kImm>(tbase + (w & 0x7FFFu), a0, a1);
-        lds64<kImm>(tbase + (w >> 16), b0, b1);
+      auto step = [&](uint32_t w, uint32_t st, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
         step_update<NB + 1>(pa, a0, b0);
         step_update<NB + 1>(pb, a1, b1);
         const bool any = (w & 0x8000u) && (pa[NB] & pb[NB]) != kFull;
@@ -406,26 +410,34 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
         }
       };
       // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
+      // Where registers allow, both steps' class words are loaded before the
+      // first is applied (four shared loads in flight instead of two); the
+      // 72-register instance would spill for it.
+      constexpr bool kBoth = MaxRegs<S, NK>::value > 72;
       const uint32_t sp = m / 2;
       uint2 wn = __ldg(steps);
       for (uint32_t j = 0; j < sp; ++j) {
         const uint2 w2 = wn;
         if (j + 1 < sp) wn = __ldg(steps + (j + 1) * 32);
-        step(w2.x, 2 * j);
-        step(w2.y, 2 * j + 1);
+        uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
+        lds64<kImm>(tbase + (w2.x & 0x7FFFu), a0, a1);
+        lds64<kImm>(tbase + (w2.x >> 16), b0, b1);
+        if constexpr (kBoth) {
+          lds64<kImm>(tbase + (w2.y & 0x7FFFu), c0, c1);
+          lds64<kImm>(tbase + (w2.y >> 16), d0, d1);
+        }
+        step(w2.x, 2 * j, a0, a1, b0, b1);
+        if constexpr (!kBoth) {
+          lds64<kImm>(tbase + (w2.y & 0x7FFFu), c0, c1);
+          lds64<kImm>(tbase + (w2.y >> 16), d0, d1);
+        }
+        step(w2.y, 2 * j + 1, c0, c1, d0, d1);
       }
     }
-    run_program<P + 1, S, ROW, CONC>(addr, kmask, kadd, first_on, steps, gids, m, tbase, W, ents, seg_pos0, hits,
+    run_program<P + 1, S, ROW, NK, CONC>(addr, kmask, kadd, first_on, steps, gids, m, tbase, W, ents, seg_pos0, hits,
                                      hit_count, hit_cap);
   }
 }
-
-// Registers per thread: 72 lets four 224-thread (or seven 128-thread) CTAs
-// share an SM; wider slot lists get more.
-template <int S, int NK>
-struct MaxRegs {
-  static constexpr int value = (S > 16 && S <= 20 && NK == 1) ? 72 : (S <= 20 ? 80 : S <= 28 ? 96 : 104);
-};
 
 // Shared memory of a CTA of W warps: two table buffers of W pairs, their
 // candidate entries, and the staging slots.
@@ -516,7 +528,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     for (uint32_t c = warp; c < chunks; c += W) {
       const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
       if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
-      run_program<0, S, ROW, CONC>(addr, kmask, kadd, first_on,
+      run_program<0, S, ROW, NK, CONC>(addr, kmask, kadd, first_on,
                                    (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
                                    pgid + (size_t)c * m * 32 + lane, m, tbase, W, ents, seg_pos0, hits, hit_count,
                                    hit_cap);
