@@ -42,6 +42,7 @@ EXPORTS = [
     "cof_server_last_error", "cof_server_stop",
     "cof_router_open", "cof_router_add_genome", "cof_router_drop_genome", "cof_router_genomes", "cof_router_submit",
     "cof_router_wait", "cof_router_release", "cof_router_last_error", "cof_router_close",
+    "cof_gzip_open", "cof_gzip_write", "cof_gzip_write_fn", "cof_gzip_close",
     "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table", "cofx_bs_programs", "cofx_genome_text",
 ]
 
@@ -131,6 +132,10 @@ def lib():
             "cof_router_release": (c.c_int, [vp, u64]),
             "cof_router_last_error": (c.c_char_p, [vp]),
             "cof_router_close": (None, [vp]),
+            "cof_gzip_open": (c.c_int, [c.c_char_p, c.c_int, c.c_int, c.POINTER(vp)]),
+            "cof_gzip_write": (c.c_int, [vp, c.c_char_p, sz]),
+            "cof_gzip_write_fn": (c.c_int, [vp, c.c_char_p, sz]),
+            "cof_gzip_close": (c.c_int, [vp]),
             "cof_batch_add_input": (c.c_int, [vp, c.c_char_p, sz, c.POINTER(u32)]),
             "cof_batch_size": (c.c_int, [vp, c.POINTER(u32)]),
             "cof_job_rows": (c.c_int, [vp, u32, c.POINTER(c.c_void_p), c.POINTER(sz)]),
@@ -587,6 +592,23 @@ class Router:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def gzip_write(path, parts, level=1, threads=0):
+    """Writes the byte strings `parts` to `path` through cof_gzip_* (no GPU)."""
+    L = lib()
+    z = ctypes.c_void_p()
+    st = L.cof_gzip_open(os.fsencode(path), level, threads, ctypes.byref(z))
+    if st != COF_OK:
+        raise CofError(st, "cof_gzip_open failed")
+    for p in parts:
+        st = L.cof_gzip_write(z, p, len(p))
+        if st != COF_OK:
+            L.cof_gzip_close(z)
+            raise CofError(st, "cof_gzip_write failed")
+    st = L.cof_gzip_close(z)
+    if st != COF_OK:
+        raise CofError(st, "cof_gzip_close failed")
 
 
 def pipe_rates(device=0):

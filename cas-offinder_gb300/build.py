@@ -27,7 +27,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function"]
 
 CU_SOURCES = ["kernels.cu", "comparer_bs.cu", "engine.cu", "server.cu", "pipe_rates.cu", "noalloc.cu"]
-CPP_SOURCES = ["input.cpp", "genome_io.cpp", "synth.cpp", "router.cpp"]
+CPP_SOURCES = ["input.cpp", "genome_io.cpp", "synth.cpp", "router.cpp", "gzip_out.cpp"]
 # comparer_bs_inst.cu is compiled once per (table row words, window words,
 # concrete-only) instance set of the bit-sliced comparer.
 BS_INSTANCES = [(row, nk, conc) for row, nk in ((36, 1), (36, 2), (68, 2)) for conc in (1, 0)]
@@ -89,7 +89,7 @@ def build(verbose=False):
             if verbose and out:
                 print(out, file=sys.stderr)
     if _stale(LIB, objs):
-        _run([nvcc(), "-shared", *ARCH, "-o", LIB, *objs, "-cudart", "static", "-lpthread"])
+        _run([nvcc(), "-shared", *ARCH, "-o", LIB, *objs, "-cudart", "static", "-lpthread", "-ldl"])
     cli_src = os.path.join(CSRC, "cli.cpp")
     if _stale(CLI, [cli_src, LIB] + hdrs):
         _run(["g++", *CXX_FLAGS, cli_src, "-o", CLI, "-L" + os.path.dirname(LIB), "-lcasoff",

@@ -7,7 +7,9 @@
 // output starts with the reference's two header lines (writeHeaders,
 // cas-offinder.cpp:319-328), then the rows of each genome file.  All work runs
 // on one CUDA device through libcasoff.so; the device letter is accepted for
-// compatibility and the first listed id (default 0) is the CUDA ordinal.
+// compatibility and the first listed id (default 0) is the CUDA ordinal.  An
+// output file name ending in ".gz" gets the same text gzip-compressed
+// (cof_gzip_*, blocks deflated on all host cores).
 #include <dirent.h>
 #include <sys/stat.h>
 #include <sys/time.h>
@@ -107,16 +109,30 @@ int main(int argc, char** argv) {
   if (!summary_path.empty()) cof_set_summary(h, 1);
 
   FILE* out = stdout;
-  if (pos[2] != "-") {
+  cof_gzip* gz = nullptr;
+  const bool gzip = pos[2].size() > 3 && pos[2].compare(pos[2].size() - 3, 3, ".gz") == 0;
+  if (gzip) {
+    const cof_status st = cof_gzip_open(pos[2].c_str(), 1, 0, &gz);
+    if (st != COF_OK) {
+      std::cerr << (st == COF_ERR_UNSUPPORTED ? "No zlib for gzip output " : "Cannot open output file ") << pos[2]
+                << std::endl;
+      return 1;
+    }
+  } else if (pos[2] != "-") {
     out = fopen(pos[2].c_str(), "wb");
     if (!out) {
       std::cerr << "Cannot open output file " << pos[2] << std::endl;
       return 1;
     }
   }
+  // Rows are written as they come off the GPU, chunk by chunk.
+  cof_write_fn writer = gz ? cof_gzip_write_fn : [](void* ctx, const char* data, size_t n) -> int {
+    return write_all((FILE*)ctx, data, n) ? 0 : 1;
+  };
+  void* wctx = gz ? (void*)gz : (void*)out;
   const char* header = cof_header_text();
-  write_all(out, header, strlen(header));
-  fflush(out);
+  writer(wctx, header, strlen(header));
+  if (!gz) fflush(out);
 
   int failed = 0;
   auto run_file = [&](const std::string& path) {
@@ -131,17 +147,13 @@ int main(int argc, char** argv) {
       failed = 1;
       return;
     }
-    // Rows are written as they come off the GPU, chunk by chunk.
-    cof_write_fn writer = [](void* ctx, const char* data, size_t n) -> int {
-      return write_all((FILE*)ctx, data, n) ? 0 : 1;
-    };
-    if ((st = cof_search_stream(h, writer, out, nullptr)) != COF_OK) {
+    if ((st = cof_search_stream(h, writer, wctx, nullptr)) != COF_OK) {
       if (st == COF_ERR_IO) std::cerr << "Write error on " << pos[2] << std::endl;
       else std::cerr << "Search failed on " << path << ": " << cof_last_error(h) << std::endl;
       failed = 1;
       return;
     }
-    fflush(out);
+    if (!gz) fflush(out);
     if (!summary_path.empty()) {
       std::cerr << "Writing summary file..." << std::endl;
       const char* text = nullptr;
@@ -175,7 +187,14 @@ int main(int argc, char** argv) {
     }
     run_file(target);
   }
-  if (out != stdout) fclose(out);
+  if (gz) {
+    if (cof_gzip_close(gz) != COF_OK) {
+      std::cerr << "Write error on " << pos[2] << std::endl;
+      failed = 1;
+    }
+  } else if (out != stdout) {
+    fclose(out);
+  }
   cof_close(h);
   gettimeofday(&t1, nullptr);
   std::cerr << (float)((t1.tv_sec - t0.tv_sec) + (t1.tv_usec - t0.tv_usec) / 1e6) << " seconds elapsed." << std::endl;

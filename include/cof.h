@@ -38,7 +38,7 @@ enum {
   COF_ERR_INPUT = 4,       /* malformed input file; message = the reference's text */
   COF_ERR_IO = 5,          /* a file could not be read, or the caller's row writer failed */
   COF_ERR_STATE = 6,       /* call out of order (no input or no genome loaded) */
-  COF_ERR_UNSUPPORTED = 7, /* pattern longer than COF_MAX_PATTERN */
+  COF_ERR_UNSUPPORTED = 7, /* pattern longer than COF_MAX_PATTERN; gzip output without zlib */
   COF_ERR_NOT_GENOME = 8,  /* file is neither FASTA nor 2BIT ("Skipping non-acceptable file") */
   COF_ERR_DEVICE = 9,      /* a kernel reported an internal inconsistency */
   COF_ERR_TOO_LARGE = 10,  /* input larger than a fixed limit of the entry point */
@@ -207,6 +207,22 @@ cof_status cof_router_release(cof_router* r, uint64_t ticket);
 const char* cof_router_last_error(cof_router* r);
 /* Stops every server; requests not finished end. */
 void cof_router_close(cof_router* r);
+
+/* ---- gzip row output.  The reference writes plain text (cas-offinder.cpp:450);
+ * for searches with GBs of rows the output can be written gzip-compressed:
+ * blocks of 8 MiB are deflated on `threads` host threads (0 = one per core),
+ * each into one gzip member, and written in order (gunzip, zcat and zlib read
+ * the members as one stream).  `level` 1 (fastest) .. 9.  Needs the system
+ * zlib (libz.so.1, loaded at run time): COF_ERR_UNSUPPORTED without it.  The
+ * CLI uses it when the output file name ends in ".gz".  `path` "-" = stdout. */
+typedef struct cof_gzip cof_gzip;
+cof_status cof_gzip_open(const char* path, int level, int threads, cof_gzip** out);
+cof_status cof_gzip_write(cof_gzip* z, const char* data, size_t len);
+/* cof_gzip_write as a cof_write_fn (ctx = the cof_gzip*), for cof_search_stream. */
+int cof_gzip_write_fn(void* ctx, const char* data, size_t len);
+/* Compresses and writes what is left, closes the file and frees `z`; returns
+ * the first error of any write. */
+cof_status cof_gzip_close(cof_gzip* z);
 
 /* Hit count of the last search (hits = (variant, position, strand) triples
  * with mismatches <= threshold, before expansion into bulge rows). */

@@ -328,3 +328,15 @@ def test_cli_directory_matches_oracle(P, built, oracle, tmp_path):
     assert {b"chr1", b"chr3"} <= chroms  # rows from both genome files
     assert ta == open(b, "rb").read()
     assert open(sa, "rb").read() == open(sb, "rb").read()
+
+
+def test_cli_gzip_output(P, built, tmp_path):
+    """An output name ending in .gz: the same bytes, gzip-compressed."""
+    import gzip
+    case = "nrg_bulge_2bit"
+    d = os.path.join(GOLDEN, case)
+    inp = golden_input(case, tmp_path)
+    out = str(tmp_path / "gpu.tsv.gz")
+    r = cases.run_cli(P.CLI_PATH, inp, out, device="G0")
+    assert r.returncode == 0, r.stderr.decode()
+    assert gzip.decompress(open(out, "rb").read()) == open(os.path.join(d, "expected.tsv"), "rb").read()
