@@ -4,6 +4,7 @@ All comparisons are byte-exact: the engine emits rows in the order the
 reference emits them for one chunk with work-items in order, which is also
 the oracle's order."""
 import os
+import random
 
 import numpy as np
 import pytest
@@ -51,6 +52,16 @@ RANDOM_CASES = [
     # without bulges, 4 guides at mm 4 (and one at 6), planted sites.
     dict(seed=208, lens=[3000000, 2600000, 2400000, 2000000], pattern="N" * 21 + "GG", mm=[4, 4, 4, 6],
          per_guide=60, n_frac=0.01),
+    # The longest pattern (62 + DNA bulge 2 = 64 positions: two plane words
+    # per window), and windows of exactly one plane word (32, no bulge).
+    dict(seed=209, lens=[40000, 30000], pattern="N" * 59 + "NGG", dna=2, rna=1, mm=[8, 12], per_guide=30),
+    dict(seed=210, lens=[60000], pattern="N" * 29 + "NRG", mm=6, per_guide=40, iupac_frac=0.05),
+    # A 48-position pattern whose guides leave the first 18 spacer bases N:
+    # 27 positions that can mismatch, so the bit-sliced comparer takes the
+    # two-word windows (68-column class rows).
+    dict(seed=211, lens=[80000, 20000], pattern="N" * 45 + "NGG", dna=1, rna=1, mm=5, per_guide=40,
+         guides=["N" * 18 + "".join(random.Random(211 + i).choice("ACGT") for _ in range(27)) + "NNN"
+                 for i in range(3)]),
 ]
 
 
