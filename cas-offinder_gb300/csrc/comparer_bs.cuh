@@ -347,26 +347,56 @@ struct MaxRegs {
   static constexpr int value = (S > 16 && S <= 20 && NK == 1) ? 72 : (S <= 20 ? 80 : S <= 28 ? 96 : 104);
 };
 
-// Runs one lane program on pairs P.. W-1 of the current tile (`addr` points
-// at pair 0 of the current buffer, `tbase` is that buffer's base; the pair
-// index is a compile-time constant, so every load is [register + immediate]).
-template <int P, int S, int ROW, int NK, bool CONC>
-__device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
-                                            uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
-                                            const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase, unsigned W,
-                                            const uint32_t* ents, uint64_t seg_pos0, uint64_t* __restrict__ hits,
-                                            unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
-  if constexpr (P < kMaxWarps) {
-    if ((unsigned)P >= W) return;
-    constexpr int NB = bit_width(S);
-    constexpr uint32_t kImm = P * TableRows<CONC>::kRows * ROW * 8;
-    uint32_t xa[S], xb[S];
+// The full count of a lane program's first variant on pair P: its S class
+// words summed into NB bit planes.  P is a compile-time constant so that every
+// load is [register + immediate] (`addr` points at pair 0 of the buffer).
+template <int P, int S, int ROW, bool CONC>
+__device__ __forceinline__ void full_count(const uint32_t (&addr)[S], uint32_t (&ba)[bit_width(S)],
+                                           uint32_t (&bb)[bit_width(S)]) {
+  constexpr int NB = bit_width(S);
+  constexpr uint32_t kImm = P * TableRows<CONC>::kRows * ROW * 8;
+  uint32_t xa[S], xb[S];
 #pragma unroll
-    for (int s = 0; s < S; ++s) lds64<kImm>(addr[s], xa[s], xb[s]);
+  for (int s = 0; s < S; ++s) lds64<kImm>(addr[s], xa[s], xb[s]);
+  CountTree<S, 0, NB>::run(xa, ba);
+  CountTree<S, 0, NB>::run(xb, bb);
+}
+
+// Runs one lane program on pair P of the current tile (`addr` points at pair
+// 0 of the current buffer, `tbase` is that buffer's base).  PF >= 0: P is the
+// constant PF; PF < 0: P is a run-time index and only the full count is
+// compiled once per pair index, while the steps, which address their words
+// from the pair's base, run from one copy of the code for every pair (one
+// copy per pair made the loop of an eight-warp CTA larger than the
+// instruction cache).
+template <int PF, int S, int ROW, int NK, bool CONC>
+__device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
+                                         uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
+                                         const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase,
+                                         const uint32_t* ents, uint64_t seg_pos0, uint64_t* __restrict__ hits,
+                                         unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+  constexpr int NB = bit_width(S);
+  constexpr uint32_t kPairBytes = TableRows<CONC>::kRows * ROW * 8;
+  static_assert(kMaxWarps == 8, "one full_count case per pair index");
+  {
     uint32_t ba[NB], bb[NB];
-    CountTree<S, 0, NB>::run(xa, ba);
-    CountTree<S, 0, NB>::run(xb, bb);
+    if constexpr (PF >= 0) {
+      P = PF;
+      full_count<PF, S, ROW, CONC>(addr, ba, bb);
+    } else {
+      switch (P) {
+        case 0: full_count<0, S, ROW, CONC>(addr, ba, bb); break;
+        case 1: full_count<1, S, ROW, CONC>(addr, ba, bb); break;
+        case 2: full_count<2, S, ROW, CONC>(addr, ba, bb); break;
+        case 3: full_count<3, S, ROW, CONC>(addr, ba, bb); break;
+        case 4: full_count<4, S, ROW, CONC>(addr, ba, bb); break;
+        case 5: full_count<5, S, ROW, CONC>(addr, ba, bb); break;
+        case 6: full_count<6, S, ROW, CONC>(addr, ba, bb); break;
+        default: full_count<7, S, ROW, CONC>(addr, ba, bb); break;
+      }
+    }
     const uint32_t* pe = ents + P * 64;
+    const uint32_t pbase = tbase + P * kPairBytes;  // this pair's class words
     if (m == 1) {
       // One variant per lane: only the carry out of count + bias matters.
       uint32_t ca = 0, cb = 0;
@@ -381,60 +411,77 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
         emit_hits<NB>(hita, ba, 0u, pe, gid, seg_pos0, hits, hit_count, hit_cap);
         emit_hits<NB>(hitb, bb, 0u, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
       }
-    } else {
-      // Biased counters (count + bias in NB + 1 planes): a variant passes
-      // while the top plane is clear.
-      uint32_t pa[NB + 1], pb[NB + 1];
-      add_bias<NB>(ba, kmask, pa);
-      add_bias<NB>(bb, kmask, pb);
-      uint32_t hita = ~pa[NB] & first_on, hitb = ~pb[NB] & first_on;
-      if (__any_sync(kFull, hita | hitb)) {
-        const uint32_t gid = __ldg(gids);
-        emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-        emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
-      }
-      // Step st tests its variant when it emits (bit 15); the variant's id is
-      // entry st + 1 of the lane's id list.  A candidate passes while the top
-      // plane is clear, so a step has hits when the flag is set and some
-      // candidate of the pair has that plane clear.
-      auto step = [&](uint32_t w, uint32_t st, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
-        step_update<NB + 1>(pa, a0, b0);
-        step_update<NB + 1>(pb, a1, b1);
-        const bool any = (w & 0x8000u) && (pa[NB] & pb[NB]) != kFull;
-        if (__any_sync(kFull, any)) {
-          const uint32_t on = any ? kFull : 0u;
-          const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
-          const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
-          emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-          emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
-        }
-      };
-      // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
-      // Where registers allow, both steps' class words are loaded before the
-      // first is applied (four shared loads in flight instead of two); the
-      // 72-register instance would spill for it.
-      constexpr bool kBoth = MaxRegs<S, NK>::value > 72;
-      const uint32_t sp = m / 2;
-      uint2 wn = __ldg(steps);
-      for (uint32_t j = 0; j < sp; ++j) {
-        const uint2 w2 = wn;
-        if (j + 1 < sp) wn = __ldg(steps + (j + 1) * 32);
-        uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
-        lds64<kImm>(tbase + (w2.x & 0x7FFFu), a0, a1);
-        lds64<kImm>(tbase + (w2.x >> 16), b0, b1);
-        if constexpr (kBoth) {
-          lds64<kImm>(tbase + (w2.y & 0x7FFFu), c0, c1);
-          lds64<kImm>(tbase + (w2.y >> 16), d0, d1);
-        }
-        step(w2.x, 2 * j, a0, a1, b0, b1);
-        if constexpr (!kBoth) {
-          lds64<kImm>(tbase + (w2.y & 0x7FFFu), c0, c1);
-          lds64<kImm>(tbase + (w2.y >> 16), d0, d1);
-        }
-        step(w2.y, 2 * j + 1, c0, c1, d0, d1);
-      }
+      return;
     }
-    run_program<P + 1, S, ROW, NK, CONC>(addr, kmask, kadd, first_on, steps, gids, m, tbase, W, ents, seg_pos0, hits,
+    // Biased counters (count + bias in NB + 1 planes): a variant passes
+    // while the top plane is clear.
+    uint32_t pa[NB + 1], pb[NB + 1];
+    add_bias<NB>(ba, kmask, pa);
+    add_bias<NB>(bb, kmask, pb);
+    const uint32_t hita = ~pa[NB] & first_on, hitb = ~pb[NB] & first_on;
+    if (__any_sync(kFull, hita | hitb)) {
+      const uint32_t gid = __ldg(gids);
+      emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+    }
+    // Step st tests its variant when it emits (bit 15); the variant's id is
+    // entry st + 1 of the lane's id list.  A candidate passes while the top
+    // plane is clear, so a step has hits when the flag is set and some
+    // candidate of the pair has that plane clear.
+    auto step = [&](uint32_t w, uint32_t st, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
+      step_update<NB + 1>(pa, a0, b0);
+      step_update<NB + 1>(pb, a1, b1);
+      const bool any = (w & 0x8000u) && (pa[NB] & pb[NB]) != kFull;
+      if (__any_sync(kFull, any)) {
+        const uint32_t on = any ? kFull : 0u;
+        const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
+        const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
+        emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+        emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+      }
+    };
+    // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
+    // Where registers allow, both steps' class words are loaded before the
+    // first is applied (four shared loads in flight instead of two); the
+    // 72-register instance would spill for it.
+    constexpr bool kBoth = MaxRegs<S, NK>::value > 72;
+    const uint32_t sp = m / 2;
+    uint2 wn = __ldg(steps);
+    for (uint32_t j = 0; j < sp; ++j) {
+      const uint2 w2 = wn;
+      if (j + 1 < sp) wn = __ldg(steps + (j + 1) * 32);
+      uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
+      lds64<0>(pbase + (w2.x & 0x7FFFu), a0, a1);
+      lds64<0>(pbase + (w2.x >> 16), b0, b1);
+      if constexpr (kBoth) {
+        lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
+        lds64<0>(pbase + (w2.y >> 16), d0, d1);
+      }
+      step(w2.x, 2 * j, a0, a1, b0, b1);
+      if constexpr (!kBoth) {
+        lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
+        lds64<0>(pbase + (w2.y >> 16), d0, d1);
+      }
+      step(w2.y, 2 * j + 1, c0, c1, d0, d1);
+    }
+  }
+}
+
+// Runs one lane program on pairs 0 .. W-1 of the current tile; ONE: the CTA
+// is one warp (W = 1), so the pair index is the constant 0.
+template <int S, int ROW, int NK, bool CONC, bool ONE>
+__device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
+                                            uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
+                                            const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase, unsigned W,
+                                            const uint32_t* ents, uint64_t seg_pos0, uint64_t* __restrict__ hits,
+                                            unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+  if constexpr (ONE) {
+    run_pair<0, S, ROW, NK, CONC>(0, addr, kmask, kadd, first_on, steps, gids, m, tbase, ents, seg_pos0, hits,
+                                  hit_count, hit_cap);
+  } else {
+#pragma unroll 1
+    for (unsigned P = 0; P < W; ++P)
+      run_pair<-1, S, ROW, NK, CONC>(P, addr, kmask, kadd, first_on, steps, gids, m, tbase, ents, seg_pos0, hits,
                                      hit_count, hit_cap);
   }
 }
@@ -447,7 +494,7 @@ __host__ __device__ constexpr size_t bs_smem_bytes(unsigned W) {
          2 * Stage<NK>::kSlots * (32 * W) * 4;
 }
 
-template <int S, int ROW, int NK, bool CONC>
+template <int S, int ROW, int NK, bool CONC, bool ONE>
 __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::value)) comparer_bs_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
     const uint32_t* __restrict__ queue, const uint32_t* __restrict__ qcount, uint64_t seg_pos0,
@@ -528,7 +575,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     for (uint32_t c = warp; c < chunks; c += W) {
       const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
       if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
-      run_program<0, S, ROW, NK, CONC>(addr, kmask, kadd, first_on,
+      run_program<S, ROW, NK, CONC, ONE>(addr, kmask, kadd, first_on,
                                    (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
                                    pgid + (size_t)c * m * 32 + lane, m, tbase, W, ents, seg_pos0, hits, hit_count,
                                    hit_cap);
@@ -578,15 +625,15 @@ void launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcoun
   const unsigned warps = bs_warps(chunks);
   const int threads = 32 * (int)warps;
   const size_t smem = bs_smem_bytes<ROW, NK, CONC>(warps);
-  cudaFuncSetAttribute(comparer_bs_kernel<S, ROW, NK, CONC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  // One-warp CTAs (one chunk) get the instance with the pair index constant.
+  auto kernel = warps == 1 ? comparer_bs_kernel<S, ROW, NK, CONC, true> : comparer_bs_kernel<S, ROW, NK, CONC, false>;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)bs_smem_bytes<ROW, NK, CONC>(kMaxWarps));
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, comparer_bs_kernel<S, ROW, NK, CONC>, threads, smem) !=
-          cudaSuccess ||
-      per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
-  comparer_bs_kernel<S, ROW, NK, CONC><<<sm_count * per_sm, threads, smem, stream>>>(
-      g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, tile_ctr, hits, hit_count, hit_cap);
+  kernel<<<sm_count * per_sm, threads, smem, stream>>>(g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks,
+                                                        m, L, tile_ctr, hits, hit_count, hit_cap);
 }
 
 }  // namespace
