@@ -39,7 +39,7 @@ EXPORTS = [
     "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cof_search_chunk_static",
     "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
     "cof_server_start", "cof_server_submit", "cof_server_wait", "cof_server_release", "cof_server_stats",
-    "cof_server_last_error", "cof_server_stop",
+    "cof_server_set_hit_reserve", "cof_server_memory", "cof_server_last_error", "cof_server_stop",
     "cof_router_open", "cof_router_add_genome", "cof_router_drop_genome", "cof_router_genomes", "cof_router_submit",
     "cof_router_wait", "cof_router_release", "cof_router_last_error", "cof_router_close",
     "cof_gzip_open", "cof_gzip_write", "cof_gzip_write_fn", "cof_gzip_close",
@@ -120,6 +120,8 @@ def lib():
                                           c.POINTER(c.c_double)]),
             "cof_server_release": (c.c_int, [vp, u64]),
             "cof_server_stats": (c.c_int, [vp] + [c.POINTER(u64)] * 6),
+            "cof_server_set_hit_reserve": (c.c_int, [vp, u64]),
+            "cof_server_memory": (c.c_int, [vp] + [c.POINTER(u64)] * 3),
             "cof_server_last_error": (c.c_char_p, [vp]),
             "cof_server_stop": (None, [vp]),
             "cof_router_open": (c.c_int, [c.c_int, u64, u64, u64, c.c_int, c.POINTER(vp)]),
@@ -512,6 +514,15 @@ class Server:
         self._L.cof_server_stats(self._s, *[ctypes.byref(v) for v in vals])
         keys = ("steps", "admitted", "completed", "pending", "active", "max_active")
         return dict(zip(keys, (v.value for v in vals)))
+
+    def set_hit_reserve(self, nbytes):
+        """Hit memory charged per running request at least, for admission."""
+        self._L.cof_server_set_hit_reserve(self._s, int(nbytes))
+
+    def memory(self):
+        vals = [ctypes.c_uint64() for _ in range(3)]
+        self._L.cof_server_memory(self._s, *[ctypes.byref(v) for v in vals])
+        return dict(zip(("held_hit_bytes", "max_held_hit_bytes", "queue_bytes"), (v.value for v in vals)))
 
     def stop(self):
         if self._s:

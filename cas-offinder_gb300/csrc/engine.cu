@@ -686,6 +686,10 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       uint32_t* qc = h->qcounts.as<uint32_t>() + s * G + gi;
       uint32_t* q = h->queue[b].as<uint32_t>();
       if (pass >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
+      // A profiled search times every launch alone: the finder also waits
+      // for the previous pass's comparer, or its events would count the time
+      // it spends queued behind that comparer's CTAs.
+      if (h->profiling && pass >= 1) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[1 - b], 0));
       if (h->upload_pending) {
         // Segment s reads plane words up to w1 + 2 (chunks s and s + 1); its
         // finder follows the copies up to chunk s + 2 on the same stream.
@@ -886,6 +890,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
         const PatternGroup& g = h->groups[idx % G];
         p.units = (double)qc[idx] * g.nonN_sum;
         h->stats["comparer.tests"].units += (double)qc[idx] * (double)g.gids.size();
+        h->stats["finder.candidates"].units += (double)qc[idx];  // queue entries the finder wrote
       }
     collect(h, evs);
   }

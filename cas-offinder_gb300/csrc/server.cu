@@ -5,9 +5,9 @@
 // file) at once.  The genome is walked as a ring of segments; one step
 // processes one segment for every request in the current comparer tables.
 // Requests are admitted at any step boundary -- while others are already
-// running -- as long as the admitted compare variants fit the variant budget,
-// and each request is complete once it has seen every segment of the ring,
-// wherever it joined.  Requests with the same padded pattern share one PAM
+// running -- as long as the admitted compare variants fit the variant budget
+// and their hit memory fits the hit budget (below), and each request is
+// complete once it has seen every segment of the ring, wherever it joined.  Requests with the same padded pattern share one PAM
 // scan and one comparer launch per step, but keep their own variants, ids and
 // thresholds, so every request's rows are exactly those of a search of that
 // input file alone.
@@ -24,6 +24,15 @@
 //             and copies the rows into a pinned host buffer taken from the
 //             handle's pool (returned on cof_server_release), so delivering
 //             GBs of rows touches no fresh pages once the pool is warm.
+// Memory.  The candidate queues (two, 2 x segment positions x 4 B each) and
+// the step's hit buffer are sized by the ring segment and shared by every
+// request, so admitting a request adds no candidate memory.  What grows with
+// the admitted set is each request's own device hit buffer (8 B per hit,
+// kept until its rows are formatted).  A running request is charged the
+// larger of that buffer and a per-request reservation (hit_reserve_bytes),
+// and a waiting request is admitted only while the charges of the running
+// and finishing requests plus its own reservation fit hit_buffer_bytes;
+// nothing running always admits one.
 // Device buffers that change with the request mix are stream-ordered
 // (cudaMallocAsync / cudaFreeAsync), so no step waits for a device-wide
 // synchronisation.  While a server runs, the handle must not be used for
@@ -63,6 +72,7 @@ struct Request {
   bool ran = false;  // has completed the ring (or failed): no more hits
   DevBuf hits;       // device hit keys with request-local variant ids
   uint64_t n_hits = 0;
+  uint64_t charged = 0;  // hits.cap when handed to the finisher (server's finishing_bytes)
   cudaEvent_t last_append = nullptr;
   // result, published under the server mutex with `done`
   bool done = false;
@@ -97,6 +107,9 @@ struct cof_server {
   cof_handle* h = nullptr;
   uint64_t max_active_variants = 0;
   uint64_t hit_buffer_bytes = 0;
+  uint64_t hit_reserve_bytes = 64ull << 20;  // charged per running request at least
+  uint64_t finishing_bytes = 0;              // hit buffers handed to the finisher, not yet freed (under mu)
+  uint64_t held_hit_bytes = 0, max_held_hit_bytes = 0;  // after the latest step (under mu)
 
   std::thread worker, builder, finisher;
   std::mutex mu;
@@ -179,13 +192,22 @@ void want_build(cof_server* s) {
   s->cv_build.notify_one();
 }
 
-// True when the front pending request fits the variant budget (under mu).
+// Device bytes a running request is charged against the hit budget.  Runs
+// on the worker thread, the only thread that grows a running request's hits.
+uint64_t hit_charge(const cof_server* s, const Request& r) { return std::max<uint64_t>(r.hits.cap, s->hit_reserve_bytes); }
+
+// True when the front pending request fits the variant budget and the hit
+// memory budget (under mu, on the worker thread).
 bool admissible(const cof_server* s) {
   if (s->pending.empty()) return false;
   if (s->active.empty()) return true;
-  uint64_t used = 0;
-  for (const ReqPtr& r : s->active) used += r->nvar;
-  return used + s->pending.front()->nvar <= s->max_active_variants;
+  uint64_t used = 0, bytes = s->finishing_bytes;
+  for (const ReqPtr& r : s->active) {
+    used += r->nvar;
+    bytes += hit_charge(s, *r);
+  }
+  return used + s->pending.front()->nvar <= s->max_active_variants &&
+         bytes + s->hit_reserve_bytes <= s->hit_buffer_bytes;
 }
 
 // True when the current tables hold a request still walking the ring.
@@ -411,6 +433,10 @@ void finisher_main(cof_server* s) {
     const cof_status st = r->status ? r->status : format_request(s, *r, err);
     r->hits.st = s->fin_stream;
     r->hits.release();
+    {
+      std::lock_guard<std::mutex> lock(s->mu);
+      s->finishing_bytes -= r->charged;
+    }
     if (r->last_append) {
       cudaEventDestroy(r->last_append);
       r->last_append = nullptr;
@@ -473,6 +499,13 @@ void worker_main(cof_server* s) {
     }
     if (!tables_live(s)) continue;
     const cof_status st = run_step(s);
+    {
+      std::lock_guard<std::mutex> lock(s->mu);
+      uint64_t held = s->finishing_bytes;
+      for (const ReqPtr& r : s->active) held += r->hits.cap;
+      s->held_hit_bytes = held;
+      s->max_held_hit_bytes = std::max(s->max_held_hit_bytes, held);
+    }
     std::vector<ReqPtr> finished;
     for (const ReqPtr& r : s->tables->reqs)
       if (!r->ran && (st || ++r->steps_seen >= s->ring)) finished.push_back(r);
@@ -480,6 +513,8 @@ void worker_main(cof_server* s) {
       std::lock_guard<std::mutex> lock(s->mu);
       for (const ReqPtr& r : finished) {
         r->ran = true;
+        r->charged = r->hits.cap;  // freed by the finisher
+        s->finishing_bytes += r->charged;
         if (st) {
           r->status = st;
           r->err = h->err;
@@ -617,6 +652,23 @@ cof_status cof_server_release(cof_server* s, uint64_t ticket) {
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end() || !it->second->done) return COF_ERR_ARG;
   s->tickets.erase(it);
+  return COF_OK;
+}
+
+cof_status cof_server_set_hit_reserve(cof_server* s, uint64_t bytes) {
+  if (!s) return COF_ERR_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  s->hit_reserve_bytes = bytes;
+  return COF_OK;
+}
+
+cof_status cof_server_memory(cof_server* s, uint64_t* held_hit_bytes, uint64_t* max_held_hit_bytes,
+                             uint64_t* queue_bytes) {
+  if (!s) return COF_ERR_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  if (held_hit_bytes) *held_hit_bytes = s->held_hit_bytes;
+  if (max_held_hit_bytes) *max_held_hit_bytes = s->max_held_hit_bytes;
+  if (queue_bytes) *queue_bytes = 2 * (2 * s->seg_words * 32 * 4);
   return COF_OK;
 }
 

@@ -151,9 +151,17 @@ cof_status cof_job_rows(const cof_handle* h, uint32_t job, const char** rows, si
  * request larger than that runs alone).  A request finishes after one full
  * ring, wherever it joined.  Active requests with the same padded pattern
  * share the PAM scan and the comparer launch of each step, but each request's
- * rows are exactly those of cof_search on that input file alone.  One step's
- * hits must fit `hit_buffer_bytes` (0 = 8 GiB).  While a server runs, use the
- * handle only through server calls; submit/wait/release are thread-safe. */
+ * rows are exactly those of cof_search on that input file alone.
+ * Memory: the candidate queues are sized by the ring segment and shared by
+ * all requests, so admission adds no candidate memory; each running request
+ * holds a device hit buffer (8 B per hit) until its rows are formatted.  A
+ * request is charged the larger of its hit buffer and a reservation (64 MiB
+ * unless cof_server_set_hit_reserve says otherwise), and a waiting request is
+ * admitted only while the charges of the running and finishing requests plus
+ * its own reservation fit `hit_buffer_bytes` (0 = 8 GiB); nothing running
+ * always admits one.  One step's hits must fit `hit_buffer_bytes` as well.
+ * While a server runs, use the handle only through server calls;
+ * submit/wait/release are thread-safe. */
 typedef struct cof_server cof_server;
 /* `segment_positions` sets the ring's granularity (rounded down to a multiple
  * of 32, at most 2^26 = the default for 0): smaller segments let requests join
@@ -171,6 +179,13 @@ cof_status cof_server_wait(cof_server* s, uint64_t ticket, int timeout_ms, const
 cof_status cof_server_release(cof_server* s, uint64_t ticket);
 cof_status cof_server_stats(cof_server* s, uint64_t* steps, uint64_t* admitted, uint64_t* completed,
                             uint64_t* pending, uint64_t* active, uint64_t* max_active);
+/* Hit memory charged per running request at least (default 64 MiB); applies
+ * to admissions after the call. */
+cof_status cof_server_set_hit_reserve(cof_server* s, uint64_t bytes);
+/* Device bytes of request hit buffers after the latest ring step, their
+ * maximum so far, and the bytes of the two shared candidate queues. */
+cof_status cof_server_memory(cof_server* s, uint64_t* held_hit_bytes, uint64_t* max_held_hit_bytes,
+                             uint64_t* queue_bytes);
 const char* cof_server_last_error(cof_server* s);
 /* Stops the worker; requests not finished end with COF_ERR_STATE. */
 void cof_server_stop(cof_server* s);

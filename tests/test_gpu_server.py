@@ -74,6 +74,31 @@ def test_server_mix_equals_alone(P, built, oracle, tmp_path):
                 assert P.HEADER.encode() + rows == want[j], f"request {j} alone"
 
 
+def test_server_admits_by_hit_memory(P, built, oracle, tmp_path):
+    """Admission by device memory: each running request is charged at least
+    its hit reservation against hit_buffer_bytes, so a reservation of half the
+    budget lets at most two requests run together, and one of the whole budget
+    only one; the rows stay those of each input file alone."""
+    genome, texts = make_genome_and_requests(P, tmp_path)
+    texts = texts[:6]
+    want = oracle_rows(oracle, tmp_path, texts)
+    budget = 1 << 20
+    with P.CasOFFinder(0) as eng:
+        eng.load_genome_file(genome)
+        for reserve, most in ((budget // 2, 2), (budget, 1)):
+            with P.Server(eng, hit_buffer_bytes=budget, segment_positions=1 << 15) as srv:
+                srv.set_hit_reserve(reserve)
+                tickets = [srv.submit(t) for t in texts]
+                got = [srv.wait(t) for t in tickets]
+                stats, mem = srv.stats(), srv.memory()
+            for j, (rows, _) in enumerate(got):
+                assert P.HEADER.encode() + rows == want[j], f"request {j}, reservation {reserve}"
+            assert stats["completed"] == len(texts)
+            assert 1 <= stats["max_active"] <= most, stats
+            assert mem["queue_bytes"] == 2 * 2 * (1 << 15) * 4  # two queues, two entries per position
+            assert 0 < mem["max_held_hit_bytes"] <= budget
+
+
 def test_server_rejects_bad_input_and_times_out_cleanly(P, built, tmp_path):
     genome, texts = make_genome_and_requests(P, tmp_path)
     with P.CasOFFinder(0) as eng:
