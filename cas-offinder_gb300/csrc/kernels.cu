@@ -50,8 +50,10 @@ __device__ __forceinline__ uint32_t bits_at(uint32_t w0, uint32_t w1, uint32_t w
 // all of a lane's words are loaded before any is tested, to keep many loads
 // in flight.  A warp's candidates (up to kFinderStage) are staged in shared
 // memory in scan order, then written to the queue with one atomic
-// reservation and coalesced stores; a warp with more candidates (dense
-// patterns) stores them directly.
+// reservation and coalesced 16-byte stores (the staged entries start at the
+// queue position's offset within a 16-byte line, so source and destination
+// line up); a warp with more candidates (dense patterns) stores them
+// directly.
 constexpr int kFinderThreads = 128;
 constexpr int kFinderWords = 4;     // plane words per lane per pass
 constexpr int kFinderStage = 1024;  // staged entries per warp; denser warps store directly
@@ -79,9 +81,11 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     uint64_t w_begin, uint64_t w_end, uint64_t pos_end, const __grid_constant__ FinderMasks pat,
     uint32_t* __restrict__ queue, uint32_t* __restrict__ qcount) {
   constexpr int K = kFinderWords;
-  __shared__ uint32_t stage[kFinderThreads / 32][kFinderStage];
+  // Four words of room for the queue's phase; rows stay 16-byte aligned.
+  __shared__ __align__(16) uint32_t stage[kFinderThreads / 32][kFinderStage + 4];
   const unsigned lane = threadIdx.x & 31;
   uint32_t* my = stage[threadIdx.x >> 5];
+  const bool vec_queue = ((uintptr_t)queue & 15u) == 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * K;
   for (uint64_t wb = w_begin + ((uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u)) * K; wb < w_end;
        wb += stride) {
@@ -99,26 +103,36 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
       }
     }
     static_assert(K % 2 == 0, "counts are scanned two per word");
+    // Pattern position outer, word inner: each position's offset and class
+    // masks are read once per pass.
+    uint32_t badf[K], badr[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) badf[k] = badr[k] = 0;
+    for (uint32_t j = 0; j < pat.nf; ++j) {
+      const unsigned q = pat.fk[j];
+      const uint32_t mt = pat.fm[j][0], mc = pat.fm[j][1], ma = pat.fm[j][2], mg = pat.fm[j][3], mo = pat.fm[j][4];
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        badf[k] |= mismatch_word(window_bits<NK>(h[k][0], h[k][1], h[k][NK], q),
+                                 window_bits<NK>(l[k][0], l[k][1], l[k][NK], q),
+                                 window_bits<NK>(o[k][0], o[k][1], o[k][NK], q), mt, mc, ma, mg, mo);
+    }
+    for (uint32_t j = 0; j < pat.nr; ++j) {
+      const unsigned q = pat.rk[j];
+      const uint32_t mt = pat.rm[j][0], mc = pat.rm[j][1], ma = pat.rm[j][2], mg = pat.rm[j][3], mo = pat.rm[j][4];
+#pragma unroll
+      for (int k = 0; k < K; ++k)
+        badr[k] |= mismatch_word(window_bits<NK>(h[k][0], h[k][1], h[k][NK], q),
+                                 window_bits<NK>(l[k][0], l[k][1], l[k][NK], q),
+                                 window_bits<NK>(o[k][0], o[k][1], o[k][NK], q), mt, mc, ma, mg, mo);
+    }
     uint32_t fwd[K], rev[K], cnt[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
       const uint32_t h0 = h[k][0], h1 = h[k][1], h2 = NK == 1 ? 0u : h[k][NK];
       const uint32_t l0 = l[k][0], l1 = l[k][1], l2 = NK == 1 ? 0u : l[k][NK];
       const uint32_t o0 = o[k][0], o1 = o[k][1], o2 = NK == 1 ? 0u : o[k][NK];
-      uint32_t badf = 0, badr = 0;
-      for (uint32_t j = 0; j < pat.nf; ++j) {
-        const unsigned q = pat.fk[j];
-        badf |= mismatch_word(window_bits<NK>(h0, h1, h2, q), window_bits<NK>(l0, l1, l2, q),
-                              window_bits<NK>(o0, o1, o2, q), pat.fm[j][0], pat.fm[j][1], pat.fm[j][2],
-                              pat.fm[j][3], pat.fm[j][4]);
-      }
-      for (uint32_t j = 0; j < pat.nr; ++j) {
-        const unsigned q = pat.rk[j];
-        badr |= mismatch_word(window_bits<NK>(h0, h1, h2, q), window_bits<NK>(l0, l1, l2, q),
-                              window_bits<NK>(o0, o1, o2, q), pat.rm[j][0], pat.rm[j][1], pat.rm[j][2],
-                              pat.rm[j][3], pat.rm[j][4]);
-      }
-      uint32_t f = ~badf, r = ~badr;
+      uint32_t f = ~badf[k], r = ~badr[k];
       // Words past w_end (loaded as zeros) test nothing; and only windows
       // that end inside the genome count: start < n - L + 1, whatever the
       // plane bits past the end hold.
@@ -191,7 +205,30 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
         }
       }
     };
-    if (total <= (uint32_t)kFinderStage) {  // warp-uniform
+    if (total <= (uint32_t)kFinderStage && vec_queue) {  // warp-uniform
+      // Entry i is staged at my[ph + i], so staged word w and queue word
+      // base - ph + w share their offset within a 16-byte line.  Whole lines
+      // are stored as uint4; the first and last lines, which the warp may
+      // share with others, word by word.
+      const uint32_t ph = base & 3u;
+      emit(my + ph);
+      __syncwarp();
+      const uint32_t nv = (ph + total + 3) / 4;
+      const uint4* src = reinterpret_cast<const uint4*>(my);
+      uint32_t* q0 = queue + (base - ph);
+      for (uint32_t v = lane; v < nv; v += 32) {
+        const uint4 x = src[v];
+        if (v > 0 && v + 1 < nv) {
+          reinterpret_cast<uint4*>(q0)[v] = x;
+        } else {
+          const uint32_t w0 = 4 * v, xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+          for (uint32_t c = 0; c < 4; ++c)
+            if (w0 + c >= ph && w0 + c < ph + total) q0[w0 + c] = xs[c];
+        }
+      }
+      __syncwarp();
+    } else if (total <= (uint32_t)kFinderStage) {
       emit(my);
       __syncwarp();
       for (uint32_t i = lane; i < total; i += 32) queue[base + i] = my[i];
