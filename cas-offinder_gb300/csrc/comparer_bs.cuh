@@ -170,6 +170,82 @@ __device__ __forceinline__ void unstage(RawWindow<NK>& r, const uint32_t* st, ui
   }
 }
 
+// Window words of one pair (entry ea -> group a, eb -> group b), copied into
+// shared memory asynchronously.  The 64 entries are consecutive in the queue,
+// which the finder fills in genome order, so their windows nearly always lie
+// within a few plane words: when every window lies in [w0, w0 + 32), lane l
+// copies word w0 + l of each plane (three copies of consecutive words per
+// warp; a gather of each lane's own words would copy the same few words many
+// times over, one L1 wavefront per distinct word) and `meta` records w0.
+// Otherwise -- a pair where two finder warps' queue ranges meet, or windows
+// spread out around a run of N -- each lane copies its own candidates' words
+// into its slots and `meta` records kNoWindow.  Only the words the windows
+// cover are read.  The same warp reads `meta` back after the copies land.
+constexpr uint32_t kNoWindow = 0xFFFFFFFFu;
+constexpr int kWindowWords = 32;  // per plane
+constexpr int kCoopWords = 4 * kWindowWords;  // per warp: three planes, then meta
+
+// The pair's entries go to `ents` (its 64 entry slots), where unstage_pair
+// reads them back, so they hold no registers while the current tile is
+// counted.
+template <int NK>
+__device__ __forceinline__ void stage_pair(uint32_t coop, uint32_t* meta, uint32_t dst_a, uint32_t dst_b, uint32_t kS,
+                                           const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo,
+                                           const uint32_t* __restrict__ ot, uint32_t ea, uint32_t eb,
+                                           uint64_t seg_pos0, unsigned lane, uint32_t* ents) {
+  ents[lane] = ea;
+  ents[32 + lane] = eb;
+  // Plane word of each window's first position (< 2^31 for genomes below 2^36 positions).
+  const bool ha = ea != 0xFFFFFFFFu, hb = eb != 0xFFFFFFFFu;
+  const uint32_t wa = (uint32_t)((seg_pos0 + (ea >> 1)) >> 5), wb = (uint32_t)((seg_pos0 + (eb >> 1)) >> 5);
+  const uint32_t w0 = __reduce_min_sync(kFull, min(ha ? wa : 0xFFFFFFFFu, hb ? wb : 0xFFFFFFFFu));
+  const uint32_t w1 = __reduce_max_sync(kFull, max(ha ? wa : 0u, hb ? wb : 0u)) + NK;  // last word read
+  if (w0 != 0xFFFFFFFFu && w1 - w0 < (uint32_t)kWindowWords) {  // warp-uniform
+    const uint32_t w = w0 + lane;
+    const uint32_t bytes = w <= w1 ? 4u : 0u;
+    const uint32_t ws = bytes ? w : w0;
+    cp_async4(coop + (0 * kWindowWords + lane) * 4, hi + ws, bytes);
+    cp_async4(coop + (1 * kWindowWords + lane) * 4, lo + ws, bytes);
+    cp_async4(coop + (2 * kWindowWords + lane) * 4, ot + ws, bytes);
+    if (lane == 0) *meta = w0;
+  } else {
+    stage_planes<NK>(dst_a, kS, hi, lo, ot, ea, seg_pos0);
+    stage_planes<NK>(dst_b, kS, hi, lo, ot, eb, seg_pos0);
+    if (lane == 0) *meta = kNoWindow;
+  }
+}
+
+// Reads back the pair staged by stage_pair (call after cp_async_wait_all):
+// each lane waited for its own copies; the warp barrier makes the other
+// lanes' copies and `meta` visible.  Entries past the end of the queue read
+// word w0 (their windows are never reported).
+template <int NK>
+__device__ __forceinline__ void unstage_pair(RawWindow<NK>& ra, RawWindow<NK>& rb, const uint32_t* coop_w,
+                                             const uint32_t* meta, const uint32_t* st, uint32_t kS,
+                                             const uint32_t* ents, unsigned lane, uint64_t seg_pos0) {
+  __syncwarp();
+  const uint32_t w0 = *meta;
+  const uint32_t ea = ents[lane], eb = ents[32 + lane];
+  if (w0 != kNoWindow) {
+    const uint32_t ia = ea != 0xFFFFFFFFu ? (uint32_t)((seg_pos0 + (ea >> 1)) >> 5) - w0 : 0u;
+    const uint32_t ib = eb != 0xFFFFFFFFu ? (uint32_t)((seg_pos0 + (eb >> 1)) >> 5) - w0 : 0u;
+    ra.e = ea;
+    rb.e = eb;
+#pragma unroll
+    for (int i = 0; i <= NK; ++i) {
+      ra.h[i] = coop_w[0 * kWindowWords + ia + i];
+      ra.l[i] = coop_w[1 * kWindowWords + ia + i];
+      ra.o[i] = coop_w[2 * kWindowWords + ia + i];
+      rb.h[i] = coop_w[0 * kWindowWords + ib + i];
+      rb.l[i] = coop_w[1 * kWindowWords + ib + i];
+      rb.o[i] = coop_w[2 * kWindowWords + ib + i];
+    }
+  } else {
+    unstage<NK>(ra, st, kS, ea);
+    unstage<NK>(rb, st + Stage<NK>::kSlots * kS, kS, eb);
+  }
+}
+
 // The window of one candidate, strand-oriented: positions 0..L-1 in bits
 // 0..L-1 of (h, l, o) words; a '-' strand window is the reverse complement.
 template <int NK>
@@ -215,15 +291,14 @@ struct TableRows {
 
 // Builds pair p of a tile from two groups of candidates (`ra` -> .x, `rb` ->
 // .y): oriented windows, transposed, expanded to class words in `pt` (the
-// pair's table, [row][ROW] uint2) and candidate entries in `ents` (64).
+// pair's table, [row][ROW] uint2).  The pair's entries are already in its
+// entry slots (stage_pair).
 template <int NK, int ROW, bool CONC>
 __device__ __forceinline__ void build_pair(const RawWindow<NK>& ra, const RawWindow<NK>& rb, uint64_t seg_pos0,
-                                           uint32_t L, unsigned lane, uint2* pt, uint32_t* ents) {
+                                           uint32_t L, unsigned lane, uint2* pt) {
   uint32_t ha[NK], la[NK], oa[NK], hb[NK], lb[NK], ob[NK];
   orient<NK>(ra, seg_pos0, L, ha, la, oa);
   orient<NK>(rb, seg_pos0, L, hb, lb, ob);
-  ents[lane] = ra.e;
-  ents[32 + lane] = rb.e;
 #pragma unroll
   for (int i = 0; i < NK; ++i) {
     const uint32_t h0 = warp_transpose(ha[i], lane), h1 = warp_transpose(hb[i], lane);
@@ -487,11 +562,12 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
 }
 
 // Shared memory of a CTA of W warps: two table buffers of W pairs, their
-// candidate entries, and the staging slots.
+// candidate entries, the per-thread staging slots and the per-warp window
+// copies (with their meta word).
 template <int ROW, int NK, bool CONC>
 __host__ __device__ constexpr size_t bs_smem_bytes(unsigned W) {
   return 2 * ((size_t)W * TableRows<CONC>::kRows * ROW * sizeof(uint2) + W * 64 * 4) +
-         2 * Stage<NK>::kSlots * (32 * W) * 4;
+         2 * Stage<NK>::kSlots * (32 * W) * 4 + (size_t)W * kCoopWords * 4;
 }
 
 template <int S, int ROW, int NK, bool CONC, bool ONE>
@@ -518,6 +594,8 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   const uint32_t* stage = ents_all + 2 * W * 64 + threadIdx.x;
   const uint32_t stage_a = (uint32_t)__cvta_generic_to_shared(stage);
   const uint32_t stage_b = stage_a + Stage<NK>::kSlots * kS * 4;
+  // This warp's window copies: the three planes, then the meta word.
+  auto coop_words = [&]() { return ents_all + 2 * W * 64 + 2 * Stage<NK>::kSlots * kS + warp * kCoopWords; };
   const uint32_t words = 1 + S / 2 + 2 * (m / 2);  // per lane program
 
   // Row 0 (pattern bytes that never mismatch: padding slots) stays zero.
@@ -544,17 +622,20 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   if (resident && warp < chunks)
     load_program<S>(prog + (size_t)warp * words * 32 + lane, table_base, addr, kmask, kadd, first_on);
   // Entries: e* of the tile being staged, n* of the tile after it.
-  uint32_t ea = load_entry(queue, t * tile_n + ca, n), eb = load_entry(queue, t * tile_n + cb, n);
-  stage_planes<NK>(stage_a, kS * 4, hi, lo, ot, ea, seg_pos0);
-  stage_planes<NK>(stage_b, kS * 4, hi, lo, ot, eb, seg_pos0);
+  {
+    uint32_t* cw = coop_words();
+    stage_pair<NK>((uint32_t)__cvta_generic_to_shared(cw), cw + 3 * kWindowWords, stage_a, stage_b, kS * 4, hi, lo,
+                   ot, load_entry(queue, t * tile_n + ca, n), load_entry(queue, t * tile_n + cb, n), seg_pos0, lane,
+                   ents_all + warp * 64);
+  }
   uint32_t na = load_entry(queue, tn * tile_n + ca, n);
   uint32_t nb = load_entry(queue, tn * tile_n + cb, n);
   cp_async_wait_all();
   if (t < ntiles) {
     RawWindow<NK> ra, rb;
-    unstage<NK>(ra, stage, kS, ea);
-    unstage<NK>(rb, stage + Stage<NK>::kSlots * kS, kS, eb);
-    build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + warp * kPairWords, ents_all + warp * 64);
+    const uint32_t* cw = coop_words();
+    unstage_pair<NK>(ra, rb, cw, cw + 3 * kWindowWords, stage, kS, ents_all + warp * 64, lane, seg_pos0);
+    build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + warp * kPairWords);
   }
   if (threadIdx.x == 0) claimed[0] = claim;
   __syncthreads();
@@ -564,10 +645,11 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   while (t < ntiles) {
     const uint32_t tnn = claimed[par];  // the tile after tn
     if (threadIdx.x == 0) claim = 2 * gridDim.x + atomicAdd(tile_ctr, 1u);
-    ea = na;
-    eb = nb;
-    stage_planes<NK>(stage_a, kS * 4, hi, lo, ot, ea, seg_pos0);
-    stage_planes<NK>(stage_b, kS * 4, hi, lo, ot, eb, seg_pos0);
+    {
+      uint32_t* cw = coop_words();
+      stage_pair<NK>((uint32_t)__cvta_generic_to_shared(cw), cw + 3 * kWindowWords, stage_a, stage_b, kS * 4, hi,
+                     lo, ot, na, nb, seg_pos0, lane, ents_all + (cur ^ 1) * (W * 64) + warp * 64);
+    }
     na = load_entry(queue, tnn * tile_n + ca, n);
     nb = load_entry(queue, tnn * tile_n + cb, n);
     const uint32_t* ents = ents_all + cur * (W * 64);
@@ -583,10 +665,10 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     cp_async_wait_all();
     if (tn < ntiles) {
       RawWindow<NK> ra, rb;
-      unstage<NK>(ra, stage, kS, ea);
-      unstage<NK>(rb, stage + Stage<NK>::kSlots * kS, kS, eb);
-      build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + (cur ^ 1) * kBufWords + warp * kPairWords,
-                                ents_all + (cur ^ 1) * (W * 64) + warp * 64);
+      const uint32_t* cw = coop_words();
+      unstage_pair<NK>(ra, rb, cw, cw + 3 * kWindowWords, stage, kS, ents_all + (cur ^ 1) * (W * 64) + warp * 64,
+                       lane, seg_pos0);
+      build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + (cur ^ 1) * kBufWords + warp * kPairWords);
     }
     if (threadIdx.x == 0) claimed[par ^ 1] = claim;
     __syncthreads();
