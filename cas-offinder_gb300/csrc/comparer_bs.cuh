@@ -519,12 +519,16 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
     // Where registers allow, both steps' class words are loaded before the
     // first is applied (four shared loads in flight instead of two); the
     // 72-register instance would spill for it.
+    // A program of up to m variants has at most m - 1 steps: (m - 1) / 2
+    // pairs, then one step alone when m - 1 is odd (the pair layout's last
+    // slot is padding then).
     constexpr bool kBoth = MaxRegs<S, NK>::value > 72;
-    const uint32_t sp = m / 2;
-    uint2 wn = __ldg(steps);
+    const uint32_t ns = m - 1, sp = ns / 2;
+    uint2 wn = make_uint2(0u, 0u);
+    if (ns) wn = __ldg(steps);
     for (uint32_t j = 0; j < sp; ++j) {
       const uint2 w2 = wn;
-      if (j + 1 < sp) wn = __ldg(steps + (j + 1) * 32);
+      if (2 * (j + 1) < ns) wn = __ldg(steps + (j + 1) * 32);
       uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
       lds64<0>(pbase + (w2.x & 0x7FFFu), a0, a1);
       lds64<0>(pbase + (w2.x >> 16), b0, b1);
@@ -538,6 +542,12 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
         lds64<0>(pbase + (w2.y >> 16), d0, d1);
       }
       step(w2.y, 2 * j + 1, c0, c1, d0, d1);
+    }
+    if (ns & 1) {
+      uint32_t a0, a1, b0, b1;
+      lds64<0>(pbase + (wn.x & 0x7FFFu), a0, a1);
+      lds64<0>(pbase + (wn.x >> 16), b0, b1);
+      step(wn.x, ns - 1, a0, a1, b0, b1);
     }
   }
 }
