@@ -503,22 +503,28 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
     // entry st + 1 of the lane's id list.  A candidate passes while the top
     // plane is clear, so a step has hits when the flag is set and some
     // candidate of the pair has that plane clear.
+    auto emit_step = [&](bool any, uint32_t st) {
+      const uint32_t on = any ? kFull : 0u;
+      const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
+      const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
+      emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+    };
     auto step = [&](uint32_t w, uint32_t st, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
       step_update<NB + 1>(pa, a0, b0);
       step_update<NB + 1>(pb, a1, b1);
       const bool any = (w & 0x8000u) && (pa[NB] & pb[NB]) != kFull;
-      if (__any_sync(kFull, any)) {
-        const uint32_t on = any ? kFull : 0u;
-        const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
-        const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
-        emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-        emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
-      }
+      if (__any_sync(kFull, any)) emit_step(any, st);
     };
     // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
-    // Where registers allow, both steps' class words are loaded before the
-    // first is applied (four shared loads in flight instead of two); the
-    // 72-register instance would spill for it.
+    // Where registers allow (kBoth), both steps' class words are loaded
+    // before the first is applied (four shared loads in flight instead of
+    // two), and the pair's two steps share one vote: t0 & t1 (the top planes
+    // after each step) has a clear bit exactly when some candidate passed
+    // either step.  In that rare case the second step is undone (+b - a is
+    // the exact inverse of +a - b) to report the first step's hits, then
+    // redone.  The 72-register instance would spill for either, so it loads
+    // and votes step by step.
     // A program of up to m variants has at most m - 1 steps: (m - 1) / 2
     // pairs, then one step alone when m - 1 is odd (the pair layout's last
     // slot is padding then).
@@ -535,13 +541,30 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
       if constexpr (kBoth) {
         lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
         lds64<0>(pbase + (w2.y >> 16), d0, d1);
-      }
-      step(w2.x, 2 * j, a0, a1, b0, b1);
-      if constexpr (!kBoth) {
+        step_update<NB + 1>(pa, a0, b0);
+        step_update<NB + 1>(pb, a1, b1);
+        const uint32_t t0 = pa[NB] & pb[NB];
+        step_update<NB + 1>(pa, c0, d0);
+        step_update<NB + 1>(pb, c1, d1);
+        const uint32_t t1 = pa[NB] & pb[NB];
+        if (__any_sync(kFull, (t0 & t1) != kFull)) {
+          const bool e0 = (w2.x & 0x8000u) && t0 != kFull;
+          const bool e1 = (w2.y & 0x8000u) && t1 != kFull;
+          if (__any_sync(kFull, e0)) {
+            step_update<NB + 1>(pa, d0, c0);
+            step_update<NB + 1>(pb, d1, c1);
+            emit_step(e0, 2 * j);
+            step_update<NB + 1>(pa, c0, d0);
+            step_update<NB + 1>(pb, c1, d1);
+          }
+          if (__any_sync(kFull, e1)) emit_step(e1, 2 * j + 1);
+        }
+      } else {
+        step(w2.x, 2 * j, a0, a1, b0, b1);
         lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
         lds64<0>(pbase + (w2.y >> 16), d0, d1);
+        step(w2.y, 2 * j + 1, c0, c1, d0, d1);
       }
-      step(w2.y, 2 * j + 1, c0, c1, d0, d1);
     }
     if (ns & 1) {
       uint32_t a0, a1, b0, b1;
