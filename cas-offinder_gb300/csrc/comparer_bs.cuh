@@ -415,11 +415,13 @@ __device__ __forceinline__ void step_update(uint32_t (&p)[NP], uint32_t a, uint3
   }
 }
 
-// Registers per thread: 72 lets four 224-thread (or seven 128-thread) CTAs
-// share an SM; wider slot lists get more.
+// Registers per thread: 80 lets 25 one-warp CTAs (or three 256-thread CTAs)
+// share an SM; wider slot lists get more.  (A 72-register budget, 28 one-warp
+// CTAs, spilled once both steps of a pair were loaded ahead and measured
+// slower.)
 template <int S, int NK>
 struct MaxRegs {
-  static constexpr int value = (S > 16 && S <= 20 && NK == 1) ? 72 : (S <= 20 ? 80 : S <= 28 ? 96 : 104);
+  static constexpr int value = S <= 20 ? 80 : S <= 28 ? 96 : 104;
 };
 
 // The full count of a lane program's first variant on pair P: its S class
@@ -517,18 +519,15 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
       if (__any_sync(kFull, any)) emit_step(any, st);
     };
     // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
-    // Where registers allow (kBoth), both steps' class words are loaded
-    // before the first is applied (four shared loads in flight instead of
-    // two), and the pair's two steps share one vote: t0 & t1 (the top planes
-    // after each step) has a clear bit exactly when some candidate passed
-    // either step.  In that rare case the second step is undone (+b - a is
-    // the exact inverse of +a - b) to report the first step's hits, then
-    // redone.  The 72-register instance would spill for either, so it loads
-    // and votes step by step.
+    // Both steps' class words are loaded before the first is applied (four
+    // shared loads in flight instead of two), and the pair's two steps share
+    // one vote: t0 & t1 (the top planes after each step) has a clear bit
+    // exactly when some candidate passed either step.  In that rare case the
+    // second step is undone (+b - a is the exact inverse of +a - b) to report
+    // the first step's hits, then redone.
     // A program of up to m variants has at most m - 1 steps: (m - 1) / 2
     // pairs, then one step alone when m - 1 is odd (the pair layout's last
     // slot is padding then).
-    constexpr bool kBoth = MaxRegs<S, NK>::value > 72;
     const uint32_t ns = m - 1, sp = ns / 2;
     uint2 wn = make_uint2(0u, 0u);
     if (ns) wn = __ldg(steps);
@@ -538,32 +537,25 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
       uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
       lds64<0>(pbase + (w2.x & 0x7FFFu), a0, a1);
       lds64<0>(pbase + (w2.x >> 16), b0, b1);
-      if constexpr (kBoth) {
-        lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
-        lds64<0>(pbase + (w2.y >> 16), d0, d1);
-        step_update<NB + 1>(pa, a0, b0);
-        step_update<NB + 1>(pb, a1, b1);
-        const uint32_t t0 = pa[NB] & pb[NB];
-        step_update<NB + 1>(pa, c0, d0);
-        step_update<NB + 1>(pb, c1, d1);
-        const uint32_t t1 = pa[NB] & pb[NB];
-        if (__any_sync(kFull, (t0 & t1) != kFull)) {
-          const bool e0 = (w2.x & 0x8000u) && t0 != kFull;
-          const bool e1 = (w2.y & 0x8000u) && t1 != kFull;
-          if (__any_sync(kFull, e0)) {
-            step_update<NB + 1>(pa, d0, c0);
-            step_update<NB + 1>(pb, d1, c1);
-            emit_step(e0, 2 * j);
-            step_update<NB + 1>(pa, c0, d0);
-            step_update<NB + 1>(pb, c1, d1);
-          }
-          if (__any_sync(kFull, e1)) emit_step(e1, 2 * j + 1);
+      lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
+      lds64<0>(pbase + (w2.y >> 16), d0, d1);
+      step_update<NB + 1>(pa, a0, b0);
+      step_update<NB + 1>(pb, a1, b1);
+      const uint32_t t0 = pa[NB] & pb[NB];
+      step_update<NB + 1>(pa, c0, d0);
+      step_update<NB + 1>(pb, c1, d1);
+      const uint32_t t1 = pa[NB] & pb[NB];
+      if (__any_sync(kFull, (t0 & t1) != kFull)) {
+        const bool e0 = (w2.x & 0x8000u) && t0 != kFull;
+        const bool e1 = (w2.y & 0x8000u) && t1 != kFull;
+        if (__any_sync(kFull, e0)) {
+          step_update<NB + 1>(pa, d0, c0);
+          step_update<NB + 1>(pb, d1, c1);
+          emit_step(e0, 2 * j);
+          step_update<NB + 1>(pa, c0, d0);
+          step_update<NB + 1>(pb, c1, d1);
         }
-      } else {
-        step(w2.x, 2 * j, a0, a1, b0, b1);
-        lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
-        lds64<0>(pbase + (w2.y >> 16), d0, d1);
-        step(w2.y, 2 * j + 1, c0, c1, d0, d1);
+        if (__any_sync(kFull, e1)) emit_step(e1, 2 * j + 1);
       }
     }
     if (ns & 1) {
