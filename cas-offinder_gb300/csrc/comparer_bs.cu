@@ -47,6 +47,7 @@ bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32
                         uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,
                         unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream) {
   if (chunks == 0) return true;
+  if (seg_pos0 & 31) return false;  // the kernels address windows from the segment's first plane word
 #define COF_BS_ROW(ROWV, NKV)                                                                                       \
   return concrete_only ? dispatch_s<ROWV, NKV, true>(slots, g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L,  \
                                                       tile_ctr, hits, hit_count, hit_cap, sm_count, stream)         \

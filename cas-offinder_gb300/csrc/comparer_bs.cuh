@@ -146,9 +146,9 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 template <int NK>
 __device__ __forceinline__ void stage_planes(uint32_t dst, uint32_t kS, const uint32_t* __restrict__ hi,
                                              const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
-                                             uint32_t e, uint64_t seg_pos0) {
+                                             uint32_t e, uint32_t seg_w0) {
   const bool have = e != 0xFFFFFFFFu;
-  const uint64_t w = have ? (seg_pos0 + (e >> 1)) >> 5 : 0;
+  const uint32_t w = have ? seg_w0 + (e >> 6) : 0u;
   const uint32_t bytes = have ? 4u : 0u;
 #pragma unroll
   for (int i = 0; i <= NK; ++i) {
@@ -192,12 +192,12 @@ template <int NK>
 __device__ __forceinline__ void stage_pair(uint32_t coop, uint32_t* meta, uint32_t dst_a, uint32_t dst_b, uint32_t kS,
                                            const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo,
                                            const uint32_t* __restrict__ ot, uint32_t ea, uint32_t eb,
-                                           uint64_t seg_pos0, unsigned lane, uint32_t* ents) {
+                                           uint32_t seg_w0, unsigned lane, uint32_t* ents) {
   ents[lane] = ea;
   ents[32 + lane] = eb;
   // Plane word of each window's first position (< 2^31 for genomes below 2^36 positions).
   const bool ha = ea != 0xFFFFFFFFu, hb = eb != 0xFFFFFFFFu;
-  const uint32_t wa = (uint32_t)((seg_pos0 + (ea >> 1)) >> 5), wb = (uint32_t)((seg_pos0 + (eb >> 1)) >> 5);
+  const uint32_t wa = seg_w0 + (ea >> 6), wb = seg_w0 + (eb >> 6);
   const uint32_t w0 = __reduce_min_sync(kFull, min(ha ? wa : 0xFFFFFFFFu, hb ? wb : 0xFFFFFFFFu));
   const uint32_t w1 = __reduce_max_sync(kFull, max(ha ? wa : 0u, hb ? wb : 0u)) + NK;  // last word read
   if (w0 != 0xFFFFFFFFu && w1 - w0 < (uint32_t)kWindowWords) {  // warp-uniform
@@ -209,8 +209,8 @@ __device__ __forceinline__ void stage_pair(uint32_t coop, uint32_t* meta, uint32
     cp_async4(coop + (2 * kWindowWords + lane) * 4, ot + ws, bytes);
     if (lane == 0) *meta = w0;
   } else {
-    stage_planes<NK>(dst_a, kS, hi, lo, ot, ea, seg_pos0);
-    stage_planes<NK>(dst_b, kS, hi, lo, ot, eb, seg_pos0);
+    stage_planes<NK>(dst_a, kS, hi, lo, ot, ea, seg_w0);
+    stage_planes<NK>(dst_b, kS, hi, lo, ot, eb, seg_w0);
     if (lane == 0) *meta = kNoWindow;
   }
 }
@@ -222,13 +222,13 @@ __device__ __forceinline__ void stage_pair(uint32_t coop, uint32_t* meta, uint32
 template <int NK>
 __device__ __forceinline__ void unstage_pair(RawWindow<NK>& ra, RawWindow<NK>& rb, const uint32_t* coop_w,
                                              const uint32_t* meta, const uint32_t* st, uint32_t kS,
-                                             const uint32_t* ents, unsigned lane, uint64_t seg_pos0) {
+                                             const uint32_t* ents, unsigned lane, uint32_t seg_w0) {
   __syncwarp();
   const uint32_t w0 = *meta;
   const uint32_t ea = ents[lane], eb = ents[32 + lane];
   if (w0 != kNoWindow) {
-    const uint32_t ia = ea != 0xFFFFFFFFu ? (uint32_t)((seg_pos0 + (ea >> 1)) >> 5) - w0 : 0u;
-    const uint32_t ib = eb != 0xFFFFFFFFu ? (uint32_t)((seg_pos0 + (eb >> 1)) >> 5) - w0 : 0u;
+    const uint32_t ia = ea != 0xFFFFFFFFu ? seg_w0 + (ea >> 6) - w0 : 0u;
+    const uint32_t ib = eb != 0xFFFFFFFFu ? seg_w0 + (eb >> 6) - w0 : 0u;
     ra.e = ea;
     rb.e = eb;
 #pragma unroll
@@ -246,20 +246,23 @@ __device__ __forceinline__ void unstage_pair(RawWindow<NK>& ra, RawWindow<NK>& r
   }
 }
 
-// The window of one candidate, strand-oriented: positions 0..L-1 in bits
-// 0..L-1 of (h, l, o) words; a '-' strand window is the reverse complement.
+// The window of one candidate: positions 0..L-1 in bits 0..L-1 of (h, l, o)
+// words (a segment starts on a plane word, so the window's first position is
+// bit (e >> 1) & 31 of its first word).  NK > 1: a '-' strand window is turned
+// into its reverse complement here; NK == 1 windows are turned after the
+// transpose (build_pair), for the whole group at once.
 template <int NK>
-__device__ __forceinline__ void orient(const RawWindow<NK>& raw, uint64_t seg_pos0, uint32_t L, uint32_t (&hw)[NK],
-                                       uint32_t (&lw)[NK], uint32_t (&ow)[NK]) {
+__device__ __forceinline__ void orient(const RawWindow<NK>& raw, uint32_t L, uint32_t (&hw)[NK], uint32_t (&lw)[NK],
+                                       uint32_t (&ow)[NK]) {
   const bool have = raw.e != 0xFFFFFFFFu;
-  const unsigned r = have ? (unsigned)((seg_pos0 + (raw.e >> 1)) & 31) : 0u;
+  const unsigned r = (raw.e >> 1) & 31;
 #pragma unroll
   for (int i = 0; i < NK; ++i) {
     hw[i] = __funnelshift_r(raw.h[i], raw.h[i + 1], r);
     lw[i] = __funnelshift_r(raw.l[i], raw.l[i + 1], r);
     ow[i] = __funnelshift_r(raw.o[i], raw.o[i + 1], r);
   }
-  if (have && (raw.e & 1)) {
+  if (NK > 1 && have && (raw.e & 1)) {
     // Reverse complement: reverse the L positions, flip hi of bases.
     if (NK == 1) {
       const unsigned sh = 32 - L;
@@ -294,21 +297,40 @@ struct TableRows {
 // pair's table, [row][ROW] uint2).  The pair's entries are already in its
 // entry slots (stage_pair).
 template <int NK, int ROW, bool CONC>
-__device__ __forceinline__ void build_pair(const RawWindow<NK>& ra, const RawWindow<NK>& rb, uint64_t seg_pos0,
-                                           uint32_t L, unsigned lane, uint2* pt) {
+__device__ __forceinline__ void build_pair(const RawWindow<NK>& ra, const RawWindow<NK>& rb, uint32_t L,
+                                           unsigned lane, uint2* pt) {
   uint32_t ha[NK], la[NK], oa[NK], hb[NK], lb[NK], ob[NK];
-  orient<NK>(ra, seg_pos0, L, ha, la, oa);
-  orient<NK>(rb, seg_pos0, L, hb, lb, ob);
+  orient<NK>(ra, L, ha, la, oa);
+  orient<NK>(rb, L, hb, lb, ob);
+  // NK == 1: after the transpose lane k holds position k of every window of
+  // the group; a '-' window (bit c of the strand ballot) takes position
+  // L - 1 - k instead, complemented in the hi plane, from lane L - 1 - k.
+  // Lanes k >= L hold positions no compare variant reads.
+  const uint32_t ma = NK == 1 ? __ballot_sync(kFull, ra.e & 1) : 0u;
+  const uint32_t mb = NK == 1 ? __ballot_sync(kFull, rb.e & 1) : 0u;
+  const int src = (int)((L - 1 - lane) & 31);
 #pragma unroll
   for (int i = 0; i < NK; ++i) {
-    const uint32_t h0 = warp_transpose(ha[i], lane), h1 = warp_transpose(hb[i], lane);
-    const uint32_t l0 = warp_transpose(la[i], lane), l1 = warp_transpose(lb[i], lane);
+    uint32_t h0 = warp_transpose(ha[i], lane), h1 = warp_transpose(hb[i], lane);
+    uint32_t l0 = warp_transpose(la[i], lane), l1 = warp_transpose(lb[i], lane);
     // Windows holding a non-base byte (N, a separator, another byte) are rare:
     // most pairs skip the third plane's transposes.
     uint32_t o0 = 0, o1 = 0;
-    if (__any_sync(kFull, oa[i] | ob[i])) {
+    const bool any_o = __any_sync(kFull, oa[i] | ob[i]);
+    if (any_o) {
       o0 = warp_transpose(oa[i], lane);
       o1 = warp_transpose(ob[i], lane);
+    }
+    if (NK == 1 && (ma | mb)) {  // warp-uniform
+      // (x & ~m) | (~y & m) and (x & ~m) | (y & m) over (x, y, m) = (0xF0, 0xCC, 0xAA).
+      h0 = lop3<0x72>(h0, __shfl_sync(kFull, h0, src), ma);
+      h1 = lop3<0x72>(h1, __shfl_sync(kFull, h1, src), mb);
+      l0 = lop3<0xD8>(l0, __shfl_sync(kFull, l0, src), ma);
+      l1 = lop3<0xD8>(l1, __shfl_sync(kFull, l1, src), mb);
+      if (any_o) {
+        o0 = lop3<0xD8>(o0, __shfl_sync(kFull, o0, src), ma);
+        o1 = lop3<0xD8>(o1, __shfl_sync(kFull, o1, src), mb);
+      }
     }
     const unsigned k = i * 32 + lane;
     if (k < (unsigned)ROW) {
@@ -606,6 +628,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   constexpr int kPairWords = TableRows<CONC>::kRows * ROW;  // uint2 per pair
   const unsigned lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned W = blockDim.x >> 5;  // pairs per tile = warps
+  const uint32_t seg_w0 = (uint32_t)(seg_pos0 >> 5);  // the segment starts on a plane word
   const unsigned tile_n = W * 64;
   const uint32_t kBufWords = W * kPairWords;
   const uint32_t kBufBytes = kBufWords * (uint32_t)sizeof(uint2);
@@ -650,7 +673,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   {
     uint32_t* cw = coop_words();
     stage_pair<NK>((uint32_t)__cvta_generic_to_shared(cw), cw + 3 * kWindowWords, stage_a, stage_b, kS * 4, hi, lo,
-                   ot, load_entry(queue, t * tile_n + ca, n), load_entry(queue, t * tile_n + cb, n), seg_pos0, lane,
+                   ot, load_entry(queue, t * tile_n + ca, n), load_entry(queue, t * tile_n + cb, n), seg_w0, lane,
                    ents_all + warp * 64);
   }
   uint32_t na = load_entry(queue, tn * tile_n + ca, n);
@@ -659,8 +682,8 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   if (t < ntiles) {
     RawWindow<NK> ra, rb;
     const uint32_t* cw = coop_words();
-    unstage_pair<NK>(ra, rb, cw, cw + 3 * kWindowWords, stage, kS, ents_all + warp * 64, lane, seg_pos0);
-    build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + warp * kPairWords);
+    unstage_pair<NK>(ra, rb, cw, cw + 3 * kWindowWords, stage, kS, ents_all + warp * 64, lane, seg_w0);
+    build_pair<NK, ROW, CONC>(ra, rb, L, lane, tables + warp * kPairWords);
   }
   if (threadIdx.x == 0) claimed[0] = claim;
   __syncthreads();
@@ -673,7 +696,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     {
       uint32_t* cw = coop_words();
       stage_pair<NK>((uint32_t)__cvta_generic_to_shared(cw), cw + 3 * kWindowWords, stage_a, stage_b, kS * 4, hi,
-                     lo, ot, na, nb, seg_pos0, lane, ents_all + (cur ^ 1) * (W * 64) + warp * 64);
+                     lo, ot, na, nb, seg_w0, lane, ents_all + (cur ^ 1) * (W * 64) + warp * 64);
     }
     na = load_entry(queue, tnn * tile_n + ca, n);
     nb = load_entry(queue, tnn * tile_n + cb, n);
@@ -692,8 +715,8 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
       RawWindow<NK> ra, rb;
       const uint32_t* cw = coop_words();
       unstage_pair<NK>(ra, rb, cw, cw + 3 * kWindowWords, stage, kS, ents_all + (cur ^ 1) * (W * 64) + warp * 64,
-                       lane, seg_pos0);
-      build_pair<NK, ROW, CONC>(ra, rb, seg_pos0, L, lane, tables + (cur ^ 1) * kBufWords + warp * kPairWords);
+                       lane, seg_w0);
+      build_pair<NK, ROW, CONC>(ra, rb, L, lane, tables + (cur ^ 1) * kBufWords + warp * kPairWords);
     }
     if (threadIdx.x == 0) claimed[par ^ 1] = claim;
     __syncthreads();
