@@ -1,30 +1,35 @@
 // Bit-sliced comparer: replaces comparer/comparer_cpu (cas-offinder.cl:73-155,
 // :214-286) for compare variants with at most 32 positions that can mismatch.
 //
-// Work unit: a tile of 64*W strand-oriented candidates (W pairs of 32-candidate
-// groups, W = warps = ceil(variants / 32), at most 8) against every compare
-// variant.
-//  1. Build: warp w builds pair w.  Each lane extracts two candidates'
-//     oriented windows from the genome planes (loaded one tile ahead); 32x32
-//     bit transposes (shuffles) turn the windows of a group into per-position
-//     words whose bit c is candidate c.  Lane k then writes, for window
-//     position k, the class words: for each kind of pattern byte (concrete
-//     base, 3-base code, 2-base code) the mismatch mask of the two groups as
-//     one uint2 (one LOP3 each), so one 64-bit shared load serves 64
-//     candidates.  Variants that use only A/C/G/T (and N) need 4 class rows
-//     instead of 14, and the table shrinks to match.  Two table buffers: tile
-//     t+1 is built while tile t is counted, one barrier per tile.
-//  2. Count: each lane owns one compare variant, described by the list of its
-//     positions that can mismatch as shared-memory addresses of the matching
-//     class word (N positions are skipped).  Per pair the lane loads one uint2
-//     per listed position ([register + immediate] addressing, no arithmetic)
-//     and adds the words bit-sliced with a carry-save full-adder tree (explicit
-//     LOP3: 2 per word), so the candidates' mismatch counts come out as 5-6 bit
-//     planes.  A carry chain against the variant's threshold gives the hit
-//     mask; hits (rare; one warp-uniform branch per pair) decode their exact
-//     count from the planes.  Entries past the end of the queue are dropped
-//     there, so full and partial tiles run the same code.
-// Per lane and 64 candidates: S loads + ~4.1 S LOP3 for 64 variant tests.
+// Work unit: a tile of 64*W strand-oriented candidates (W pairs of
+// 32-candidate groups, W = warps per CTA, at most 8) against every compare
+// variant of the pattern group.  CTAs are persistent: two tiles each, then
+// tiles claimed from a per-launch counter.
+//  1. Build: warp w builds pair w.  The pair's window words are copied into
+//     shared memory one tile ahead (stage_pair: one 32-word span per plane
+//     when the 64 windows lie within it, else each lane's own words).  Each
+//     lane aligns its two windows to their first position, 32x32 bit
+//     transposes (shuffles) turn the windows of a group into per-position
+//     words whose bit c is candidate c, and the group's '-' strand windows
+//     are turned into reverse complements in that form.  Lane k then writes,
+//     for window position k, the class words: for each kind of pattern byte
+//     (concrete base, 3-base code, 2-base code) the mismatch mask of the two
+//     groups as one uint2 (one LOP3 each), so one 64-bit shared load serves
+//     64 candidates.  Variants that use only A/C/G/T (and N) need 4 class
+//     rows instead of 14, and the table shrinks to match.  Two table
+//     buffers: tile t+1 is built while tile t is counted, one barrier per
+//     tile.
+//  2. Count: each lane runs a lane program (a chain of up to m compare
+//     variants, built on the host, layout in kernels.cuh) on every pair of
+//     the tile.  Its first variant is counted in full: one uint2 per
+//     position that can mismatch ([register + immediate] shared addresses),
+//     summed bit-sliced by a carry-save full-adder tree (explicit LOP3), plus
+//     a bias so that the top plane is clear exactly where count <=
+//     threshold.  Each later variant is reached by steps that add one class
+//     word and remove one (an up/down ripple, 2 LOP3 per plane), two steps
+//     per loop with one hit vote.  Hits (rare) decode their exact count from
+//     the planes; entries past the end of the queue are dropped there, so
+//     full and partial tiles run the same code.
 //
 // Kernel templates; comparer_bs_inst.cu instantiates them, once per
 // (ROW, NK, CONC) object, so the instances compile in parallel.
