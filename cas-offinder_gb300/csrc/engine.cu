@@ -936,6 +936,15 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
   COF_CUDA(h, cudaMemcpyAsync(h->job_byte0.data(), h->job_bytes.p, (J + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
   uint64_t nrows = 0;
   COF_CUDA(h, cudaMemcpyAsync(&nrows, h->small.p, 8, cudaMemcpyDeviceToHost, h->stream));
+  // Rows returned in one buffer are written in up to kRowChunks chunks of
+  // hits; each chunk's first byte offset comes back with this sync.
+  constexpr uint64_t kRowChunks = 8, kMinChunkHits = 1u << 16;
+  const uint64_t chunk_hits = std::max<uint64_t>(kMinChunkHits, (nhits + kRowChunks - 1) / kRowChunks);
+  const uint64_t nck = sink ? 0 : (nhits + chunk_hits - 1) / chunk_hits;
+  std::vector<uint64_t> ck(nck + 1, 0);
+  if (nck > 1)
+    COF_CUDA(h, cudaMemcpy2DAsync(ck.data(), 8, h->row_offsets.as<uint64_t>(), chunk_hits * 8, 8, nck,
+                                  cudaMemcpyDeviceToHost, h->stream));
   COF_CUDA(h, cudaStreamSynchronize(h->stream));
   const uint64_t bytes = h->job_byte0[J];
   // Rows are short; a size out of proportion means corrupted tables or keys.
@@ -946,13 +955,26 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
     return fail(h, COF_ERR_DEVICE, "row text of " + std::to_string(bytes) + " bytes for " + std::to_string(nrows) +
                                        " rows (" + std::to_string(nhits) + " hits)");
   if (!sink) {
+    // Chunk k's rows are copied to the host on the second stream (idle once
+    // the passes have joined) while chunk k + 1 is written.
     COF_CUDA(h, h->text.ensure(bytes + 1));
-    launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>(), nhits, h->row_offsets.as<uint64_t>(), 0, bytes,
-                      h->text.as<char>(), h->stream);
+    COF_CUDA(h, h->host_text.ensure(bytes + 1));
+    if (!h->stream_ev[0]) COF_CUDA(h, cudaEventCreateWithFlags(&h->stream_ev[0], cudaEventDisableTiming));
+    ck[0] = 0;
+    ck[nck] = bytes;
+    for (uint64_t k = 0; k < nck; ++k) {
+      const uint64_t i0 = k * chunk_hits, i1 = std::min(nhits, i0 + chunk_hits);
+      launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>() + i0, i1 - i0, h->row_offsets.as<uint64_t>() + i0, 0,
+                        ck[k + 1], h->text.as<char>(), h->stream);
+      COF_CUDA(h, cudaEventRecord(h->stream_ev[0], h->stream));
+      COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->stream_ev[0], 0));
+      if (ck[k + 1] > ck[k])
+        COF_CUDA(h, cudaMemcpyAsync((char*)h->host_text.p + ck[k], h->text.as<char>() + ck[k], ck[k + 1] - ck[k],
+                                    cudaMemcpyDeviceToHost, h->stream2));
+    }
     if ((st = record_stop(h, evs, h->stream))) return st;
     COF_CUDA(h, cudaGetLastError());
-    COF_CUDA(h, h->host_text.ensure(bytes + 1));
-    COF_CUDA(h, cudaMemcpyAsync(h->host_text.p, h->text.p, bytes, cudaMemcpyDeviceToHost, h->stream));
+    COF_CUDA(h, cudaStreamSynchronize(h->stream2));
     COF_CUDA(h, cudaStreamSynchronize(h->stream));
     ((char*)h->host_text.p)[bytes] = 0;
   } else {
