@@ -59,7 +59,7 @@ cof_status issue_upload(cof_handle* h, size_t upto) {
 }
 
 // With `streamed` the plane copies are left to the search (run_passes queues
-// them on the finders' stream two segments ahead of the scan): the host
+// them on the finders' stream one segment ahead of the scan): the host
 // planes must stay valid until that search is done.
 cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
                          uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
@@ -692,8 +692,9 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       if (h->profiling && pass >= 1) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[1 - b], 0));
       if (h->upload_pending) {
         // Segment s reads plane words up to w1 + 2 (chunks s and s + 1); its
-        // finder follows the copies up to chunk s + 2 on the same stream.
-        cof_status st = issue_upload(h, (size_t)s + 3);
+        // finder follows the copies up to chunk s + 1 on the same stream, and
+        // the copy of chunk s + 2 runs under the comparer of segment s.
+        cof_status st = issue_upload(h, (size_t)s + 2);
         if (st) return st;
       }
       cof_status st = record_start(h, evs, "finder", (double)(w1 - w0) * 32, h->stream2);
