@@ -126,9 +126,11 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
 // `pgid[(c * m + e) * 32 + l]` is the global id of lane l's first variant
 // (e = 0) and of the variant that its step e - 1 tests (e >= 1; none for a
 // step without bit 15).  Returns false if no kernel instance fits (then use
-// launch_comparer).  `concrete_only`: no variant uses a degenerate IUPAC code
-// (only the four concrete-base class rows are built).  `tile_ctr`: a u32 the
-// caller zeroes before each launch (CTAs claim tiles from it).
+// launch_comparer; also when seg_pos0 is not a multiple of 32: the kernels
+// address windows from the segment's first plane word).  `concrete_only`: no
+// variant uses a degenerate IUPAC code (only the four concrete-base class rows
+// are built).  `tile_ctr`: a u32 the caller zeroes before each launch (CTAs
+// claim tiles from it).
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                         const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
                         uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,
