@@ -557,10 +557,23 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
     // slot is padding then).
     const uint32_t ns = m - 1, sp = ns / 2;
     uint2 wn = make_uint2(0u, 0u);
-    if (ns) wn = __ldg(steps);
+    // One-warp CTAs (PF >= 0) keep their program's step words in shared
+    // memory (copied once per CTA: every tile runs the same program).
+    auto ldstep = [&](const uint2* q) {
+      if constexpr (PF >= 0) {
+        uint2 r;
+        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
+                     : "=r"(r.x), "=r"(r.y)
+                     : "r"((uint32_t)__cvta_generic_to_shared(q)));
+        return r;
+      } else {
+        return __ldg(q);
+      }
+    };
+    if (ns) wn = ldstep(steps);
     for (uint32_t j = 0; j < sp; ++j) {
       const uint2 w2 = wn;
-      if (2 * (j + 1) < ns) wn = __ldg(steps + (j + 1) * 32);
+      if (2 * (j + 1) < ns) wn = ldstep(steps + (j + 1) * 32);
       uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
       lds64<0>(pbase + (w2.x & 0x7FFFu), a0, a1);
       lds64<0>(pbase + (w2.x >> 16), b0, b1);
@@ -615,11 +628,14 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
 
 // Shared memory of a CTA of W warps: two table buffers of W pairs, their
 // candidate entries, the per-thread staging slots and the per-warp window
-// copies (with their meta word).
+// copies (with their meta word); one-warp CTAs add their program's step words
+// (m / 2 pairs per lane).
+constexpr uint32_t kMaxM = 24;  // longest lane program (the host's cost model and autotuner stay within it)
 template <int ROW, int NK, bool CONC>
-__host__ __device__ constexpr size_t bs_smem_bytes(unsigned W) {
+__host__ __device__ constexpr size_t bs_smem_bytes(unsigned W, uint32_t m) {
   return 2 * ((size_t)W * TableRows<CONC>::kRows * ROW * sizeof(uint2) + W * 64 * 4) +
-         2 * Stage<NK>::kSlots * (32 * W) * 4 + (size_t)W * kCoopWords * 4;
+         2 * Stage<NK>::kSlots * (32 * W) * 4 + (size_t)W * kCoopWords * 4 +
+         (W == 1 ? (size_t)(m / 2) * 32 * sizeof(uint2) : 0);
 }
 
 template <int S, int ROW, int NK, bool CONC, bool ONE>
@@ -674,6 +690,13 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   uint32_t addr[S], kmask[NB], kadd = 0, first_on = 0;
   if (resident && warp < chunks)
     load_program<S>(prog + (size_t)warp * words * 32 + lane, table_base, addr, kmask, kadd, first_on);
+  // One-warp CTAs: the program's step words, lane-minor as in `prog` (each
+  // lane reads back only its own words).
+  uint2* steps_sh = (uint2*)(ents_all + 2 * W * 64 + 2 * Stage<NK>::kSlots * kS + W * kCoopWords);
+  if (ONE && chunks == 1) {
+    const uint2* src = (const uint2*)(prog + (1 + S / 2) * 32) + lane;
+    for (uint32_t j = 0; j < m / 2; ++j) steps_sh[j * 32 + lane] = __ldg(src + j * 32);
+  }
   // Entries: e* of the tile being staged, n* of the tile after it.
   {
     uint32_t* cw = coop_words();
@@ -711,7 +734,8 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
       const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
       if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
       run_program<S, ROW, NK, CONC, ONE>(addr, kmask, kadd, first_on,
-                                   (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
+                                   ONE ? (const uint2*)steps_sh + lane
+                                       : (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
                                    pgid + (size_t)c * m * 32 + lane, m, tbase, W, ents, seg_pos0, hits, hit_count,
                                    hit_cap);
     }
@@ -753,22 +777,24 @@ inline unsigned bs_warps(uint32_t chunks) {
 }
 
 template <int S, int ROW, int NK, bool CONC>
-void launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
+bool launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L,
                uint32_t* tile_ctr, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
                cudaStream_t stream) {
+  if (m > kMaxM) return false;  // the shared step words are sized for kMaxM
   const unsigned warps = bs_warps(chunks);
   const int threads = 32 * (int)warps;
-  const size_t smem = bs_smem_bytes<ROW, NK, CONC>(warps);
+  const size_t smem = bs_smem_bytes<ROW, NK, CONC>(warps, m);
   // One-warp CTAs (one chunk) get the instance with the pair index constant.
   auto kernel = warps == 1 ? comparer_bs_kernel<S, ROW, NK, CONC, true> : comparer_bs_kernel<S, ROW, NK, CONC, false>;
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)bs_smem_bytes<ROW, NK, CONC>(kMaxWarps));
+                       (int)std::max(bs_smem_bytes<ROW, NK, CONC>(kMaxWarps, 0), bs_smem_bytes<ROW, NK, CONC>(1, kMaxM)));
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
   kernel<<<sm_count * per_sm, threads, smem, stream>>>(g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks,
                                                         m, L, tile_ctr, hits, hit_count, hit_cap);
+  return true;
 }
 
 }  // namespace
@@ -780,9 +806,8 @@ bool dispatch_s(int slots, const GenomeView& g, const uint32_t* queue, const uin
                 cudaStream_t stream) {
 #define COF_BS_CASE(SV)                                                                                  \
   case SV:                                                                                               \
-    launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, tile_ctr, hits,  \
-                                 hit_count, hit_cap, sm_count, stream);                                  \
-    return true;
+    return launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, tile_ctr, hits, \
+                                        hit_count, hit_cap, sm_count, stream);
   switch (slots) {
     COF_BS_CASE(8)
     COF_BS_CASE(12)
