@@ -783,6 +783,9 @@ bool launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcoun
                cudaStream_t stream) {
   if (m > kMaxM) return false;  // the shared step words are sized for kMaxM
   const unsigned warps = bs_warps(chunks);
+  // A one-warp CTA keeps one program's step words in shared memory: it must
+  // have exactly one chunk (bs_warps gives one warp for one chunk only).
+  if (warps == 1 && chunks != 1) return false;
   const int threads = 32 * (int)warps;
   const size_t smem = bs_smem_bytes<ROW, NK, CONC>(warps, m);
   // One-warp CTAs (one chunk) get the instance with the pair index constant.
