@@ -499,9 +499,12 @@ def main():
                    "sample": f"failed: {e}"[:300]}
 
     # Kernels of ours per search (finder and comparer per segment; row
-    # lengths, row writing and job bounds once), times the timed searches.
+    # lengths and job bounds once; row writing in one launch per chunk of
+    # max(2^16, ceil(hits / 8)) hits), times the timed searches.
+    chunk_hits = max(1 << 16, -(-nh // 8))
+    row_chunks = -(-nh // chunk_hits) if nh else 0
     launches = args.steps * int(stats["finder"]["launches"] + stats["comparer"]["launches"] +
-                                3 * stats["format"]["launches"])
+                                (2 + row_chunks) * stats["format"]["launches"])
     batched = None if args.no_batched else run_batched(P, eng, lens, rates, args)
     pam_variety = None if args.no_pam_variety else run_pam_variety(P, eng, lens, rates, args)
     served = None if args.no_served else run_served(P, eng, lens, args)
