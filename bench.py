@@ -20,9 +20,18 @@ after warm-up steps, max over ranks.  Under torchrun each rank runs an
 independent replica on its own GPU (weak scaling; the search has no
 cross-GPU exchange).
 
---impl reference times the reference algorithm on the host CPU cores instead:
-the reference binary built from its sources when it runs here, else the
-oracle's CPU restatement, on a bounded prefix of the same genome.
+--impl reference times the reference's own CPU path on the host cores instead
+(its finder_cpu/comparer_cpu through its unmodified host code, device C, built
+from its sources by oracle/build_ref.py; the oracle's C++ restatement only
+where that build is absent), on the first 20 Mbp of the same genome, rate
+per base extrapolated to the whole genome.  That arm loads no library of this
+package: its genome file comes from the standalone cof-synth writer.
+
+verify (on by default, --no-verify skips it): after the timed legs the oracle
+(the CPU restatement, every host core) searches the same inputs, and the GPU
+rows are compared byte for byte: the whole 3.1 Gbp genome for the plain
+search, and samples of the timed batched, PAM-variety and served searches
+over the genome's leading records.
 """
 import argparse
 import json
@@ -121,7 +130,7 @@ def served_requests(seed=9, n=12, genome_path="synthetic"):
     return out
 
 
-def run_served(P, eng, lens, args):
+def run_served(P, eng, lens, args, capture=None):
     """Served mode: the same requests arriving as a Poisson stream at several
     rates; p50/p99 latency (submit to rows in host memory) and guide-Gbp/s,
     against the plain path run once per request."""
@@ -167,9 +176,19 @@ def run_served(P, eng, lens, args):
                 threads[-1].start()
             for th in threads:
                 th.join()
+            views = [None] * len(reqs)
             for j in range(len(reqs)):
-                _, _, lat[j] = srv.wait_view(tickets[j])  # rows left in the server's pinned buffer
+                views[j] = srv.wait_view(tickets[j])  # rows left in the server's pinned buffer
+                lat[j] = views[j][2]
             span = time.perf_counter() - t0
+            if capture is not None and rate == args.served_rates[-1]:
+                import ctypes
+                keep = [f"chr{i + 1}" for i in range(VERIFY_SERVED_RECORDS)]
+                pick = sorted(range(len(reqs)), key=lambda j: (reqs[j][1], j))[:VERIFY_SERVED_REQUESTS]
+                capture["served"] = {"records": VERIFY_SERVED_RECORDS, "rate": rate,
+                                     "rows": {j: rows_of_records(ctypes.string_at(views[j][0], views[j][1]), keep)
+                                              for j in pick}}
+                capture["served_n"] = len(reqs)
             for j in range(len(reqs)):
                 srv.release(tickets[j])
             st = srv.stats()
@@ -185,6 +204,42 @@ def run_served(P, eng, lens, args):
 
 def input_text(genome_path, guides):
     return f"{genome_path}\n{PATTERN} {DNA} {RNA}\n" + "".join(f"{g} {MM}\n" for g in guides)
+
+
+# The synthetic genome: 41% GC with a +-10% drift per 100 kbp window, 5% N in
+# runs of 1-100 kbp (cofx_synth_record / cof-synth arguments).
+GENOME_ARGS = (0.41, 0.10, 100000, 0.05, 1000, 100000)
+
+
+def genome_lengths(total_bp, n_records=24, seed=GENOME_SEED, lo=47_000_000, hi=249_000_000):
+    """Record lengths drawn log-uniform in [lo, hi], rescaled to sum to
+    total_bp (numpy only; the same draw as the package's record_lengths)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    raw = np.exp(rng.uniform(np.log(lo), np.log(hi), n_records))
+    lens = np.floor(raw / raw.sum() * int(total_bp)).astype(np.int64)
+    lens[-1] += int(total_bp) - lens.sum()
+    return [int(x) for x in lens]
+
+
+def synth_binary():
+    """The standalone genome writer (compiled on demand; no CUDA)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_cof_build", os.path.join(ROOT, "cas-offinder_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build_synth()
+
+
+def write_genome(path, lens, records=None, limit=None, seed=GENOME_SEED):
+    """Writes the synthetic genome (records chr1.. of lengths `lens`; only the
+    first `records` of them, or only its first `limit` positions) as FASTA, or
+    as 2BIT when path ends in .2bit, with cof-synth; returns path."""
+    keep = lens[:records] if records else lens
+    cmd = [synth_binary()] + (["--limit", str(int(limit))] if limit else []) + \
+        [path, str(seed)] + [str(x) for x in GENOME_ARGS] + [f"chr{i + 1}:{n}" for i, n in enumerate(keep)]
+    subprocess.run(cmd, check=True)
+    return path
 
 
 def build_genome(P, total_bp, n_records=24, seed=GENOME_SEED, prefix_bp=None):
@@ -209,7 +264,7 @@ def build_genome(P, total_bp, n_records=24, seed=GENOME_SEED, prefix_bp=None):
             buf[pos] = ord(";")
             pos += 1
         starts.append(pos)
-        P.lib().cofx_synth_record(seed, r, ln, 0.41, 0.10, 100000, 0.05, 1000, 100000, base + pos)
+        P.lib().cofx_synth_record(seed, r, ln, *GENOME_ARGS, base + pos)
         pos += ln
     names = [f"chr{r + 1}" for r in range(n_records)]
     return buf, names, starts, lens
@@ -286,81 +341,208 @@ def dist_barrier(world):
         dist.barrier()
 
 
-def cpu_sample_run(binary, genome_buf, names, starts, sample_bp, guides, threads, workdir):
-    """Runs the CPU implementation on the first `sample_bp` positions of the
-    genome (as FASTA); returns (seconds, rows)."""
-    fa = os.path.join(workdir, "sample.fa")
-    if not os.path.exists(fa):
-        end = min(len(genome_buf), sample_bp)
-        P = pkg()
-        recs, nm = [], []
-        for i, s in enumerate(starts):
-            e = (starts[i + 1] - 1) if i + 1 < len(starts) else len(genome_buf)
-            if s >= end:
-                break
-            recs.append(bytes(genome_buf[s:min(e, end)]))
-            nm.append(names[i])
-        P.write_fasta(fa, nm, recs)
-    inp = os.path.join(workdir, "sample_input.txt")
+def cpu_binaries():
+    """{'reference': path or None, 'port': path or None}: the reference built
+    from its own sources on this machine (oracle/build_ref.py; absent where
+    no staged copy of its sources exists) and the oracle's C++ restatement.
+    Neither loads a library of this package."""
+    import build_oracle
+    port, ref = build_oracle.build(with_reference=True)
+    out = {"reference": None, "port": None}
+    for kind, cand in (("reference", ref), ("port", port)):
+        if cand and os.path.exists(cand):
+            try:
+                if subprocess.run([cand], capture_output=True, timeout=30).returncode == 0:
+                    out[kind] = cand
+            except (OSError, subprocess.TimeoutExpired):
+                continue
+    if not out["port"] and not out["reference"]:
+        raise RuntimeError("no CPU implementation available")
+    return out
+
+
+def cpu_run(binary, text, threads, workdir, tag="cpu"):
+    """Runs a CPU implementation (reference argv: input C output) on one input
+    file; returns (seconds, output bytes)."""
+    inp = os.path.join(workdir, f"{tag}_input.txt")
+    out = os.path.join(workdir, f"{tag}_out.tsv")
     with open(inp, "w") as f:
-        f.write(input_text(fa, guides))
-    out = os.path.join(workdir, "sample_out.tsv")
+        f.write(text)
     env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     t0 = time.perf_counter()
     r = subprocess.run([binary, inp, "C", out], env=env, capture_output=True)
     dt = time.perf_counter() - t0
     if r.returncode != 0:
-        raise RuntimeError(r.stderr.decode()[-2000:])
-    rows = sum(1 for l in open(out, "rb") if not l.startswith(b"#"))
-    return dt, rows
+        raise RuntimeError(f"{binary} failed: " + r.stderr.decode()[-2000:])
+    with open(out, "rb") as f:
+        data = f.read()
+    os.remove(out)
+    return dt, data
 
 
-def cpu_binary():
-    """(path, kind): the reference built from its sources if it runs here, else the oracle port."""
-    import build_oracle
-    port, _ = build_oracle.build(with_reference=False)
-    ref_path = os.path.join(ROOT, "oracle", "_ref", "cas-offinder-ref")  # prebuilt by build(), if at all
-    for cand, kind in ((ref_path, "reference"), (port, "port")):
-        if cand and os.path.exists(cand):
-            try:
-                r = subprocess.run([cand], capture_output=True, timeout=30)
-                if r.returncode == 0:
-                    return cand, kind
-            except OSError:
-                continue
-    raise RuntimeError("no CPU implementation available")
+def count_rows(data):
+    return sum(1 for l in data.split(b"\n") if l and not l.startswith(b"#"))
+
+
+def cpu_plain_sample(binary, lens, sample_bp, guides, threads, workdir):
+    """The plain workload on the first `sample_bp` positions of the genome:
+    (seconds, rows, guide-Gbp/s extrapolated per base to the whole genome)."""
+    fa = os.path.join(workdir, f"sample_{sample_bp}.fa")
+    if not os.path.exists(fa):
+        write_genome(fa, lens, limit=sample_bp)
+    dt, out = cpu_run(binary, input_text(fa, guides), threads, workdir, "plain")
+    return dt, count_rows(out), len(guides) * (sample_bp / 1e9) / dt
 
 
 def run_reference_arm(args, world, rank):
+    """The reference's own CPU path on this machine's cores, on the plain
+    workload's first 20 Mbp (rank 0 only).  Loads no library of this package."""
     if rank != 0:
         return
-    P = pkg()
-    P.build()
-    binary, kind = cpu_binary()
+    tools = cpu_binaries()
+    kind = "reference" if tools["reference"] else "port"
+    binary = tools[kind]
     guides = make_guides()
-    sample_bp = int(args.sample_mbp * 1e6)
-    buf, names, starts, _ = build_genome(P, args.genome_gbp * 1e9, prefix_bp=sample_bp)
+    lens = genome_lengths(args.genome_gbp * 1e9)
+    sample_bp = min(int(args.sample_mbp * 1e6), sum(lens) + len(lens) - 1)
     threads = os.cpu_count() or 1
     times = []
     with tempfile.TemporaryDirectory() as tmp:
         for i in range(args.warmup + args.steps):
-            dt, rows = cpu_sample_run(binary, buf, names, starts, sample_bp, guides, threads, tmp)
+            dt, rows, _ = cpu_plain_sample(binary, lens, sample_bp, guides, threads, tmp)
             if i >= args.warmup:
                 times.append(dt)
     total = sum(times)
-    gbp = min(len(buf), sample_bp) / 1e9
+    gbp = sample_bp / 1e9
     value = N_GUIDES * gbp * len(times) / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "guide-Gbp/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample_bp": min(len(buf), sample_bp)},
+        "config": {"workload": WORKLOAD, "sample_bp": sample_bp},
         "cpu_baseline": {"value": value, "unit": "guide-Gbp/s", "cores": threads, "kind": kind,
-                         "sample": f"first {min(len(buf), sample_bp)} bp of the same genome and input "
-                                   f"({rows} rows)"},
+                         "program": os.path.relpath(binary, ROOT),
+                         "sample": f"first {sample_bp} bp of the same genome and input ({rows} rows per step); "
+                                   f"guide-Gbp/s extrapolated per base to the whole genome"},
         "e2e": {"value": value, "unit": "guide-Gbp/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def cpu_baselines(args, lens, guides, workdir):
+    """CPU figures beside the GPU ones, all on this machine's cores: the
+    reference's own CPU path (kind "reference") where it was built here, and
+    the oracle's restatement (kind "port") as a second number.  Plain: the
+    first 20 Mbp; batched: 8 of the 1,024 input files over the first 20 Mbp;
+    PAM variety: the four 256-guide sets over the first 2 Mbp; served: 8 of
+    the requests over the first 2 Mbp.  Rates are per base, extrapolated."""
+    import random
+    tools = cpu_binaries()
+    threads = os.cpu_count() or 1
+    kinds = [k for k in ("reference", "port") if tools[k]]
+    total = sum(lens) + len(lens) - 1
+    s20 = min(int(args.sample_mbp * 1e6), total)
+    s2 = min(2_000_000, total)
+    fa20 = write_genome(os.path.join(workdir, f"sample_{s20}.fa"), lens, limit=s20)
+    fa2 = write_genome(os.path.join(workdir, f"sample_{s2}.fa"), lens, limit=s2)
+    out = {"cores": threads, "primary": kinds[0]}
+    for kind in kinds:
+        b = tools[kind]
+        dt, out_rows = cpu_run(b, input_text(fa20, guides), threads, workdir, "plain")
+        res = {"plain": {"value": len(guides) * (s20 / 1e9) / dt, "seconds": dt, "rows": count_rows(out_rows),
+                         "sample": f"first {s20} bp, 4 guides (extrapolated per base)"}}
+        if not args.no_batched:
+            texts = batched_jobs(genome_path=fa20)
+            pick = random.Random(13).sample(range(len(texts)), 8)
+            ts = [cpu_run(b, texts[j], threads, workdir, "batched")[0] for j in pick]
+            res["batched"] = {"value": (s20 / 1e9) * len(ts) / sum(ts), "seconds": sum(ts),
+                              "sample": f"input files {pick} of the 1,024 (one guide each), each alone over "
+                                        f"the first {s20} bp (extrapolated per base and per input)"}
+        if not args.no_pam_variety:
+            ts = [cpu_run(b, t, threads, workdir, "pam")[0] for t in pam_variety_jobs(genome_path=fa2)]
+            res["pam_variety"] = {"value": 1024 * (s2 / 1e9) / sum(ts), "seconds": sum(ts),
+                                  "sample": f"the four 256-guide sets over the first {s2} bp (extrapolated per base)"}
+        if not args.no_served:
+            reqs = served_requests(n=args.served_requests, genome_path=fa2)
+            pick = random.Random(17).sample(range(len(reqs)), min(8, len(reqs)))
+            ts = [cpu_run(b, reqs[j][0], threads, workdir, "served")[0] for j in pick]
+            g = sum(reqs[j][1] for j in pick)
+            res["served"] = {"value": g * (s2 / 1e9) / sum(ts), "seconds": sum(ts),
+                             "sample": f"requests {pick} ({g} guides), each alone over the first {s2} bp "
+                                       f"(extrapolated per base)"}
+        out[kind] = res
+    return out
+
+
+# ---------------------------------------------------------------- verification
+def rows_of_records(rows, keep_names):
+    """The rows (bytes, header lines dropped) whose chromosome is in keep_names,
+    in their order."""
+    keep = {n.encode() if isinstance(n, str) else n for n in keep_names}
+    out = [l for l in rows.split(b"\n") if l and not l.startswith(b"#") and l.split(b"\t", 5)[4] in keep]
+    return b"".join(l + b"\n" for l in out)
+
+
+def compare_rows(gpu, ora):
+    """{rows_compared, identical, first_difference} of two row texts (no headers)."""
+    a, b = gpu.split(b"\n"), ora.split(b"\n")
+    same = gpu == ora
+    diff = None
+    if not same:
+        for i, (x, y) in enumerate(zip(a, b)):
+            if x != y:
+                diff = {"row": i, "gpu": x.decode(errors="replace")[:200], "oracle": y.decode(errors="replace")[:200]}
+                break
+        else:
+            diff = {"row": min(len(a), len(b)), "gpu_rows": len(a), "oracle_rows": len(b)}
+    return {"rows_compared": count_rows(ora), "gpu_rows": count_rows(gpu), "identical": same,
+            "first_difference": diff}
+
+
+def oracle_rows(oracle, text, threads, workdir, tag):
+    """(seconds, the oracle's rows without the two header lines)."""
+    dt, out = cpu_run(oracle, text, threads, workdir, tag)
+    return dt, b"".join(l + b"\n" for l in out.split(b"\n") if l and not l.startswith(b"#"))
+
+
+def run_verify(capture, lens, guides, names, workdir):
+    """Byte comparison of the GPU rows captured from the timed legs against the
+    oracle run on the same inputs (see the module docstring)."""
+    import build_oracle
+    oracle, _ = build_oracle.build(with_reference=False)
+    threads = os.cpu_count() or 1
+    res = {"oracle": "oracle/cof_oracle.cpp (CPU restatement, pinned to the reference's outputs)",
+           "threads": threads}
+    full = write_genome(os.path.join(workdir, "genome.2bit"), lens)
+    if "plain" in capture:
+        dt, ora = oracle_rows(oracle, input_text(full, guides), threads, workdir, "v_plain")
+        res["plain"] = dict(compare_rows(capture["plain"], ora), oracle_s=round(dt, 1),
+                            scope=f"whole genome: {len(lens)} records, {sum(lens) + len(lens) - 1} positions")
+    os.remove(full)
+    for leg, texts_of in (("batched", lambda path: batched_jobs(genome_path=path)),
+                          ("pam_variety", lambda path: pam_variety_jobs(genome_path=path)),
+                          ("served", lambda path: [t for t, _ in served_requests(n=capture.get("served_n", 0),
+                                                                                  genome_path=path)])):
+        cap = capture.get(leg)
+        if not cap:
+            continue
+        k = cap["records"]
+        path = write_genome(os.path.join(workdir, f"prefix{k}.2bit"), lens, records=k)
+        texts = texts_of(path)
+        items, t_all, ok = [], 0.0, True
+        for j, gpu in cap["rows"].items():
+            dt, ora = oracle_rows(oracle, texts[j], threads, workdir, f"v_{leg}")
+            c = compare_rows(gpu, ora)
+            items.append({"input": j, "rows_compared": c["rows_compared"], "identical": c["identical"],
+                          "first_difference": c["first_difference"]})
+            t_all += dt
+            ok = ok and c["identical"]
+        res[leg] = {"identical": ok, "rows_compared": sum(x["rows_compared"] for x in items), "inputs": items,
+                    "oracle_s": round(t_all, 1),
+                    "scope": f"rows on the first {k} records ({', '.join(names[:k])}: "
+                             f"{sum(lens[:k]) + k - 1} positions) of the timed search"}
+    res["identical"] = all(res[l]["identical"] for l in ("plain", "batched", "pam_variety", "served") if l in res)
+    return res
 
 
 def main():
@@ -379,6 +561,7 @@ def main():
     ap.add_argument("--no-pam-variety", action="store_true", help="skip the four 256-guide PAM sets")
     ap.add_argument("--comparer", default="auto", choices=["auto", "popcount", "bitsliced"],
                     help="comparer kernel for the plain search (default: bit-sliced where it fits)")
+    ap.add_argument("--no-verify", action="store_true", help="skip the byte comparison with the oracle")
     ap.add_argument("--served-requests", type=int, default=12)
     ap.add_argument("--served-rates", type=float, nargs="+", default=[1.0, 2.0, 5.0, 10.0, 20.0, 50.0, 100.0, 200.0])
     args = ap.parse_args()
@@ -388,6 +571,7 @@ def main():
         run_reference_arm(args, world, rank)
         return
 
+    import ctypes
     import numpy as np
     import torch
     P = pkg()
@@ -437,8 +621,9 @@ def main():
     with ClockSampler(local) as clk:
         eng.timer_start()
         for _ in range(args.steps):
-            eng.search_view()
+            view = eng.search_view()
         ms = eng.timer_stop()
+    capture = {"plain": ctypes.string_at(*view)}  # the rows of the last timed search
     ms_step = dist_max(ms / args.steps, world)
     gbp = sum(lens) / 1e9
     value = world * N_GUIDES * gbp / (ms_step / 1e3)
@@ -484,19 +669,12 @@ def main():
     peaks = load_peaks()
 
     cpu = None
+    workdir = tempfile.mkdtemp(prefix="cof_bench_")
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            binary, kind = cpu_binary()
-            with tempfile.TemporaryDirectory() as tmp:
-                sample_bp = int(args.sample_mbp * 1e6)
-                threads = os.cpu_count() or 1
-                dt, srows = cpu_sample_run(binary, buf, names, starts, sample_bp, guides, threads, tmp)
-                cpu = {"value": N_GUIDES * (sample_bp / 1e9) / dt, "unit": "guide-Gbp/s", "cores": threads,
-                       "kind": kind, "sample": f"first {sample_bp} bp of the same genome and input "
-                                               f"({srows} rows, {dt:.2f} s)"}
+            cpu = cpu_baselines(args, lens, guides, workdir)
         except Exception as e:  # the baseline is reported, never required
-            cpu = {"value": None, "unit": "guide-Gbp/s", "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"failed: {e}"[:300]}
+            cpu = {"failed": f"{e}"[:300]}
 
     # Kernels of ours per search (finder and comparer per segment; row
     # lengths and job bounds once; row writing in one launch per chunk of
@@ -505,9 +683,34 @@ def main():
     row_chunks = -(-nh // chunk_hits) if nh else 0
     launches = args.steps * int(stats["finder"]["launches"] + stats["comparer"]["launches"] +
                                 (2 + row_chunks) * stats["format"]["launches"])
-    batched = None if args.no_batched else run_batched(P, eng, lens, rates, args)
-    pam_variety = None if args.no_pam_variety else run_pam_variety(P, eng, lens, rates, args)
-    served = None if args.no_served else run_served(P, eng, lens, args)
+    batched = None if args.no_batched else run_batched(P, eng, lens, rates, args, capture)
+    pam_variety = None if args.no_pam_variety else run_pam_variety(P, eng, lens, rates, args, capture)
+    served = None if args.no_served else run_served(P, eng, lens, args, capture)
+    cpu_main = None
+    if cpu and "primary" in cpu:
+        k = cpu["primary"]
+        cpu_main = {"value": cpu[k]["plain"]["value"], "unit": "guide-Gbp/s", "cores": cpu["cores"], "kind": k,
+                    "sample": cpu[k]["plain"]["sample"] + f" ({cpu[k]['plain']['rows']} rows, "
+                                                          f"{cpu[k]['plain']['seconds']:.2f} s)"}
+        if "port" in cpu and k != "port":
+            cpu_main["port"] = {"value": cpu["port"]["plain"]["value"], "seconds": cpu["port"]["plain"]["seconds"]}
+        for leg, obj in (("batched", batched), ("pam_variety", pam_variety), ("served", served)):
+            if obj is not None and leg in cpu[k]:
+                obj["cpu_baseline"] = dict(cpu[k][leg], unit="guide-Gbp/s", cores=cpu["cores"], kind=k)
+                if "port" in cpu and k != "port" and leg in cpu["port"]:
+                    obj["cpu_baseline"]["port"] = {"value": cpu["port"][leg]["value"]}
+    elif cpu:
+        cpu_main = {"value": None, "unit": "guide-Gbp/s", "cores": os.cpu_count(), "kind": "port",
+                    "sample": cpu.get("failed")}
+    verify = None
+    if rank == 0 and not args.no_verify:
+        eng.close()
+        eng = None
+        try:
+            verify = run_verify(capture, lens, guides, names, workdir)
+        except Exception as e:
+            verify = {"identical": False, "failed": f"{e}"[:500]}
+    shutil.rmtree(workdir, ignore_errors=True)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "guide-Gbp/s", "n_gpus": world, "steps": args.steps,
@@ -533,15 +736,22 @@ def main():
             "batched": batched,
             "pam_variety": pam_variety,
             "served": served,
-            "cpu_baseline": cpu,
+            "cpu_baseline": cpu_main,
+            "verify": verify,
             "clocks": clk.summary(),
             "gpu_launches": launches,
         }
         print(json.dumps(line), flush=True)
-    eng.close()
+    if eng is not None:
+        eng.close()
 
 
-def run_batched(P, eng, lens, rates, args):
+VERIFY_BATCHED_JOBS, VERIFY_BATCHED_RECORDS = 8, 5  # 578 Mbp, 8 segment boundaries
+VERIFY_PAM_SETS, VERIFY_PAM_RECORDS = (0, 3), 1      # NNGRRT and 5'-TTTV over chr1
+VERIFY_SERVED_REQUESTS, VERIFY_SERVED_RECORDS = 2, 5
+
+
+def run_batched(P, eng, lens, rates, args, capture=None):
     """The 1,024-guide mixed workload on the same resident genome: all 1,024
     input files in one batched search, against sequential plain searches (one
     input file at a time; a sample of them timed and scaled to 1,024)."""
@@ -568,6 +778,12 @@ def run_batched(P, eng, lens, rates, args):
     ms = eng.timer_stop() / args.batched_steps
     hits, rows = eng.last_hit_count()
     gbp = sum(lens) / 1e9
+    if capture is not None:  # rows of sampled jobs of the last timed search, on the leading records
+        import random
+        keep = [f"chr{i + 1}" for i in range(VERIFY_BATCHED_RECORDS)]
+        pick = sorted(random.Random(11).sample(range(len(texts)), VERIFY_BATCHED_JOBS))
+        capture["batched"] = {"records": VERIFY_BATCHED_RECORDS,
+                              "rows": {j: rows_of_records(eng.job_rows(j), keep) for j in pick}}
     # Sequential plain searches of the same input files.
     k = args.plain_sample
     eng.readInputFile(texts[0])
@@ -593,7 +809,7 @@ def run_batched(P, eng, lens, rates, args):
     }
 
 
-def run_pam_variety(P, eng, lens, rates, args):
+def run_pam_variety(P, eng, lens, rates, args, capture=None):
     """The four 256-guide PAM sets in one batched search of the resident
     genome, against the four sets searched one after another."""
     texts = pam_variety_jobs()
@@ -616,6 +832,10 @@ def run_pam_variety(P, eng, lens, rates, args):
     ms = eng.timer_stop() / args.batched_steps
     hits, rows = eng.last_hit_count()
     gbp = sum(lens) / 1e9
+    if capture is not None:
+        keep = [f"chr{i + 1}" for i in range(VERIFY_PAM_RECORDS)]
+        capture["pam_variety"] = {"records": VERIFY_PAM_RECORDS,
+                                  "rows": {j: rows_of_records(eng.job_rows(j), keep) for j in VERIFY_PAM_SETS}}
     seq_ms = 0.0
     for t in texts:
         eng.readInputFile(t)

@@ -43,7 +43,7 @@ EXPORTS = [
     "cof_router_open", "cof_router_add_genome", "cof_router_drop_genome", "cof_router_genomes", "cof_router_submit",
     "cof_router_wait", "cof_router_release", "cof_router_last_error", "cof_router_close",
     "cof_gzip_open", "cof_gzip_write", "cof_gzip_write_fn", "cof_gzip_close",
-    "cofx_synth_record", "cofx_pipe_rates", "cofx_mismatch_table", "cofx_bs_programs", "cofx_genome_text",
+    "cofx_synth_record", "cofx_mismatch_table", "cofx_bs_programs", "cofx_genome_text",
 ]
 
 # cof_write_fn: int (*)(void* ctx, const char* data, size_t len)
@@ -145,8 +145,6 @@ def lib():
             "cof_search_chunk_static": (c.c_int, [vp, vp, vp, u64, c.c_char_p, c.c_char_p, u32, c.c_uint16, vp,
                                                   u64, vp, vp]),
             "cof_timer_stop": (c.c_int, [vp, c.POINTER(c.c_double)]),
-            "cofx_pipe_rates": (c.c_int, [c.c_int, c.POINTER(c.c_double), c.POINTER(c.c_double),
-                                          c.POINTER(c.c_double)]),
             "cofx_mismatch_table": (None, [vp]),
             "cofx_bs_programs": (c.c_int, [c.c_char_p, sz, vp, vp, sz, vp, sz, vp, sz]),
             "cofx_genome_text": (c.c_int, [c.c_char_p, vp, u64, c.POINTER(u64)]),
@@ -622,10 +620,18 @@ def gzip_write(path, parts, level=1, threads=0):
         raise CofError(st, "cof_gzip_close failed")
 
 
+RATES_LIB_PATH = os.path.join(PKG_DIR, "lib", "libcofrates.so")
+SYNTH_PATH = os.path.join(PKG_DIR, "bin", "cof-synth")
+
+
 def pipe_rates(device=0):
-    """Measured integer-pipe throughput (lane-ops/s): {'lop3', 'popc', 'iadd'}."""
+    """Measured integer-pipe throughput (lane-ops/s): {'lop3', 'popc', 'iadd'}.
+    From libcofrates.so, the measurement library built beside the engine."""
+    L = ctypes.CDLL(RATES_LIB_PATH)
+    L.cofx_pipe_rates.restype = ctypes.c_int
+    L.cofx_pipe_rates.argtypes = [ctypes.c_int] + [ctypes.POINTER(ctypes.c_double)] * 3
     a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
-    if lib().cofx_pipe_rates(device, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)) != 0:
+    if L.cofx_pipe_rates(device, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)) != 0:
         raise RuntimeError("cofx_pipe_rates failed")
     return {"lop3": a.value, "popc": b.value, "iadd": c.value}
 

@@ -500,6 +500,7 @@ cof_status autotune_group(cof_handle* h, PatternGroup& g, const std::vector<cons
     build_bs_programs(vars, g.gids, g.bs_slots, row, prog, pgid, chunks, mm, m, nullptr);
     DevBuf dprog, dpgid;
     float us = 1e30f;
+    bool declined = false;  // the launcher refused this geometry: m is not a candidate
     auto run = [&]() -> cof_status {
       COF_CUDA(h, dprog.ensure(prog.size() * 4));
       COF_CUDA(h, dpgid.ensure(pgid.size() * 4));
@@ -509,9 +510,12 @@ cof_status autotune_group(cof_handle* h, PatternGroup& g, const std::vector<cons
         COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
         COF_CUDA(h, cudaMemsetAsync(qc + 1, 0, 4, h->stream));
         COF_CUDA(h, cudaEventRecord(ev[0], h->stream));
-        launch_comparer_bs(gv, q, qc, w0 * 32, dprog.as<uint32_t>(), dpgid.as<uint32_t>(), chunks, mm, g.bs_slots,
-                           g.L, g.concrete_only, qc + 1, h->hits.as<uint64_t>(),
-                           h->hit_count.as<unsigned long long>(), cap, h->sm_count, h->stream);
+        if (!launch_comparer_bs(gv, q, qc, w0 * 32, dprog.as<uint32_t>(), dpgid.as<uint32_t>(), chunks, mm,
+                                g.bs_slots, g.L, g.concrete_only, qc + 1, h->hits.as<uint64_t>(),
+                                h->hit_count.as<unsigned long long>(), cap, h->sm_count, h->stream)) {
+          declined = true;
+          return COF_OK;
+        }
         COF_CUDA(h, cudaEventRecord(ev[1], h->stream));
         COF_CUDA(h, cudaEventSynchronize(ev[1]));
         float ms = 0;
@@ -522,6 +526,7 @@ cof_status autotune_group(cof_handle* h, PatternGroup& g, const std::vector<cons
       return COF_OK;
     };
     if ((st = run())) break;
+    if (declined) continue;
     g.bs_tuned.emplace_back(mm, us);
     if (us < best_us) {
       best_us = us;

@@ -21,6 +21,12 @@
 // checks the result, and caches it per device; later calls reuse it.  Make the
 // first call on a device before any stream capture begins.
 //
+// The pattern and compare string are upper-cased first, as the reference does
+// with its input file; every other byte keeps its meaning (IUPAC codes, 'N'
+// and any byte outside the IUPAC set never mismatch).  The compare string's
+// masks are handed to the GPU as a kernel argument, so the call reads no host
+// memory after it returns.
+//
 // Every call shares the one array, and the array keeps what the last call left
 // in it: each call clears the queue counter (and the caller's hit counter)
 // before use.  Two calls whose work overlaps on the GPU (different streams, or
@@ -71,14 +77,32 @@ cudaError_t scratch_address(uint32_t** out) {
   return cudaSuccess;
 }
 
-std::string revcomp_of(const char* s, uint32_t L) {
+std::string revcomp_of(const std::string& s) {
+  const size_t L = s.size();
   std::string r(L, 'N');
-  for (uint32_t k = 0; k < L; ++k) r[k] = (char)complement_byte((unsigned char)s[L - 1 - k]);
+  for (size_t k = 0; k < L; ++k) r[k] = (char)complement_byte((unsigned char)s[L - 1 - k]);
   return r;
 }
 
+// The reference upper-cases the pattern and every guide before it builds its
+// compare strings (cas-offinder.cpp:625, :640); so does this entry point.
+std::string upper_of(const char* s, uint32_t L) {
+  std::string r(s, L);
+  for (char& c : r)
+    if (c >= 'a' && c <= 'z') c = (char)(c - 32);
+  return r;
+}
+
+// Writes one variant's class masks into the scratch array.  The masks travel
+// as a kernel argument, so nothing on the host is read after the launch is
+// queued.
 template <int NW>
-void fill_mask(VariantMask<NW>& vm, const char* comp, uint32_t L, uint32_t thr) {
+__global__ void store_mask_kernel(VariantMask<NW> vm, VariantMask<NW>* dst) {
+  if (threadIdx.x == 0) *dst = vm;
+}
+
+template <int NW>
+void fill_mask(VariantMask<NW>& vm, const std::string& comp, uint32_t L, uint32_t thr) {
   std::memset(&vm, 0, sizeof vm);
   for (uint32_t k = 0; k < L; ++k) {
     const uint32_t m = class_bits_of((unsigned char)comp[k]);
@@ -104,6 +128,10 @@ extern "C" cof_status cof_search_chunk_static(const uint32_t* d_hi, const uint32
   if (patternlen == 0 || patternlen > (uint32_t)kMaxL) return COF_ERR_UNSUPPORTED;
   if (n > kStaticMaxPositions) return COF_ERR_TOO_LARGE;
   cudaStream_t st = (cudaStream_t)stream;
+  // An unread error of the caller's own CUDA work is left for the caller:
+  // nothing is queued, so every error this call reports after its launches
+  // is its own.
+  if (cudaPeekAtLastError() != cudaSuccess) return COF_ERR_CUDA;
   uint32_t* scratch = nullptr;
   if (scratch_address(&scratch) != cudaSuccess) return COF_ERR_CUDA;
   int dev = 0, sms = 0;
@@ -119,10 +147,11 @@ extern "C" cof_status cof_search_chunk_static(const uint32_t* d_hi, const uint32
 
   FinderPattern fp;
   std::memset(&fp, 0, sizeof fp);
-  const std::string rev = revcomp_of(pattern, patternlen);
+  const std::string pat = upper_of(pattern, patternlen), cmp = upper_of(comp, patternlen);
+  const std::string rev = revcomp_of(pat);
   fp.L = patternlen;
   for (uint32_t k = 0; k < patternlen; ++k) {
-    const uint32_t mf = class_bits_of((unsigned char)pattern[k]);
+    const uint32_t mf = class_bits_of((unsigned char)pat[k]);
     if (mf) {
       fp.fk[fp.nf] = (uint8_t)k;
       fp.fm[fp.nf++] = (uint8_t)mf;
@@ -134,23 +163,16 @@ extern "C" cof_status cof_search_chunk_static(const uint32_t* d_hi, const uint32
     }
   }
   const int nw = patternlen <= 32 ? 1 : 2;
-  VariantMask<2> vm2;
-  VariantMask<1> vm1;
-  const void* host_mask;
-  size_t mask_bytes;
   if (nw == 1) {
-    fill_mask<1>(vm1, comp, patternlen, threshold);
-    host_mask = &vm1;
-    mask_bytes = sizeof vm1;
+    VariantMask<1> vm;
+    fill_mask<1>(vm, cmp, patternlen, threshold);
+    store_mask_kernel<1><<<1, 32, 0, st>>>(vm, reinterpret_cast<VariantMask<1>*>(scratch + kMaskOffset));
   } else {
-    fill_mask<2>(vm2, comp, patternlen, threshold);
-    host_mask = &vm2;
-    mask_bytes = sizeof vm2;
+    VariantMask<2> vm;
+    fill_mask<2>(vm, cmp, patternlen, threshold);
+    store_mask_kernel<2><<<1, 32, 0, st>>>(vm, reinterpret_cast<VariantMask<2>*>(scratch + kMaskOffset));
   }
-  // A copy from pageable host memory returns once the bytes are staged, so
-  // the stack structs may go out of scope afterwards.
-  if (cudaMemcpyAsync(scratch + kMaskOffset, host_mask, mask_bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
-    return COF_ERR_CUDA;
+  if (cudaGetLastError() != cudaSuccess) return COF_ERR_CUDA;
 
   GenomeView g;
   std::memset(&g, 0, sizeof g);

@@ -1,15 +1,19 @@
-// Integer-pipe throughput probe (cofx_pipe_rates, include/cof_tools.h).
+// Integer-pipe throughput probe: libcofrates.so, a measurement library that
+// bench.py loads beside the engine; it is not part of libcasoff.so.
 //
 // The comparer's roofline is set by the integer pipes, not by HBM or the tensor
 // cores, so its denominator is measured here on the running GPU: sustained
 // lane-operations per second of LOP3, POPC and IADD3, each from a kernel of
 // many independent dependency chains (enough warps and chains to saturate the
 // pipe), timed with CUDA events.
+//
+//   int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd);
+// measures on CUDA device `device`, in lane-operations per second: LOP3
+// (3-input logic), POPC (population count) and IADD (32-bit add).  Takes
+// about a second.  Returns 0 on success.
 #include <cuda_runtime.h>
 
 #include <cstdint>
-
-#include "../../include/cof_tools.h"
 
 namespace {
 

@@ -30,12 +30,6 @@ uint64_t cofx_synth_record(uint64_t seed, uint32_t record, uint64_t len, double 
  * uses: a genome byte is one of T, C, A, G or "any other byte"). */
 void cofx_mismatch_table(uint8_t* out);
 
-/* Measures sustained integer-pipe throughput on CUDA device `device`, in
- * lane-operations per second: LOP3 (3-input logic), POPC (population count)
- * and IADD (32-bit add).  These are the denominators of the comparer's
- * roofline.  Takes about a second.  Returns 0 on success. */
-int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd);
-
 /* Test hook: loads a FASTA or 2BIT file with the engine's loaders (no GPU
  * needed) and writes the reference's genome string (records joined by ';')
  * to `out` when `cap` suffices; *n = its length.  Returns 0, or 1 when the

@@ -12,7 +12,7 @@
  *   non_n_index         cas-offinder.cpp:60-70  (set_seq_flags)
  *   mism                cas-offinder.cl:30-43   (IUPAC mismatch predicate)
  *   find_candidates     cas-offinder.cl:157-213 (finder_cpu)
- *   compare_variant     cas-offinder.cl:214-286 (comparer_cpu)
+ *   compare_all         cas-offinder.cl:214-286 (comparer_cpu, every variant)
  *   format_hits         cas-offinder.cpp:394-455 (compareAll's row surgery)
  *   read_fasta          read_fasta.cpp:11-58
  *   read_twobit         read_twobit.cpp:44-131
@@ -325,9 +325,12 @@ bool read_twobit(const std::string& path, Genome& gn) {
 }
 
 // ---------------------------------------------------------------- search
+// A candidate start and its finder flag packed in one word: pos << 2 | flag.
+// flag 0: both strands, 1: forward only, 2: reverse only.
 struct Candidate {
-  uint64_t pos;
-  char flag;  // 0: both strands, 1: forward only, 2: reverse only
+  uint64_t v;
+  uint64_t pos() const { return v >> 2; }
+  char flag() const { return (char)(v & 3); }
 };
 struct Hit {
   uint64_t pos;
@@ -375,49 +378,84 @@ std::vector<Candidate> find_candidates(const std::string& chr, const std::string
       }
       if (flag == 3) continue;
       if (memchr(g + i, ';', L)) continue;
-      mine.push_back(Candidate{i, flag});
+      mine.push_back(Candidate{i << 2 | (uint64_t)flag});
     }
   }
-  for (auto& p : part) out.insert(out.end(), p.begin(), p.end());  // static schedule keeps order
+  size_t total = 0;
+  for (auto& p : part) total += p.size();
+  out.reserve(total);
+  for (auto& p : part) {  // static schedule: thread t holds the t-th range, so this keeps position order
+    out.insert(out.end(), p.begin(), p.end());
+    std::vector<Candidate>().swap(p);
+  }
   return out;
 }
 
-// Mismatches of `comp` at its non-N positions against chr[pos..], with the
-// reference's early exit once the count passes the threshold.
-inline unsigned count_mm(const char* g, const std::string& comp, const std::vector<int>& idx, unsigned thr) {
+// Mismatches of `comp` at its non-N positions against chr[pos..].  The
+// reference stops counting once the count passes the threshold and then
+// drops the candidate (cas-offinder.cl:241-243); this counts every position.
+// Both keep a candidate exactly when the full count is <= the threshold, and
+// then the two counts are equal, so the hits and their counts are the same.
+// Counting without the data-dependent exit avoids a mispredicted branch per
+// position, which made the early-exit loop several times slower.
+inline unsigned count_mm(const char* g, const char* comp, const int* idx, size_t n) {
   unsigned c = 0;
-  for (int k : idx)
-    if (mism(comp[k], g[k]) && ++c > thr) break;
+  for (size_t j = 0; j < n; ++j) c += g_mism[(unsigned char)comp[idx[j]]][(unsigned char)g[idx[j]]];
   return c;
 }
 
-// comparer_cpu (cas-offinder.cl:214-286), hits in work-item order.
-std::vector<Hit> compare_variant(const std::string& chr, const std::vector<Candidate>& cands,
-                                 const std::string& comp, uint16_t thr) {
-  const std::string rcomp = revcomp(comp);
-  const std::vector<int> fi = non_n_index(comp), ri = non_n_index(rcomp);
-  const int T = nthreads();
-  std::vector<std::vector<Hit>> part(T);
-#pragma omp parallel
-  {
-    std::vector<Hit>& mine = part[thread_id()];
-#pragma omp for schedule(static)
-    for (long long c = 0; c < (long long)cands.size(); ++c) {
-      const Candidate& cd = cands[c];
-      const char* g = chr.data() + cd.pos;
-      if (cd.flag == 0 || cd.flag == 1) {
-        unsigned m = count_mm(g, comp, fi, thr);
-        if (m <= thr) mine.push_back(Hit{cd.pos, (uint16_t)m, '+'});
-      }
-      if (cd.flag == 0 || cd.flag == 2) {
-        unsigned m = count_mm(g, rcomp, ri, thr);
-        if (m <= thr) mine.push_back(Hit{cd.pos, (uint16_t)m, '-'});
+// One compare variant as comparer_cpu sees it (cas-offinder.cpp:360-370 sets
+// its arguments): the compare string and its reverse complement, with the
+// non-N index lists of both, and the threshold.
+struct CompareArgs {
+  std::string comp, rcomp;
+  std::vector<int> fi, ri;
+  unsigned thr;
+};
+
+// comparer_cpu (cas-offinder.cl:214-286) for every variant: hits[v] holds
+// variant v's hits in work-item order ('+' before '-' for one candidate).
+// The candidates are cut into blocks that threads take in any order; a block
+// is tested against every variant while its windows are in cache, and the
+// per-block hit lists are joined in block order, so every variant's list is
+// the one a single sequential pass over all candidates gives.
+std::vector<std::vector<Hit>> compare_all(const std::string& chr, const std::vector<Candidate>& cands,
+                                          const std::vector<CompareArgs>& vs) {
+  const size_t V = vs.size();
+  std::vector<std::vector<Hit>> hits(V);
+  if (cands.empty() || V == 0) return hits;
+  const size_t B = 2048, nb = (cands.size() + B - 1) / B;
+  std::vector<std::vector<Hit>> blk_hits(nb);
+  std::vector<std::vector<uint32_t>> blk_off(nb);  // variant v's hits of block b: [off[v], off[v+1])
+#pragma omp parallel for schedule(dynamic, 4)
+  for (long long bb = 0; bb < (long long)nb; ++bb) {
+    const size_t c0 = (size_t)bb * B, c1 = std::min(cands.size(), c0 + B);
+    std::vector<Hit>& H = blk_hits[bb];
+    std::vector<uint32_t>& off = blk_off[bb];
+    off.resize(V + 1);
+    for (size_t v = 0; v < V; ++v) {
+      off[v] = (uint32_t)H.size();
+      const CompareArgs& a = vs[v];
+      for (size_t c = c0; c < c1; ++c) {
+        const uint64_t pos = cands[c].pos();
+        const char flag = cands[c].flag();
+        const char* g = chr.data() + pos;
+        if (flag == 0 || flag == 1) {
+          const unsigned m = count_mm(g, a.comp.data(), a.fi.data(), a.fi.size());
+          if (m <= a.thr) H.push_back(Hit{pos, (uint16_t)m, '+'});
+        }
+        if (flag == 0 || flag == 2) {
+          const unsigned m = count_mm(g, a.rcomp.data(), a.ri.data(), a.ri.size());
+          if (m <= a.thr) H.push_back(Hit{pos, (uint16_t)m, '-'});
+        }
       }
     }
+    off[V] = (uint32_t)H.size();
   }
-  std::vector<Hit> out;
-  for (auto& p : part) out.insert(out.end(), p.begin(), p.end());
-  return out;
+  for (size_t v = 0; v < V; ++v)
+    for (size_t b = 0; b < nb; ++b)
+      hits[v].insert(hits[v].end(), blk_hits[b].begin() + blk_off[b][v], blk_hits[b].begin() + blk_off[b][v + 1]);
+  return hits;
 }
 
 // compareAll's per-hit row construction (cas-offinder.cpp:394-455).
@@ -519,11 +557,22 @@ void search_file(const std::string& path, const Input& in, std::ostream& os, con
   }
   const bool want_summary = !summary_path.empty();
   const std::vector<Candidate> cands = find_candidates(gn.seq, in.pattern);
+  // compareAll (cas-offinder.cpp:356) walks the variants in std::map key order.
+  std::vector<CompareArgs> args;
+  std::vector<const std::pair<const std::string, Variant>*> order;
   for (const auto& kv : in.variants) {
-    if (cands.empty()) break;
-    const std::vector<Hit> hits = compare_variant(gn.seq, cands, kv.first, kv.second.threshold);
-    format_hits(os, gn, in, kv.first, kv.second, hits, want_summary ? &summary : nullptr);
+    CompareArgs a;
+    a.comp = kv.first;
+    a.rcomp = revcomp(kv.first);
+    a.fi = non_n_index(a.comp);
+    a.ri = non_n_index(a.rcomp);
+    a.thr = kv.second.threshold;
+    args.push_back(std::move(a));
+    order.push_back(&kv);
   }
+  const std::vector<std::vector<Hit>> hits = compare_all(gn.seq, cands, args);
+  for (size_t v = 0; v < order.size(); ++v)
+    format_hits(os, gn, in, order[v]->first, order[v]->second, hits[v], want_summary ? &summary : nullptr);
   os.flush();
   if (want_summary) write_summary(summary_path, summary);
 }

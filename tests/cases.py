@@ -181,3 +181,63 @@ def row_problems(row: str):
     elif low != mm:
         out.append(f"{low} lower-case != {mm}")
     return out
+
+
+# ---------------------------------------------------------------- kernel restatement
+def mismatch_table():
+    """The reference kernel's mismatch predicate as a 256 x 256 table
+    [pattern byte][genome byte] (golden fixture dumped from cas-offinder.cl)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "mismatch_table.bin")
+    return np.fromfile(path, np.uint8).reshape(256, 256)
+
+
+def _revcomp_bytes(s):
+    return bytes(s[::-1]).translate(bytes.maketrans(b"ACGTRYKMHDBV", b"TGCAYRMKDHVB"))
+
+
+def _mismatch_counts(M, g, s, starts):
+    """Mismatches of pattern string `s` against g[i:i+len(s)] for each i in `starts`."""
+    cnt = np.zeros(len(starts), np.int32)
+    for k, p in enumerate(bytes(s)):
+        col = M[p]
+        if col.any():
+            cnt += col[g[starts + k]]
+    return cnt
+
+
+def restate_finder(text, pattern):
+    """finder_cpu (cas-offinder.cl:157-213) over every start of `text` (the
+    reference's genome string), in work-item order: (loci, flags) with flag
+    0 both strands, 1 forward only, 2 reverse only.  Windows holding ';' are
+    dropped."""
+    M = mismatch_table()
+    g = np.frombuffer(bytes(text), np.uint8)
+    L = len(pattern)
+    npos = max(len(g) - L + 1, 0)
+    starts = np.arange(npos, dtype=np.int64)
+    fwd = _mismatch_counts(M, g, pattern, starts) > 0
+    rev = _mismatch_counts(M, g, _revcomp_bytes(pattern), starts) > 0
+    sep = np.convolve((g == ord(";")).astype(np.int32), np.ones(L, np.int32), "valid")[:npos] > 0
+    flag = fwd.astype(np.int32) * 2 + rev.astype(np.int32)
+    keep = (flag != 3) & ~sep
+    return starts[keep], flag[keep]
+
+
+def restate_comparer(text, loci, flags, comp, threshold):
+    """comparer_cpu (cas-offinder.cl:214-286) for one compare string: hits as
+    (start, '-' strand, mismatches), ordered by candidate then '+' before '-'.
+    The reference stops counting past the threshold and then drops the
+    candidate, so a full count gives the same hits."""
+    M = mismatch_table()
+    g = np.frombuffer(bytes(text), np.uint8)
+    loci = np.asarray(loci, np.int64)
+    flags = np.asarray(flags)
+    fwd = _mismatch_counts(M, g, comp, loci)
+    rev = _mismatch_counts(M, g, _revcomp_bytes(comp), loci)
+    out = []
+    for i, f, a, b in zip(loci.tolist(), flags.tolist(), fwd.tolist(), rev.tolist()):
+        if f in (0, 1) and a <= threshold:
+            out.append((i, False, a))
+        if f in (0, 2) and b <= threshold:
+            out.append((i, True, b))
+    return out

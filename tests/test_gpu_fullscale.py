@@ -1,18 +1,16 @@
 """Full-scale plain search (the 3.1 Gbp synthetic genome of 24 records, NRG
-with DNA bulge 2 and RNA bulge 1, 4 guides, mm 5) checked through properties
-that hold at any size:
+with DNA bulge 2 and RNA bulge 1, 4 guides, mm 5):
 
-- prefix parity: the rows inside the first 20 Mbp of chr1 are byte for byte
-  the oracle's rows for that 20 Mbp prefix (windows that reach the prefix end
-  excluded on both sides);
+- whole-genome parity: every row of the GPU search, over all 24 records and
+  all 47 segments of 2^26 start positions (so every segment boundary), is
+  byte for byte the oracle's row, in the same order, the oracle searching
+  the same genome written as 2BIT by the standalone writer;
 - every sampled row is consistent with the genome: its DNA column is a
   window at the reported location and strand, lower case exactly where the
   IUPAC rule says mismatch against an aligned crRNA letter, and the number of
   lower-case letters equals the mismatch column (at most the guide's limit;
   at most the column for '-' strand RNA-bulge rows, whose shown window is
-  cut short).  The same checks hold on every row of the golden fixtures.
-Row order is covered by the prefix comparison (the same rows in the same
-order)."""
+  cut short).  The same checks hold on every row of the golden fixtures."""
 import os
 import random
 import sys
@@ -25,7 +23,6 @@ import cases
 pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-PREFIX = 20_000_000
 COMP = bytes.maketrans(b"ACGTRYKMBVDHacgtrykmbvdh", b"TGCAYRMKVBHDtgcayrmkvbhd")
 
 
@@ -47,21 +44,15 @@ def full(P, built):
     return bench, buf, names, starts, guides, rows
 
 
-def test_prefix_rows_equal_the_oracle(full, oracle, tmp_path):
+def test_whole_genome_rows_equal_the_oracle(full, oracle, tmp_path):
     bench, buf, names, starts, guides, rows = full
-    dt, nrows = bench.cpu_sample_run(oracle, buf, names, starts, PREFIX, guides, os.cpu_count() or 1,
-                                     str(tmp_path))
-    want_all = cases.rows_of(open(os.path.join(str(tmp_path), "sample_out.tsv"), "rb").read())
-    cut = PREFIX - 128
-
-    def inside(r):
-        f = r.split(b"\t")
-        return f[4] == names[0].encode() and int(f[5]) < cut
-
-    got = [r for r in cases.rows_of(rows) if inside(r)]
-    want = [r for r in want_all if inside(r)]
-    assert len(want) > 1000
-    assert got == want
+    lens = bench.genome_lengths(3.1e9)
+    assert [s for s in starts] == [sum(lens[:i]) + i for i in range(len(lens))]
+    path = bench.write_genome(str(tmp_path / "genome.2bit"), lens)
+    _, want = bench.oracle_rows(oracle, bench.input_text(path, guides), os.cpu_count() or 1, str(tmp_path), "full")
+    c = bench.compare_rows(rows, want)
+    assert c["rows_compared"] > 1_000_000
+    assert c["identical"], c["first_difference"]
 
 
 def test_sampled_rows_agree_with_the_genome(full):

@@ -204,40 +204,29 @@ def read_fasta(path):
 
 def test_kernel_level_chunk_abi(P, built, tmp_path):
     """cof_finder_chunk / cof_comparer_chunk (the OpenCL kernels' contracts)
-    against a direct restatement of finder_cpu/comparer_cpu on a small chunk."""
+    against the numpy restatement of finder_cpu/comparer_cpu (cases.py,
+    itself checked against the reference's rows) on a small chunk: concrete,
+    IUPAC-coded and 2-word compare strings."""
     names, seqs = read_fasta(os.path.join(GOLDEN, "ngg_fasta", "genome.fa"))
     text, _ = P.reference_text(seqs)
     text = text[:30000]
-    pattern = b"N" * 21 + b"GG"
-    L = len(pattern)
-    rc = bytes(pattern[::-1].translate(bytes.maketrans(b"ACGTRYKMHDBV", b"TGCAYRMKDHVB")))
-    worksize = len(text) - L + 1
+    rc_tab = bytes.maketrans(b"ACGTRYKMHDBV", b"TGCAYRMKDHVB")
     with P.CasOFFinder(0) as eng:
-        loci, flag = eng.finder_chunk(text, worksize, pattern + rc, L)
-        # finder_cpu: GG at +21 on '+', CC at +0 on '-'; windows with ';' dropped
-        exp = []
-        for i in range(worksize):
-            win = text[i:i + L]
-            f = win[21:23] == b"GG"
-            r = win[0:2] == b"CC"
-            if (f or r) and b";" not in win:
-                exp.append((i, 0 if (f and r) else (1 if f else 2)))
-        assert list(zip(loci.tolist(), flag.tolist())) == exp
-        comp = b"GGCCGACCTGTCGCTGACGCNNN"
-        mm_loci, mm_count, direction = eng.comparer_chunk(text, loci, flag, comp, 9)
-        rcomp = comp[::-1].translate(bytes.maketrans(b"ACGT", b"TGCA"))
-        exp_hits = []
-        for i, fl in zip(loci.tolist(), flag.tolist()):
-            win = text[i:i + L]
-            for s, c in ((b"+", comp), (b"-", rcomp)):
-                if (s == b"+" and fl == 2) or (s == b"-" and fl == 1):
-                    continue
-                m = sum(1 for k in range(L) if c[k:k + 1] != b"N" and win[k] != c[k])
-                if m <= 9:
-                    exp_hits.append((i, m, s))
-        got = list(zip(mm_loci.tolist(), mm_count.tolist(), [bytes([x]) for x in direction]))
-        assert got == exp_hits
-        assert len(got) > 0
+        for pattern, queries in (
+                (b"N" * 21 + b"GG", [(b"GGCCGACCTGTCGCTGACGCNNN", 9), (b"GGCCRACCTGYCGCTGASGCNNN", 8),
+                                     (b"ACGTHBVDACGTWSKMACGTNNN", 12)]),
+                (b"N" * 45 + b"NGG", [(b"GGCCGACCTGTCGCTGACGCAGTCRYACGGTTACGATCGATCGAANNN", 26)])):
+            L = len(pattern)
+            worksize = len(text) - L + 1
+            loci, flag = eng.finder_chunk(text, worksize, pattern + pattern[::-1].translate(rc_tab), L)
+            exp_loci, exp_flag = cases.restate_finder(text, pattern)
+            assert loci.tolist() == exp_loci.tolist()
+            assert flag.tolist() == exp_flag.tolist()
+            for comp, thr in queries:
+                mm_loci, mm_count, direction = eng.comparer_chunk(text, loci, flag, comp, thr)
+                got = list(zip(mm_loci.tolist(), [d == ord("-") for d in direction], mm_count.tolist()))
+                assert got == cases.restate_comparer(text, loci, flag, comp, thr), comp
+                assert len(got) > 0, comp
 
 
 @pytest.mark.parametrize("spec", RANDOM_CASES[:5], ids=[str(c["seed"]) for c in RANDOM_CASES[:5]])

@@ -101,3 +101,40 @@ def test_golden_rows_obey_the_row_rules():
             assert not cases.row_problems(row.decode()), (case, row)
             n += 1
     assert n > 4000
+
+
+def _fasta_records(path):
+    names, seqs = [], []
+    for line in open(path, "rb").read().split(b"\n"):
+        line = line.rstrip(b"\r")
+        if line.startswith(b">"):
+            names.append(line[1:].decode())
+            seqs.append(bytearray())
+        elif line:
+            seqs[-1] += line.upper()
+    return names, seqs
+
+
+@pytest.mark.parametrize("case", ["ngg_fasta", "iupac_nngrrt"])
+def test_kernel_restatement_matches_reference_golden(case, P):
+    """cases.restate_finder / restate_comparer (the numpy restatement of
+    finder_cpu and comparer_cpu that the chunk-level GPU tests check against)
+    give, guide by guide, exactly the hits of the reference's rows on two
+    fixtures without bulges, one of them with IUPAC codes in the guides."""
+    d = os.path.join(GOLDEN, case)
+    lines = open(os.path.join(d, "input.txt")).read().split("\n")
+    pattern = lines[1].split()[0].upper().encode()
+    names, seqs = _fasta_records(os.path.join(d, "genome.fa"))
+    text, starts = P.reference_text(seqs)
+    loci, flags = cases.restate_finder(text, pattern)
+    rows = cases.rows_of(open(os.path.join(d, "expected.tsv"), "rb").read())
+    total = 0
+    for no, line in enumerate(l for l in lines[2:] if l.strip()):
+        tok = line.split()
+        gid = tok[2] if len(tok) == 3 else str(no)
+        want = sorted((starts[names.index(r[4].decode())] + int(r[5]), r[6] == b"-", int(r[7]))
+                      for r in (x.split(b"\t") for x in rows) if r[0].decode() == gid)
+        got = sorted(cases.restate_comparer(text, loci, flags, tok[0].upper().encode(), int(tok[1])))
+        assert got == want, gid
+        total += len(got)
+    assert total == len(rows) > 0
