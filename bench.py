@@ -130,10 +130,19 @@ def served_requests(seed=9, n=12, genome_path="synthetic"):
     return out
 
 
+def percentile(xs, q):
+    """Nearest-rank percentile (q in [0, 1]) of a list of numbers."""
+    ys = sorted(xs)
+    return ys[min(len(ys) - 1, max(0, int(round(q * (len(ys) - 1)))))]
+
+
 def run_served(P, eng, lens, args, capture=None):
-    """Served mode: the same requests arriving as a Poisson stream at several
-    rates; p50/p99 latency (submit to rows in host memory) and guide-Gbp/s,
-    against the plain path run once per request."""
+    """Served mode: the same request list arriving as a Poisson stream at each
+    rate; per rate p50/p99 latency (submit to rows in host memory) over every
+    request, where each request's latency went (admission, table build, ring
+    pass, formatting), and whole-run guide-Gbp/s, against the plain path run
+    once per request."""
+    import ctypes
     import random
     import statistics
     import threading
@@ -150,53 +159,54 @@ def run_served(P, eng, lens, args, capture=None):
         eng.timer_start()
         eng.search_view()
         plain_ms.append(eng.timer_stop())
-    out = {"workload": f"{len(reqs)} requests, 1-512 guides each (log-uniform; {guides} guides), PAM NGG/NRG/"
-                       "NNGRRT/TTTV, mm 2-6, DNA/RNA bulge 0-2, on the same 3.1 Gbp genome",
+    out = {"workload": f"{len(reqs)} requests per rate, 1-512 guides each (log-uniform; {guides} guides), PAM NGG/"
+                       "NRG/NNGRRT/TTTV, mm 2-6, DNA/RNA bulge 0-2, on the same 3.1 Gbp genome",
            "plain_value": guides * gbp / (sum(plain_ms) / 1e3), "unit": "guide-Gbp/s",
-           "plain_latency_ms": {"p50": statistics.median(plain_ms), "max": max(plain_ms)}, "rates": []}
+           "plain_latency_ms": {"p50": statistics.median(plain_ms), "p99": percentile(plain_ms, 0.99),
+                                "max": max(plain_ms)}, "rates": []}
+    keep = [f"chr{i + 1}" for i in range(VERIFY_SERVED_RECORDS)]
+    pick = sorted(range(len(reqs)), key=lambda j: (reqs[j][1], j))[:VERIFY_SERVED_REQUESTS]
+    stages = ("admission", "build", "ring", "format")
     for rate in args.served_rates:
         rng = random.Random(int(rate * 1000))
-        lat, tickets = [None] * len(reqs), [None] * len(reqs)
+        lat, parts = [None] * len(reqs), [None] * len(reqs)
+        kept = {}
+        verify_here = capture is not None and rate == args.served_rates[-1]
         with P.Server(eng) as srv:
             t0 = time.perf_counter()
 
-            # Each arrival is submitted from its own thread, as concurrent
-            # callers would (submit parses the input file on the caller's
-            # thread).
-            def submit(j, at):
+            # Each arrival is submitted from its own thread, as a concurrent
+            # caller would (submit parses the input file on the caller's
+            # thread), which then waits for its rows and releases them.
+            def client(j, at):
                 d = at - time.perf_counter()
                 if d > 0:
                     time.sleep(d)
-                tickets[j] = srv.submit(reqs[j][0])
+                t = srv.submit(reqs[j][0])
+                addr, n, lat[j] = srv.wait_view(t)
+                parts[j] = srv.timing(t)
+                if verify_here and j in pick:
+                    kept[j] = rows_of_records(ctypes.string_at(addr, n), keep)
+                srv.release(t)
 
             threads, at = [], t0
             for j in range(len(reqs)):
                 at += rng.expovariate(rate)
-                threads.append(threading.Thread(target=submit, args=(j, at)))
+                threads.append(threading.Thread(target=client, args=(j, at)))
                 threads[-1].start()
             for th in threads:
                 th.join()
-            views = [None] * len(reqs)
-            for j in range(len(reqs)):
-                views[j] = srv.wait_view(tickets[j])  # rows left in the server's pinned buffer
-                lat[j] = views[j][2]
             span = time.perf_counter() - t0
-            if capture is not None and rate == args.served_rates[-1]:
-                import ctypes
-                keep = [f"chr{i + 1}" for i in range(VERIFY_SERVED_RECORDS)]
-                pick = sorted(range(len(reqs)), key=lambda j: (reqs[j][1], j))[:VERIFY_SERVED_REQUESTS]
-                capture["served"] = {"records": VERIFY_SERVED_RECORDS, "rate": rate,
-                                     "rows": {j: rows_of_records(ctypes.string_at(views[j][0], views[j][1]), keep)
-                                              for j in pick}}
-                capture["served_n"] = len(reqs)
-            for j in range(len(reqs)):
-                srv.release(tickets[j])
             st = srv.stats()
-        lat_sorted = sorted(lat)
-        p99 = lat_sorted[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
-        out["rates"].append({"arrivals_per_s": rate, "p50_ms": statistics.median(lat), "p99_ms": p99,
-                             "value": guides * gbp / span, "makespan_s": span, "max_active": st["max_active"],
-                             "ring_steps": st["steps"]})
+        if verify_here:
+            capture["served"] = {"records": VERIFY_SERVED_RECORDS, "rate": rate, "rows": kept}
+            capture["served_n"] = len(reqs)
+        out["rates"].append({
+            "arrivals_per_s": rate, "requests": len(reqs), "p50_ms": statistics.median(lat),
+            "p99_ms": percentile(lat, 0.99), "value": guides * gbp / span, "makespan_s": span,
+            "max_active": st["max_active"], "ring_steps": st["steps"],
+            "latency_parts_ms": {k: {"p50": statistics.median(p[k] for p in parts),
+                                     "mean": statistics.fmean(p[k] for p in parts)} for k in stages}})
     out["value"] = max(r["value"] for r in out["rates"])
     out["speedup_vs_plain"] = out["value"] / out["plain_value"]
     return out
@@ -562,7 +572,7 @@ def main():
     ap.add_argument("--comparer", default="auto", choices=["auto", "popcount", "bitsliced"],
                     help="comparer kernel for the plain search (default: bit-sliced where it fits)")
     ap.add_argument("--no-verify", action="store_true", help="skip the byte comparison with the oracle")
-    ap.add_argument("--served-requests", type=int, default=12)
+    ap.add_argument("--served-requests", type=int, default=200, help="requests per arrival rate")
     ap.add_argument("--served-rates", type=float, nargs="+", default=[1.0, 2.0, 5.0, 10.0, 20.0, 50.0, 100.0, 200.0])
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
@@ -659,6 +669,7 @@ def main():
                  f"comparisons per test; measured LOP3 {rates['lop3'] / 1e12:.2f}, POPC {rates['popc'] / 1e12:.2f} "
                  f"T lane-ops/s")
     traffic = committed_traffic("comparer")
+    issued = issued_roofline(eng, cmp, rates)
     # Finder bytes: 0.375 B of planes read per position scanned plus the 4 B
     # queue entry written per candidate; the profiled search runs each
     # finder launch alone, so its events time the kernel itself.
@@ -725,7 +736,7 @@ def main():
             "roofline": {"bound": "int-pipe", "kernel": "comparer", "achieved": achieved, "peak": peak,
                          "unit": "G base-comparisons/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,
-                         "peak_basis": basis, "base_comparisons_per_test": mean_nonN},
+                         "peak_basis": basis, "base_comparisons_per_test": mean_nonN, "issued": issued},
             "roofline_finder": {"bound": "hbm", "achieved": finder_gbs, "peak": peaks.get("hbm_gbs"),
                                 "unit": "GB/s", "frac": finder_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs")
                                 else None, "bytes_per_launch": finder_bytes / max(fnd["launches"], 1),
@@ -794,6 +805,28 @@ def run_batched(P, eng, lens, rates, args, capture=None):
         eng.readInputFile(t)
         eng.search_view()
     plain_ms = eng.timer_stop() / k
+    # Where a plain input's time goes: setup (parse, table upload, the
+    # autotuner's timed trial launches, CUDA-graph capture: the first search
+    # of an input minus a repeat) and the search itself (the repeat), with the
+    # autotuner on (the default) and off.
+    split = {}
+    for tune in (True, False):
+        eng.set_autotune(tune)
+        setup, search = [], []
+        for t in texts[:k]:
+            eng.synchronize()
+            t0 = time.perf_counter()
+            eng.readInputFile(t)
+            eng.search_view()
+            t1 = time.perf_counter()
+            eng.search_view()
+            t2 = time.perf_counter()
+            search.append((t2 - t1) * 1e3)
+            setup.append(max(0.0, (t1 - t0) * 1e3 - search[-1]))
+        split["autotune_on" if tune else "autotune_off"] = {
+            "setup_ms": statistics.fmean(setup), "search_ms": statistics.fmean(search),
+            "speedup_vs_plain_search_only": statistics.fmean(search) * len(texts) / ms}
+    eng.set_autotune(True)
     achieved = cmp["units"] / (cmp["ms"] * 1e-3) / 1e9 if cmp["ms"] else 0.0
     peak = rates["lop3"] * 16 / 1e9
     return {
@@ -802,10 +835,13 @@ def run_batched(P, eng, lens, rates, args, capture=None):
         "value": len(texts) * gbp / (ms / 1e3), "unit": "guide-Gbp/s", "ms_per_step": ms,
         "steps": args.batched_steps, "variants": info["variants"], "hits": hits, "rows": rows,
         "plain_value": gbp / (plain_ms / 1e3), "plain_ms_per_input": plain_ms, "plain_sample_inputs": k,
+        "plain_setup_ms": split["autotune_on"]["setup_ms"], "plain_search_ms": split["autotune_on"]["search_ms"],
+        "plain_split": split,
         "speedup_vs_plain": (plain_ms * len(texts)) / ms, "kernel_ms_profiled": kernel_ms,
         "comparer_schedule": schedule,
         "comparer_roofline": {"achieved": achieved, "peak": peak, "unit": "G base-comparisons/s",
-                              "frac": achieved / peak if peak else None},
+                              "frac": achieved / peak if peak else None,
+                              "issued": issued_roofline(eng, cmp, rates)},
     }
 
 
@@ -855,8 +891,26 @@ def run_pam_variety(P, eng, lens, rates, args, capture=None):
         "sequential_value": guides * gbp / (seq_ms / 1e3), "sequential_ms": seq_ms,
         "speedup_vs_sequential": seq_ms / ms, "kernel_ms_profiled": kernel_ms, "comparer_schedule": schedule,
         "comparer_roofline": {"achieved": achieved, "peak": peak, "unit": "G base-comparisons/s",
-                              "frac": achieved / peak if peak else None},
+                              "frac": achieved / peak if peak else None,
+                              "issued": issued_roofline(eng, cmp, rates)},
     }
+
+
+def issued_roofline(eng, cmp, rates):
+    """The bit-sliced comparer against the LOP3 pipe by the instructions it
+    issues: the engine's op model counts, per launch, the lane LOP3
+    instructions of the count phase (full count, bias, update steps, votes;
+    ceil(candidates / 64) pairs x 32 lanes x chunks x the per-lane count of the
+    group's slots and program length), and this divides them by the comparer's
+    time and the measured LOP3 rate.  Unlike the base-comparison figure it
+    does not credit the lane programs for the work their steps avoid."""
+    ops = eng.kernel_stats("comparer.lop3")["units"]
+    if not ops or not cmp["ms"]:
+        return None
+    achieved = ops / (cmp["ms"] * 1e-3)
+    return {"lop3_lane_ops": ops, "achieved": achieved / 1e12, "peak": rates["lop3"] / 1e12,
+            "unit": "T lane-LOP3/s", "frac": achieved / rates["lop3"],
+            "model": "count phase only (the table build's transposes and class words are not counted)"}
 
 
 def committed_traffic(kernel):

@@ -39,6 +39,7 @@ EXPORTS = [
     "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cof_search_chunk_static",
     "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
     "cof_server_start", "cof_server_submit", "cof_server_wait", "cof_server_release", "cof_server_stats",
+    "cof_server_timing",
     "cof_server_set_hit_reserve", "cof_server_memory", "cof_server_last_error", "cof_server_stop",
     "cof_router_open", "cof_router_add_genome", "cof_router_drop_genome", "cof_router_genomes", "cof_router_submit",
     "cof_router_wait", "cof_router_release", "cof_router_last_error", "cof_router_close",
@@ -119,6 +120,7 @@ def lib():
             "cof_server_wait": (c.c_int, [vp, u64, c.c_int, c.POINTER(c.c_void_p), c.POINTER(sz),
                                           c.POINTER(c.c_double)]),
             "cof_server_release": (c.c_int, [vp, u64]),
+            "cof_server_timing": (c.c_int, [vp, u64] + [c.POINTER(c.c_double)] * 4),
             "cof_server_stats": (c.c_int, [vp] + [c.POINTER(u64)] * 6),
             "cof_server_set_hit_reserve": (c.c_int, [vp, u64]),
             "cof_server_memory": (c.c_int, [vp] + [c.POINTER(u64)] * 3),
@@ -506,6 +508,14 @@ class Server:
 
     def release(self, ticket):
         self._L.cof_server_release(self._s, ticket)
+
+    def timing(self, ticket):
+        """Latency stages of a finished request (ms): admission, build, ring, format."""
+        vals = [ctypes.c_double() for _ in range(4)]
+        st = self._L.cof_server_timing(self._s, ticket, *[ctypes.byref(v) for v in vals])
+        if st != COF_OK:
+            raise CofError(st, "cof_server_timing")
+        return dict(zip(("admission", "build", "ring", "format"), (v.value for v in vals)))
 
     def stats(self):
         vals = [ctypes.c_uint64() for _ in range(6)]

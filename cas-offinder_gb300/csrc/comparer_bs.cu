@@ -42,6 +42,30 @@ uint32_t bs_class_of(unsigned char p) {
   }
 }
 
+namespace {
+// LOP3-class instructions of CountTree<N, LEV, NB> (comparer_bs.cuh) that
+// survive dead-code elimination: a level's sums (xor3 / xor) only while LEV <
+// NB, its carries (maj3 / and) only while LEV + 1 < NB.
+int tree_ops(int N, int LEV, int NB) {
+  if (N <= 1) return 0;
+  const int fa = N >= 3 ? (N - 1) / 2 : 0, left = N - 2 * fa, carry = fa + (left == 2 ? 1 : 0);
+  const int per = (LEV < NB ? 1 : 0) + (LEV + 1 < NB ? 1 : 0);
+  return (fa + (left == 2 ? 1 : 0)) * per + tree_ops(carry, LEV + 1, NB);
+}
+int width_of(int s) { return s <= 1 ? 1 : 1 + width_of(s >> 1); }
+}  // namespace
+
+double bs_lane_lop3(int slots, uint32_t m) {
+  const int NB = width_of(slots), NP = NB + 1;
+  double ops = 2.0 * tree_ops(slots, 0, NB);  // full count of the first variant, groups a and b
+  if (m <= 1) return ops + 2.0 * NB;          // carry of count + bias, per group
+  ops += 2.0 * 2 * NB;                        // add_bias: xor3 + maj3 per plane, per group
+  const uint32_t ns = m - 1;
+  ops += (double)ns * 2 * (2 * NP);           // step_update: t = a ^ b, NP xors, NP - 1 lop3, per group
+  ops += (double)(ns / 2) * 3 + (ns & 1);     // votes: t0, t1, t0 & t1 per pair of steps; one for a lone step
+  return ops;
+}
+
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                         const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
                         uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,

@@ -896,6 +896,9 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
         const PatternGroup& g = h->groups[idx % G];
         p.units = (double)qc[idx] * g.nonN_sum;
         h->stats["comparer.tests"].units += (double)qc[idx] * (double)g.gids.size();
+        if (g.bs_slots && g.bs_chunks)  // lane LOP3 ops the bit-sliced count issues (op model)
+          h->stats["comparer.lop3"].units +=
+              (double)((qc[idx] + 63) / 64) * 32.0 * g.bs_chunks * bs_lane_lop3(g.bs_slots, g.bs_m);
         h->stats["finder.candidates"].units += (double)qc[idx];  // queue entries the finder wrote
       }
     collect(h, evs);

@@ -135,6 +135,12 @@ bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32
                         const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
                         uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,
                         unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
+// Op model of the count phase: LOP3-class logic instructions one lane issues
+// per pair of 32-candidate groups for a lane program of m variants with
+// `slots` class words (full count, bias, m - 1 update steps, hit votes; hit
+// emission and the table build aside).  Every lane of a launch runs the same
+// count, so a launch issues ceil(candidates / 64) * 32 * chunks times this.
+double bs_lane_lop3(int slots, uint32_t m);
 int bs_slots_for(int max_positions);  // 0 when more than 32 positions can mismatch
 int bs_row_for(uint32_t L);           // words per class row of the shared table
 uint32_t bs_class_of(unsigned char p);  // class row of a pattern byte (0: never mismatches)

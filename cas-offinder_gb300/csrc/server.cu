@@ -66,7 +66,8 @@ struct Request {
   uint64_t ticket = 0;
   Job job;
   uint32_t nvar = 0;
-  double t_submit = 0, t_admit = 0, t_done = 0;
+  // submit, admitted, first step with its tables, ring complete, rows in host memory
+  double t_submit = 0, t_admit = 0, t_adopt = 0, t_ran = 0, t_done = 0;
   // worker-owned until handed to the finisher
   uint64_t steps_seen = 0;
   bool ran = false;  // has completed the ring (or failed): no more hits
@@ -482,6 +483,9 @@ void worker_main(cof_server* s) {
         st = upload_group(h, pg, fresh->host[g], h->stream);
       }
       s->tables = std::move(fresh);
+      const double t = now_s();
+      for (const ReqPtr& r : s->tables->reqs)
+        if (r->t_adopt == 0) r->t_adopt = t;
       if (st) {
         std::lock_guard<std::mutex> lock(s->mu);
         for (const ReqPtr& r : s->tables->reqs)
@@ -509,6 +513,10 @@ void worker_main(cof_server* s) {
     std::vector<ReqPtr> finished;
     for (const ReqPtr& r : s->tables->reqs)
       if (!r->ran && (st || ++r->steps_seen >= s->ring)) finished.push_back(r);
+    if (!finished.empty()) {
+      const double t = now_s();
+      for (const ReqPtr& r : finished) r->t_ran = t;
+    }
     if (!finished.empty()) {
       std::lock_guard<std::mutex> lock(s->mu);
       for (const ReqPtr& r : finished) {
@@ -618,7 +626,7 @@ cof_status cof_server_submit(cof_server* s, const char* text, size_t len, uint64
     s->tickets[r->ticket] = r;
     if (r->nvar == 0) {  // nothing to search: done at once
       r->done = r->ran = true;
-      r->t_admit = r->t_done = r->t_submit;
+      r->t_admit = r->t_adopt = r->t_ran = r->t_done = r->t_submit;
       ++s->completed;
       s->cv_done.notify_all();
       return COF_OK;
@@ -644,6 +652,22 @@ cof_status cof_server_wait(cof_server* s, uint64_t ticket, int timeout_ms, const
   if (latency_ms) *latency_ms = (r->t_done - r->t_submit) * 1e3;
   if (r->status) s->last_error = r->err;
   return r->status;
+}
+
+cof_status cof_server_timing(cof_server* s, uint64_t ticket, double* admission_ms, double* build_ms, double* ring_ms,
+                             double* format_ms) {
+  if (!s) return COF_ERR_ARG;
+  std::lock_guard<std::mutex> lock(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end() || !it->second->done) return COF_ERR_ARG;
+  const Request& r = *it->second;
+  // A request that failed before its tables were adopted has no later stages.
+  const double adopt = r.t_adopt ? r.t_adopt : r.t_admit, ran = r.t_ran ? r.t_ran : adopt;
+  if (admission_ms) *admission_ms = (r.t_admit - r.t_submit) * 1e3;
+  if (build_ms) *build_ms = (adopt - r.t_admit) * 1e3;
+  if (ring_ms) *ring_ms = (ran - adopt) * 1e3;
+  if (format_ms) *format_ms = (r.t_done - ran) * 1e3;
+  return COF_OK;
 }
 
 cof_status cof_server_release(cof_server* s, uint64_t ticket) {

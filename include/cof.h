@@ -177,6 +177,16 @@ cof_status cof_server_submit(cof_server* s, const char* text, size_t len, uint64
 cof_status cof_server_wait(cof_server* s, uint64_t ticket, int timeout_ms, const char** rows, size_t* rows_len,
                            double* latency_ms);
 cof_status cof_server_release(cof_server* s, uint64_t ticket);
+/* Where a finished request's latency went (after cof_server_wait, before
+ * cof_server_release), in ms; the four add up to its latency:
+ *   admission  submit -> admitted (waiting for the variant and hit budgets)
+ *   build      admitted -> its comparer tables in use (host table build, then
+ *              the next ring step boundary)
+ *   ring       one full ring of steps with its tables
+ *   format     ring done -> rows sorted, formatted and in host memory.
+ * No counterpart in the reference, which has no request queue. */
+cof_status cof_server_timing(cof_server* s, uint64_t ticket, double* admission_ms, double* build_ms, double* ring_ms,
+                             double* format_ms);
 cof_status cof_server_stats(cof_server* s, uint64_t* steps, uint64_t* admitted, uint64_t* completed,
                             uint64_t* pending, uint64_t* active, uint64_t* max_active);
 /* Hit memory charged per running request at least (default 64 MiB); applies
@@ -326,7 +336,9 @@ cof_status cof_comparer_info(const cof_handle* h, int* kind, int* slots);
 /* ---- instrumentation: per-kernel CUDA-event timing on the engine's stream. */
 cof_status cof_set_profiling(cof_handle* h, int enable);
 /* Totals since profiling was enabled for kernel `name` ("finder", "comparer",
- * "format"; "comparer.tests" counts variant tests in `units`): launches,
+ * "format"; "comparer.tests" counts variant tests in `units`,
+ * "comparer.lop3" the lane LOP3 instructions the bit-sliced comparer's count
+ * issues by its op model, "finder.candidates" the queue entries written): launches,
  * summed device milliseconds and algorithmic units
  * (finder: genome positions scanned; comparer: base comparisons, i.e. the
  * non-N positions of each compare variant times the strand-oriented
