@@ -564,6 +564,10 @@ def main():
     ap.add_argument("--genome-gbp", type=float, default=3.1)
     ap.add_argument("--sample-mbp", type=float, default=20.0, help="CPU baseline sample (Mbp)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-search", choices=["plain", "batched", "pam_variety"], default=None,
+                    help="profiling aid: warm up, then run ONE profiled search of that workload between "
+                         "cudaProfilerStart/Stop (for ncu --profile-from-start off) and print its per-kernel "
+                         "statistics as JSON instead of the benchmark line")
     ap.add_argument("--no-batched", action="store_true", help="skip the 1,024-guide batched comparison")
     ap.add_argument("--batched-steps", type=int, default=2)
     ap.add_argument("--plain-sample", type=int, default=32, help="plain searches timed for the comparison")
@@ -579,6 +583,9 @@ def main():
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference_arm(args, world, rank)
+        return
+    if args.profile_search:
+        profile_search(args)
         return
 
     import ctypes
@@ -648,6 +655,21 @@ def main():
         _, rows_len = eng.search_planes_view(hi, lo, ot, n, None, None, names, starts)
     e2e_ms = dist_max(eng.timer_stop() / args.steps, world)
     e2e_value = world * N_GUIDES * gbp / (e2e_ms / 1e3)
+    # The same host -> device bytes copied alone (one copy of the pinned
+    # planes, CUDA events): the floor under the e2e step.
+    dev = torch.empty(3 * W, dtype=torch.int32, device=f"cuda:{local}")
+    dev.copy_(pinned, non_blocking=True)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h2d = []
+    for _ in range(3):
+        ev0.record()
+        dev.copy_(pinned, non_blocking=True)
+        ev1.record()
+        ev1.synchronize()
+        h2d.append(ev0.elapsed_time(ev1))
+    h2d_alone_ms = min(h2d)
+    del dev
 
     # ---- roofline of the dominant kernel (comparer: integer pipes)
     rates = P.pipe_rates(local)
@@ -732,7 +754,9 @@ def main():
                        "hits": nh, "rows": nrows, "l2": "no flush: inputs (1.16 GB planes) exceed L2",
                        "genome_gen_s": round(gen_s, 1), "comparer_schedule": schedule},
             "e2e": {"value": e2e_value, "unit": "guide-Gbp/s", "h2d_bytes_per_step": h2d_bytes,
-                    "d2h_bytes_per_step": rows_len + 16, "ms_per_step": e2e_ms},
+                    "d2h_bytes_per_step": rows_len + 16, "ms_per_step": e2e_ms,
+                    "planes_h2d_alone_ms": h2d_alone_ms,
+                    "planes_h2d_alone_gbs": 3 * W * 4 / (h2d_alone_ms * 1e-3) / 1e9},
             "roofline": {"bound": "int-pipe", "kernel": "comparer", "achieved": achieved, "peak": peak,
                          "unit": "G base-comparisons/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,
@@ -894,6 +918,46 @@ def run_pam_variety(P, eng, lens, rates, args, capture=None):
                               "frac": achieved / peak if peak else None,
                               "issued": issued_roofline(eng, cmp, rates)},
     }
+
+
+def profile_search(args):
+    """One profiled search of a workload on a genome of --genome-gbp, after
+    warm-up searches, between cudaProfilerStart and cudaProfilerStop, so that
+    `ncu --profile-from-start off` captures exactly that search's launches.
+    Prints the engine's per-kernel statistics (events, algorithmic units,
+    the comparer's LOP3 op model) as one JSON line."""
+    import numpy as np
+    import torch
+    P = pkg()
+    P.build()
+    buf, names, starts, lens = build_genome(P, args.genome_gbp * 1e9)
+    n = len(buf)
+    W = P.plane_words(n)
+    hi, lo, ot = (np.empty(W, np.uint32) for _ in range(3))
+    P.pack_text(buf, out=(hi, lo, ot))
+    eng = P.CasOFFinder(0)
+    if args.profile_search == "plain":
+        eng.readInputFile(input_text("synthetic", make_guides()))
+    else:
+        eng.batch_clear()
+        for t in (batched_jobs() if args.profile_search == "batched" else pam_variety_jobs()):
+            eng.batch_add_input(t)
+    eng.load_genome_planes(hi, lo, ot, n, None, None, names, starts)
+    for _ in range(2):
+        eng.search_view()
+    eng.synchronize()
+    eng.reset_stats()
+    eng.set_profiling(True)
+    torch.cuda.profiler.start()
+    eng.search_view()
+    eng.synchronize()
+    torch.cuda.profiler.stop()
+    eng.set_profiling(False)
+    out = {k: eng.kernel_stats(k) for k in ("finder", "finder.candidates", "comparer", "comparer.tests",
+                                            "comparer.lop3", "format")}
+    out.update(workload=args.profile_search, genome_bp=n, schedule=eng.schedule().strip())
+    print(json.dumps(out), flush=True)
+    eng.close()
 
 
 def issued_roofline(eng, cmp, rates):

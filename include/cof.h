@@ -300,7 +300,12 @@ cof_status cof_comparer_chunk(cof_handle* h, const char* chr, uint64_t chrlen, c
  * to 2^21 positions: larger chunks return COF_ERR_TOO_LARGE.  The first call
  * on a device looks up that array's device address; make it before any stream
  * capture.  All calls share the array: calls that overlap on the GPU race, so
- * order them (e.g. one stream).  Nothing is allocated or freed. */
+ * order them (e.g. one stream).  Nothing is allocated or freed.  `pattern` and
+ * `comp` are upper-cased first (as the reference upper-cases its input file);
+ * the compare string's masks travel as a kernel argument, so nothing on the
+ * host is read after the call returns.  If the calling thread already holds an
+ * unread CUDA error, the call returns COF_ERR_CUDA without queuing work and
+ * leaves that error for the caller. */
 cof_status cof_search_chunk_static(const uint32_t* d_hi, const uint32_t* d_lo, const uint32_t* d_ot, uint64_t n,
                                    const char* pattern, const char* comp, uint32_t patternlen, uint16_t threshold,
                                    uint64_t* d_hits, uint64_t hit_cap, unsigned long long* d_hit_count,
