@@ -183,32 +183,25 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(qcount, total);
     base = __shfl_sync(kFull, base, 0);
-    // Within a word: the '+' entries in descending bit order, then the '-'
-    // entries likewise.  One loop takes a bit of each strand per iteration
-    // (two independent chains), so it runs max(+, -) times rather than
-    // (+) + (-) times, as often as the lane with the most candidates.
+    // Within a word: descending bit order, '+' before '-'.
     auto emit = [&](uint32_t* dst) {
       uint32_t pass0 = 0;  // entries of the earlier passes
 #pragma unroll
       for (int k = 0; k < K; ++k) {
         const uint32_t mine = (k & 1) ? incl[k / 2] >> 16 : incl[k / 2] & 0xFFFFu;
-        const uint32_t at = pass0 + mine - cnt[k];
+        uint32_t at = pass0 + mine - cnt[k];
         pass0 += tot[k];
-        const uint32_t base = (uint32_t)((wb + 32 * k + lane - w_begin) << 6);  // entry of bit 0, '+'
+        const uint32_t rel = (uint32_t)((wb + 32 * k + lane - w_begin) << 5);
         uint32_t f = fwd[k], r = rev[k];
-        uint32_t* df = dst + at;
-        uint32_t* dr = df + __popc(f);
-        while (f | r) {
-          if (f) {
-            const unsigned b = 31 - __clz(f);
-            f ^= 1u << b;
-            *df++ = base + 2 * b;
-          }
-          if (r) {
-            const unsigned b = 31 - __clz(r);
-            r ^= 1u << b;
-            *dr++ = base + 2 * b + 1;
-          }
+        while (f) {
+          const unsigned b = 31 - __clz(f);
+          f ^= 1u << b;
+          dst[at++] = (rel + b) << 1;
+        }
+        while (r) {
+          const unsigned b = 31 - __clz(r);
+          r ^= 1u << b;
+          dst[at++] = ((rel + b) << 1) | 1u;
         }
       }
     };
