@@ -39,7 +39,7 @@ EXPORTS = [
     "cof_synchronize", "cof_set_comparer", "cof_comparer_info", "cof_search_chunk_static",
     "cof_batch_clear", "cof_batch_add_input", "cof_batch_size", "cof_job_rows", "cof_job_summary_text",
     "cof_server_start", "cof_server_submit", "cof_server_wait", "cof_server_release", "cof_server_stats",
-    "cof_server_timing",
+    "cof_server_timing", "cof_server_set_step_segments",
     "cof_server_set_hit_reserve", "cof_server_memory", "cof_server_last_error", "cof_server_stop",
     "cof_router_open", "cof_router_add_genome", "cof_router_drop_genome", "cof_router_genomes", "cof_router_submit",
     "cof_router_wait", "cof_router_release", "cof_router_last_error", "cof_router_close",
@@ -121,6 +121,7 @@ def lib():
                                           c.POINTER(c.c_double)]),
             "cof_server_release": (c.c_int, [vp, u64]),
             "cof_server_timing": (c.c_int, [vp, u64] + [c.POINTER(c.c_double)] * 4),
+            "cof_server_set_step_segments": (c.c_int, [vp, u32]),
             "cof_server_stats": (c.c_int, [vp] + [c.POINTER(u64)] * 6),
             "cof_server_set_hit_reserve": (c.c_int, [vp, u64]),
             "cof_server_memory": (c.c_int, [vp] + [c.POINTER(u64)] * 3),
@@ -522,6 +523,12 @@ class Server:
         self._L.cof_server_stats(self._s, *[ctypes.byref(v) for v in vals])
         keys = ("steps", "admitted", "completed", "pending", "active", "max_active")
         return dict(zip(keys, (v.value for v in vals)))
+
+    def set_step_segments(self, k):
+        """Ring segments one server step searches at most (default 4)."""
+        st = self._L.cof_server_set_step_segments(self._s, int(k))
+        if st != COF_OK:
+            raise CofError(st, "cof_server_set_step_segments")
 
     def set_hit_reserve(self, nbytes):
         """Hit memory charged per running request at least, for admission."""

@@ -913,9 +913,15 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
   COF_CUDA(h, h->small.ensure(64));
   COF_CUDA(h, h->job_start.ensure((J + 1) * 4));
   COF_CUDA(h, h->job_bytes.ensure((J + 1) * 8));
+  // Key bits the order depends on: strand (bit 7), position, variant id up to
+  // the largest id in use.  The mismatch bits below never break a tie: a
+  // (variant, position, strand) has one hit at most.
+  int end_bit = 44;
+  for (uint64_t v = h->job_gid0.empty() ? 1 : std::max<uint64_t>(h->job_gid0.back(), 2) - 1; v; v >>= 1) ++end_bit;
+  end_bit = std::min(end_bit, 64);
   size_t tmp = 0;
   COF_CUDA(h, cub::DeviceRadixSort::SortKeys(nullptr, tmp, h->hits.as<uint64_t>(), h->hits_sorted.as<uint64_t>(),
-                                             (int64_t)nhits, 0, 64, h->stream));
+                                             (int64_t)nhits, 7, end_bit, h->stream));
   size_t tmp2 = 0;
   COF_CUDA(h, cub::DeviceScan::ExclusiveSum(nullptr, tmp2, h->row_bytes.as<uint64_t>(), h->row_offsets.as<uint64_t>(),
                                             (int64_t)nhits, h->stream));
@@ -925,7 +931,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
   COF_CUDA(h, h->sort_tmp.ensure(std::max(tmp, std::max(tmp2, tmp3))));
   tmp = h->sort_tmp.cap;
   COF_CUDA(h, cub::DeviceRadixSort::SortKeys(h->sort_tmp.p, tmp, h->hits.as<uint64_t>(), h->hits_sorted.as<uint64_t>(),
-                                             (int64_t)nhits, 0, 64, h->stream));
+                                             (int64_t)nhits, 7, end_bit, h->stream));
   // Row sizes, offsets, per-job byte ranges, then the rows themselves.
   const GenomeView gv = h->genome.view();
   FormatTables ft{h->vfmt.as<VariantFmt>(), h->sfmt.as<ShapeFmt>(), h->pool.as<char>()};

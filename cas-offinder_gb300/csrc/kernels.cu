@@ -423,7 +423,17 @@ __device__ uint32_t record_of(const GenomeView& g, uint64_t p) {
   return a ? a - 1 : 0;
 }
 
+// Decimal text of row numbers.  Values below 2^32 (every location inside a
+// record shorter than 4 Gbp, every mismatch count) take 32-bit arithmetic,
+// where division by 10 is a multiply-high and a shift; a 64-bit division
+// is a long software sequence.
 __device__ __forceinline__ uint32_t decimal_len(uint64_t v) {
+  if (v <= 0xFFFFFFFFull) {
+    const uint32_t x = (uint32_t)v;
+    uint32_t d = 1;
+    for (uint32_t p = 10; d < 10 && x >= p; p *= 10) ++d;  // 10^9 is the last power below 2^32
+    return d;
+  }
   uint32_t d = 1;
   while (v >= 10) {
     v /= 10;
@@ -435,10 +445,15 @@ __device__ __forceinline__ uint32_t decimal_len(uint64_t v) {
 __device__ __forceinline__ char* put_decimal(char* o, uint64_t v) {
   char tmp[20];
   int k = 0;
-  do {
+  while (v > 0xFFFFFFFFull) {
     tmp[k++] = (char)('0' + v % 10);
     v /= 10;
-  } while (v);
+  }
+  uint32_t x = (uint32_t)v;
+  do {
+    tmp[k++] = (char)('0' + x % 10);
+    x /= 10;
+  } while (x);
   while (k) *o++ = tmp[--k];
   return o;
 }

@@ -135,6 +135,7 @@ struct cof_server {
   // worker-only state
   std::unique_ptr<TableSet> tables;
   uint64_t seg_words = kSegWords;  // plane words (32 start positions each) per ring segment
+  std::atomic<uint32_t> step_segments{4};  // ring segments per step at most (cof_server_set_step_segments)
   uint64_t ring = 0, cur = 0;      // ring length in segments, current segment
   DevBuf step_hits, step_sorted, step_count, step_bounds, step_gid0, sort_tmp;
   // finisher-only state
@@ -219,10 +220,14 @@ bool tables_live(const cof_server* s) {
   return false;
 }
 
-// One ring step: segment s->cur for every group of the current tables.
-// Appends each hit to its request (request-local variant id) unless the
-// request has already completed the ring.
-cof_status run_step(cof_server* s) {
+// One ring step: segments s->cur .. s->cur + k - 1 (mod the ring) for every
+// group of the current tables, the finder of each pass on the second stream
+// running ahead of the comparers on the first as in a plain search.  Appends
+// each hit to its request (request-local variant id) unless the request has
+// already completed the ring.  The caller picks k no larger than the
+// segments any request of the tables still needs, so no request sees a
+// segment twice.
+cof_status run_step(cof_server* s, uint64_t k) {
   cof_handle* h = s->h;
   TableSet& T = *s->tables;
   const GenomeView gv = h->genome.view();
@@ -230,8 +235,8 @@ cof_status run_step(cof_server* s) {
   uint64_t cap = std::max<uint64_t>(s->step_hits.cap / 8, 1u << 16);
   COF_CUDA(h, s->step_hits.ensure(cap * 8));
   COF_CUDA(h, s->step_count.ensure(8));
-  // candidate counts per group, then the comparer's tile counters
-  const size_t nq = std::max<size_t>(T.groups.size(), 1);
+  // candidate counts per (segment, group), then the comparer's tile counters
+  const size_t nq = std::max<size_t>(T.groups.size(), 1) * (size_t)k;
   COF_CUDA(h, h->qcounts.ensure(2 * nq * 4));
   // at most two oriented candidates per start position of a segment
   COF_CUDA(h, h->queue[0].ensure(2 * s->seg_words * 32 * 4));
@@ -243,14 +248,16 @@ cof_status run_step(cof_server* s) {
     COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
     COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
     uint64_t pass = 0;
+    for (uint64_t si = 0; si < k; ++si)
     for (size_t gi = 0; gi < T.groups.size(); ++gi) {
       const PatternGroup& g = T.groups[gi];
       const uint64_t npos = n >= g.L ? n - g.L + 1 : 0;
       const uint64_t words = (npos + 31) / 32;
-      const uint64_t w0 = s->cur * s->seg_words, w1 = std::min(words, w0 + s->seg_words);
+      const uint64_t seg = (s->cur + si) % s->ring;
+      const uint64_t w0 = seg * s->seg_words, w1 = std::min(words, w0 + s->seg_words);
       if (w0 >= w1 || g.gids.empty()) continue;
       const int b = (int)(pass & 1);
-      uint32_t* qc = h->qcounts.as<uint32_t>() + gi;
+      uint32_t* qc = h->qcounts.as<uint32_t>() + si * T.groups.size() + gi;
       uint32_t* q = h->queue[b].as<uint32_t>();
       if (pass >= 2) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[b], 0));
       launch_finder(gv, w0, w1, g.fpat, q, qc, h->stream2);
@@ -317,7 +324,7 @@ cof_status run_step(cof_server* s) {
     }
     COF_CUDA(h, cudaGetLastError());
   }
-  ++s->steps;
+  s->steps += k;
   return COF_OK;
 }
 
@@ -502,7 +509,12 @@ void worker_main(cof_server* s) {
       }
     }
     if (!tables_live(s)) continue;
-    const cof_status st = run_step(s);
+    // Segments this step: at most the step limit, and no more than any
+    // request of the tables still needs to complete its ring.
+    uint64_t k = std::max<uint64_t>(1, s->step_segments.load());
+    for (const ReqPtr& r : s->tables->reqs)
+      if (!r->ran) k = std::min<uint64_t>(k, s->ring - std::min<uint64_t>(r->steps_seen, s->ring - 1));
+    const cof_status st = run_step(s, k);
     {
       std::lock_guard<std::mutex> lock(s->mu);
       uint64_t held = s->finishing_bytes;
@@ -512,7 +524,7 @@ void worker_main(cof_server* s) {
     }
     std::vector<ReqPtr> finished;
     for (const ReqPtr& r : s->tables->reqs)
-      if (!r->ran && (st || ++r->steps_seen >= s->ring)) finished.push_back(r);
+      if (!r->ran && (st || (r->steps_seen += k) >= s->ring)) finished.push_back(r);
     if (!finished.empty()) {
       const double t = now_s();
       for (const ReqPtr& r : finished) r->t_ran = t;
@@ -536,7 +548,7 @@ void worker_main(cof_server* s) {
       want_build(s);
       s->cv_finish.notify_one();
     }
-    s->cur = (s->cur + 1) % s->ring;
+    s->cur = (s->cur + k) % s->ring;
   }
   // Stopped: requests still queued or running end with COF_ERR_STATE.
   std::vector<ReqPtr> left;
@@ -676,6 +688,12 @@ cof_status cof_server_release(cof_server* s, uint64_t ticket) {
   auto it = s->tickets.find(ticket);
   if (it == s->tickets.end() || !it->second->done) return COF_ERR_ARG;
   s->tickets.erase(it);
+  return COF_OK;
+}
+
+cof_status cof_server_set_step_segments(cof_server* s, uint32_t segments) {
+  if (!s || segments == 0) return COF_ERR_ARG;
+  s->step_segments = segments;
   return COF_OK;
 }
 

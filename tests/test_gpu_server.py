@@ -74,6 +74,26 @@ def test_server_mix_equals_alone(P, built, oracle, tmp_path):
                 assert P.HEADER.encode() + rows == want[j], f"request {j} alone"
 
 
+def test_server_step_segments_keep_rows(P, built, oracle, tmp_path):
+    """Steps of 1, 3 and 7 ring segments (a ring of 10): requests that join
+    between steps still see each segment exactly once, so the rows are those
+    of each input file alone."""
+    genome, texts = make_genome_and_requests(P, tmp_path)
+    texts = texts[:4]
+    want = oracle_rows(oracle, tmp_path, texts)
+    with P.CasOFFinder(0) as eng:
+        eng.load_genome_file(genome)
+        for k in (1, 3, 7):
+            with P.Server(eng, max_active_variants=250, segment_positions=1 << 15) as srv:
+                srv.set_step_segments(k)
+                tickets = [srv.submit(t) for t in texts]
+                got = [srv.wait(t) for t in tickets]
+                stats = srv.stats()
+            for j, (rows, _) in enumerate(got):
+                assert P.HEADER.encode() + rows == want[j], f"request {j}, {k} segments per step"
+            assert stats["completed"] == len(texts)
+
+
 def test_server_admits_by_hit_memory(P, built, oracle, tmp_path):
     """Admission by device memory: each running request is charged at least
     its hit reservation against hit_buffer_bytes, so a reservation of half the
