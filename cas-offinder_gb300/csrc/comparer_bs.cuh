@@ -58,12 +58,24 @@ __device__ __forceinline__ uint32_t maj3(uint32_t a, uint32_t b, uint32_t c) { r
 __device__ __forceinline__ uint32_t xor3(uint32_t a, uint32_t b, uint32_t c) { return lop3<0x96>(a, b, c); }
 
 // 32x32 bit transpose across the warp: lane i holds row i; afterwards lane i
-// holds column i (bit j = bit i of row j).
+// holds column i (bit j = bit i of row j).  Each stage j swaps j-bit blocks
+// with lane i ^ j.  The 16- and 8-bit stages move whole bytes, so one byte
+// permute of (x, partner) does the merge there (lower lanes keep their low
+// blocks and take the partner's low blocks above them, upper lanes the
+// reverse); the 4-, 2- and 1-bit stages rotate the partner's word and merge
+// under a mask.
 __device__ __forceinline__ uint32_t warp_transpose(uint32_t x, unsigned lane) {
+  {
+    const uint32_t y = __shfl_xor_sync(kFull, x, 16);
+    x = __byte_perm(x, y, (lane & 16) ? 0x3276u : 0x5410u);
+  }
+  {
+    const uint32_t y = __shfl_xor_sync(kFull, x, 8);
+    x = __byte_perm(x, y, (lane & 8) ? 0x3715u : 0x6240u);
+  }
 #pragma unroll
-  for (int j = 16; j > 0; j >>= 1) {
-    const uint32_t m = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu : j == 2 ? 0x33333333u
-                                                                                                    : 0x55555555u;
+  for (int j = 4; j > 0; j >>= 1) {
+    const uint32_t m = j == 4 ? 0x0F0F0F0Fu : j == 2 ? 0x33333333u : 0x55555555u;
     const bool upper = (lane & j) != 0;
     const uint32_t y = __shfl_xor_sync(kFull, x, j);
     // upper lanes take the partner's bits shifted down, lower lanes shifted up;
@@ -795,6 +807,23 @@ bool launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcoun
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
+  // Leave one finder CTA's registers free on every SM: the next segment's
+  // PAM scan (second stream) then runs beside this launch instead of after it.
+  {
+    static int sm_regs = 0;
+    if (!sm_regs) {
+      int dev = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&sm_regs, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess)
+        sm_regs = 0;
+    }
+    cudaFuncAttributes a{};
+    const int finder_regs = finder_cta_registers(L);
+    if (sm_regs && finder_regs && cudaFuncGetAttributes(&a, kernel) == cudaSuccess) {
+      const int cta_regs = ((a.numRegs + 7) / 8) * 8 * threads;
+      while (per_sm > 1 && per_sm * cta_regs + finder_regs > sm_regs) --per_sm;
+    }
+  }
   kernel<<<sm_count * per_sm, threads, smem, stream>>>(g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks,
                                                         m, L, tile_ctr, hits, hit_count, hit_cap);
   return true;

@@ -352,7 +352,7 @@ cof_status format_request(cof_server* s, Request& r, std::string& err) {
   append_format_tables(r.job, vf, sf, pool);
   COF_FIN(s->fmt_vf.ensure(vf.size() * sizeof(VariantFmt)));
   COF_FIN(s->fmt_sf.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
-  COF_FIN(s->fmt_pool.ensure(std::max<size_t>(pool.size(), 1)));
+  COF_FIN(s->fmt_pool.ensure(pool.size() + kBytePoolPad));
   COF_FIN(s->fmt_hits.ensure(nh * 8));
   COF_FIN(s->fmt_bytes.ensure(nh * 8));
   COF_FIN(s->fmt_off.ensure(nh * 8));
@@ -590,7 +590,13 @@ cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_
   if (s->max_active_variants >= (1u << 20)) s->max_active_variants = (1u << 20) - 1;
   s->hit_buffer_bytes = hit_buffer_bytes ? hit_buffer_bytes : (8ull << 30);
   if (segment_positions) s->seg_words = std::min<uint64_t>(kSegWords, std::max<uint64_t>(1, segment_positions / 32));
-  cudaError_t e = cudaStreamCreateWithFlags(&s->fin_stream, cudaStreamNonBlocking);
+  // The finisher's stream has the greatest priority: a completed request's
+  // sort and row formatting are small next to the ring's comparer launches,
+  // and its CTAs go first whenever an SM frees up, so finished requests are
+  // not held behind the steps queued after them.
+  int lo_prio = 0, hi_prio = 0;
+  cudaError_t e = cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+  if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&s->fin_stream, cudaStreamNonBlocking, hi_prio);
   if (e != cudaSuccess) {
     delete s;
     return fail(h, COF_ERR_CUDA, std::string("server stream: ") + cudaGetErrorString(e));
