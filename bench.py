@@ -673,6 +673,7 @@ def main():
 
     # ---- roofline of the dominant kernel (comparer: integer pipes)
     rates = P.pipe_rates(local)
+    d2h = P.d2h_rates(local)
     cmp = stats["comparer"]
     cinfo = eng.comparer_info()
     nw = 1 if info["pattern_len"] <= 32 else 2
@@ -756,7 +757,8 @@ def main():
             "e2e": {"value": e2e_value, "unit": "guide-Gbp/s", "h2d_bytes_per_step": h2d_bytes,
                     "d2h_bytes_per_step": rows_len + 16, "ms_per_step": e2e_ms,
                     "planes_h2d_alone_ms": h2d_alone_ms,
-                    "planes_h2d_alone_gbs": 3 * W * 4 / (h2d_alone_ms * 1e-3) / 1e9},
+                    "planes_h2d_alone_gbs": 3 * W * 4 / (h2d_alone_ms * 1e-3) / 1e9,
+                    "d2h_1gb_gbs": {"copy_engine": d2h["dma"] / 1e9, "sm_stores": d2h["sm"] / 1e9}},
             "roofline": {"bound": "int-pipe", "kernel": "comparer", "achieved": achieved, "peak": peak,
                          "unit": "G base-comparisons/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,

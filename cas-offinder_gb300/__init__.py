@@ -653,6 +653,20 @@ def pipe_rates(device=0):
     return {"lop3": a.value, "popc": b.value, "iadd": c.value}
 
 
+def d2h_rates(device=0, nbytes=1 << 30):
+    """Device -> pinned host copy rates (bytes/s) of `nbytes`: {'dma': one
+    cudaMemcpyAsync, 'sm': a kernel storing into the mapped host buffer}.
+    From libcofrates.so, the measurement library built beside the engine."""
+    L = ctypes.CDLL(RATES_LIB_PATH)
+    L.cofx_d2h_rates.restype = ctypes.c_int
+    L.cofx_d2h_rates.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double),
+                                 ctypes.POINTER(ctypes.c_double)]
+    a, b = ctypes.c_double(), ctypes.c_double()
+    if L.cofx_d2h_rates(device, nbytes, ctypes.byref(a), ctypes.byref(b)) != 0:
+        raise RuntimeError("cofx_d2h_rates failed")
+    return {"dma": a.value, "sm": b.value}
+
+
 # ---------------------------------------------------------------- synthetic genomes
 def synth_record(seed, record, length, gc=0.41, gc_drift=0.0, drift_window=100000, n_frac=0.0,
                  n_run_min=100, n_run_max=10000) -> bytearray:

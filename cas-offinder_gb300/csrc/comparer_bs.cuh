@@ -807,23 +807,6 @@ bool launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcoun
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
     per_sm = 1;
-  // Leave one finder CTA's registers free on every SM: the next segment's
-  // PAM scan (second stream) then runs beside this launch instead of after it.
-  {
-    static int sm_regs = 0;
-    if (!sm_regs) {
-      int dev = 0;
-      if (cudaGetDevice(&dev) != cudaSuccess ||
-          cudaDeviceGetAttribute(&sm_regs, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess)
-        sm_regs = 0;
-    }
-    cudaFuncAttributes a{};
-    const int finder_regs = finder_cta_registers(L);
-    if (sm_regs && finder_regs && cudaFuncGetAttributes(&a, kernel) == cudaSuccess) {
-      const int cta_regs = ((a.numRegs + 7) / 8) * 8 * threads;
-      while (per_sm > 1 && per_sm * cta_regs + finder_regs > sm_regs) --per_sm;
-    }
-  }
   kernel<<<sm_count * per_sm, threads, smem, stream>>>(g.hi, g.lo, g.ot, queue, qcount, seg_pos0, prog, pgid, chunks,
                                                         m, L, tile_ctr, hits, hit_count, hit_cap);
   return true;

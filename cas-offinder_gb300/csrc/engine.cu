@@ -116,7 +116,7 @@ cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const
   COF_CUDA(h, dg.rec_start.ensure(std::max<size_t>(R, 1) * 8));
   COF_CUDA(h, dg.rec_name_off.ensure(std::max<size_t>(R, 1) * 4));
   COF_CUDA(h, dg.rec_name_len.ensure(std::max<size_t>(R, 1) * 4));
-  COF_CUDA(h, dg.rec_names.ensure(pool.size() + kBytePoolPad));
+  COF_CUDA(h, dg.rec_names.ensure(std::max<size_t>(pool.size(), 1)));
   if (R) {
     COF_CUDA(h, cudaMemcpyAsync(dg.rec_start.p, starts.data(), R * 8, cudaMemcpyHostToDevice, h->stream));
     COF_CUDA(h, cudaMemcpyAsync(dg.rec_name_off.p, off.data(), R * 4, cudaMemcpyHostToDevice, h->stream));
@@ -601,7 +601,7 @@ cof_status upload_jobs(cof_handle* h) {
     }
   COF_CUDA(h, h->vfmt.ensure(std::max<size_t>(total, 1) * sizeof(VariantFmt)));
   COF_CUDA(h, h->sfmt.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
-  COF_CUDA(h, h->pool.ensure(pool.size() + kBytePoolPad));
+  COF_CUDA(h, h->pool.ensure(std::max<size_t>(pool.size(), 1)));
   if (total)
     COF_CUDA(h, cudaMemcpyAsync(h->vfmt.p, vf.data(), total * sizeof(VariantFmt), cudaMemcpyHostToDevice, h->stream));
   if (!sf.empty())

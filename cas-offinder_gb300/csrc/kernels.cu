@@ -54,11 +54,7 @@ __device__ __forceinline__ uint32_t bits_at(uint32_t w0, uint32_t w1, uint32_t w
 // queue position's offset within a 16-byte line, so source and destination
 // line up); a warp with more candidates (dense patterns) stores them
 // directly.
-// Two warps per CTA: a CTA of this size (56 registers x 64 threads, 8 KB of
-// staging) still fits beside a full SM of the bit-sliced comparer's one-warp
-// CTAs, so the next segment's scan, launched on the second stream, can start
-// while the comparer of the current one runs instead of after it.
-constexpr int kFinderThreads = 64;
+constexpr int kFinderThreads = 128;
 constexpr int kFinderWords = 4;     // plane words per lane per pass
 constexpr int kFinderStage = 1024;  // staged entries per warp; denser warps store directly
 
@@ -270,18 +266,6 @@ void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const 
                                                                      queue, qcount);
 }
 
-int finder_cta_registers(uint32_t L) {
-  // Per CTA, with the allocation's granularity of 8 registers per thread.
-  static int regs[2] = {0, 0};
-  const int i = L <= 32 ? 0 : 1;
-  if (!regs[i]) {
-    cudaFuncAttributes a{};
-    const cudaError_t e = i == 0 ? cudaFuncGetAttributes(&a, finder_kernel<1>) : cudaFuncGetAttributes(&a, finder_kernel<2>);
-    regs[i] = e == cudaSuccess ? ((a.numRegs + 7) / 8) * 8 * kFinderThreads : 0;
-  }
-  return regs[i];
-}
-
 // ---------------------------------------------------------------- comparer
 template <int NW>
 struct CandWindow {
@@ -458,20 +442,20 @@ __device__ __forceinline__ uint32_t decimal_len(uint64_t v) {
   return d;
 }
 
-// Writes the digits from the last one back (no scratch array).
 __device__ __forceinline__ char* put_decimal(char* o, uint64_t v) {
-  char* const end = o + decimal_len(v);
-  char* p = end;
+  char tmp[20];
+  int k = 0;
   while (v > 0xFFFFFFFFull) {
-    *--p = (char)('0' + v % 10);
+    tmp[k++] = (char)('0' + v % 10);
     v /= 10;
   }
   uint32_t x = (uint32_t)v;
   do {
-    *--p = (char)('0' + x % 10);
+    tmp[k++] = (char)('0' + x % 10);
     x /= 10;
   } while (x);
-  return end;
+  while (k) *o++ = tmp[--k];
+  return o;
 }
 
 struct HitView {
@@ -508,33 +492,14 @@ __global__ void row_len_kernel(GenomeView g, FormatTables ft, const uint64_t* __
   row_count[i] = vf.shape_end[h.strand] - vf.shape_begin[h.strand];
 }
 
-// In-order reader of a byte pool through aligned 32-bit loads: one load per
-// four bytes read in sequence instead of one per byte (byte loads had the
-// row writer throttled on its load queue).  Pools are allocated with
-// kBytePoolPad bytes of slack, so the word holding their last byte is inside
-// the allocation.
-struct WordBytes {
-  const uint32_t* w;
-  uint64_t cur;
-  uint32_t v;
-  __device__ explicit WordBytes(const char* p) : w(reinterpret_cast<const uint32_t*>(p)), cur(~0ull), v(0) {}
-  __device__ __forceinline__ unsigned char at(uint64_t i) {
-    const uint64_t k = i >> 2;
-    if (k != cur) {
-      cur = k;
-      v = __ldg(w + k);
-    }
-    return (unsigned char)(v >> ((unsigned)(i & 3) * 8));
-  }
-};
-
 // Rows of one hit at `o` (the bytes row_len_kernel counted).
 __device__ __forceinline__ void write_row(const GenomeView& g, const FormatTables& ft, uint64_t key, char* o) {
   const HitView h = decode(key);
-  const VariantFmt* vf = ft.var + h.gid;  // fields read one by one (no copy indexed by strand)
-  const uint32_t L = vf->L, comp_off = vf->comp_off;
-  const uint32_t s0 = vf->shape_begin[h.strand], s1 = vf->shape_end[h.strand];
-  WordBytes pool(ft.pool);
+  const VariantFmt vf = ft.var[h.gid];
+  const uint32_t L = vf.L;
+  const char* comp = ft.pool + vf.comp_off;
+  // Oriented window with mismatches lower-cased (indicate_mismatches,
+  // cas-offinder.cpp:299-317: byte += 32).
   // The window's plane bits, 64 positions from h.pos (three words per plane
   // cover any L <= 64 at any bit offset).
   const uint64_t w0 = h.pos >> 5;
@@ -544,41 +509,31 @@ __device__ __forceinline__ void write_row(const GenomeView& g, const FormatTable
     return b0 ? (lo64 >> b0) | ((uint64_t)plane[w0 + 2] << (64 - b0)) : lo64;
   };
   const uint64_t H = bits64(g.hi), Lo = bits64(g.lo), O = bits64(g.ot);
-  // Byte of oriented window position k (the '-' strand reads the reverse
-  // complement), before lower-casing.
-  auto window_byte = [&](uint32_t k) -> unsigned char {
+  unsigned char win[kMaxL];
+  for (uint32_t k = 0; k < L; ++k) {
     const uint32_t q = h.strand ? L - 1 - k : k;  // window position of oriented position k
     const unsigned hb = (unsigned)(H >> q) & 1u, lb = (unsigned)(Lo >> q) & 1u;
     unsigned char c;
-    // Bases by 2BIT code from one word: 'T' 'C' 'A' 'G' in bytes 0..3.
-    if (!((O >> q) & 1u)) c = (unsigned char)(0x47414354u >> (8 * (hb * 2 + lb)));
+    if (!((O >> q) & 1u)) c = (unsigned char)"TCAG"[hb * 2 + lb];
     else if (!hb) c = lb ? ';' : 'N';
     else c = genome_byte(g, h.pos + q);  // another byte: from the exception list
-    return h.strand ? dev_complement(c) : c;
-  };
-  // Mismatched positions are lower-cased (indicate_mismatches,
-  // cas-offinder.cpp:299-317: byte += 32); bit k = oriented position k.
-  uint64_t lower = 0;
-  for (uint32_t k = 0; k < L; ++k)
-    if (dev_mismatch(pool.at(comp_off + k), window_byte(k))) lower |= 1ull << k;
+    if (h.strand) c = dev_complement(c);
+    if (dev_mismatch((unsigned char)comp[k], c)) c = (unsigned char)(c + 32);
+    win[k] = c;
+  }
   const uint32_t rec = record_of(g, h.pos);
   const uint64_t rel = h.pos - g.rec_start[rec];
-  const uint32_t name_off = g.rec_name_off[rec], name_len = g.rec_name_len[rec];
-  WordBytes names(g.rec_names);
-  for (uint32_t s = s0; s < s1; ++s) {
+  const char* name = g.rec_names + g.rec_name_off[rec];
+  const uint32_t name_len = g.rec_name_len[rec];
+  for (uint32_t s = vf.shape_begin[h.strand]; s < vf.shape_end[h.strand]; ++s) {
     const ShapeFmt sh = ft.shape[s];
-    for (uint32_t k = 0; k < sh.head_len; ++k) *o++ = (char)pool.at(sh.head_off + k);
+    for (uint32_t k = 0; k < sh.head_len; ++k) *o++ = ft.pool[sh.head_off + k];
     for (uint32_t k = 0; k < sh.dna_len; ++k) {
-      const unsigned char c = pool.at(sh.dna_off + k);
-      if (c >= 0x80) {
-        const uint32_t q = c - 0x80u;
-        *o++ = (char)(window_byte(q) + (((lower >> q) & 1u) ? 32 : 0));
-      } else {
-        *o++ = (char)c;
-      }
+      const unsigned char c = (unsigned char)ft.pool[sh.dna_off + k];
+      *o++ = (char)(c >= 0x80 ? win[c - 0x80] : c);
     }
     *o++ = '\t';
-    for (uint32_t k = 0; k < name_len; ++k) *o++ = (char)names.at((uint64_t)name_off + k);
+    for (uint32_t k = 0; k < name_len; ++k) *o++ = name[k];
     *o++ = '\t';
     o = put_decimal(o, rel + (uint64_t)sh.offset);
     *o++ = '\t';
@@ -586,7 +541,7 @@ __device__ __forceinline__ void write_row(const GenomeView& g, const FormatTable
     *o++ = '\t';
     o = put_decimal(o, h.mm);
     *o++ = '\t';
-    for (uint32_t k = 0; k < sh.tail_len; ++k) *o++ = (char)pool.at(sh.tail_off + k);
+    for (uint32_t k = 0; k < sh.tail_len; ++k) *o++ = ft.pool[sh.tail_off + k];
   }
 }
 

@@ -93,9 +93,6 @@ struct FormatTables {
   const ShapeFmt* shape;
   const char* pool;
 };
-// Slack allocated after every byte pool the row writer reads (the row
-// strings `pool`, the record names): it reads pools a 32-bit word at a time.
-constexpr size_t kBytePoolPad = 8;
 
 // ---- launchers (kernels.cu).  All run on `stream`, none synchronizes.
 // Scans start positions [32*w_begin, 32*w_end) below g.n - L + 1 (windows
@@ -103,10 +100,6 @@ constexpr size_t kBytePoolPad = 8;
 // (position - 32*w_begin) << 1 | strand to `queue`.
 void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const FinderPattern& pat, uint32_t* queue,
                    uint32_t* qcount, cudaStream_t stream);
-// Registers one finder CTA holds (patterns of length L); the bit-sliced
-// comparer leaves that many free on every SM so that the next segment's scan
-// runs beside it.
-int finder_cta_registers(uint32_t L);
 // Tests every entry of `queue` (count read on the device) against `nvar`
 // variants; appends hit keys to `hits` (count in *hit_count; entries past
 // hit_cap are counted, not written).

@@ -13,6 +13,7 @@
 // about a second.  Returns 0 on success.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 namespace {
@@ -89,7 +90,60 @@ double rate(K kernel, int blocks, int threads, double ops_per_thread, uint32_t* 
   return (double)blocks * threads * ops_per_thread / (ms * 1e-3);
 }
 
+// Device -> pinned host copy by the SMs: 16-byte loads from device memory,
+// 16-byte stores to the host buffer's device-mapped address.
+__global__ void sm_copy(const uint4* __restrict__ src, uint4* __restrict__ dst, size_t n16) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = src[i];
+}
+
 }  // namespace
+
+//   int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm);
+// Device -> pinned host copy rates in bytes/s for a buffer of `bytes` (a
+// multiple of 16): one cudaMemcpyAsync (copy engine) and a kernel whose
+// threads store into the mapped host buffer.  Best of three each.  Returns 0
+// on success.
+extern "C" int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm) {
+  if (cudaSetDevice(device) != cudaSuccess || bytes == 0 || bytes % 16) return 1;
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  void *d = nullptr, *h = nullptr, *hd = nullptr;
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return 1;
+  if (cudaHostAlloc(&h, bytes, cudaHostAllocMapped) != cudaSuccess) {
+    cudaFree(d);
+    return 1;
+  }
+  int rc = 0;
+  if (cudaHostGetDevicePointer(&hd, h, 0) != cudaSuccess || cudaMemset(d, 1, bytes) != cudaSuccess) rc = 1;
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  double best_dma = 0, best_sm = 0;
+  for (int rep = 0; rc == 0 && rep < 4; ++rep) {  // the first of each is a warm-up
+    float ms = 0;
+    cudaEventRecord(a);
+    cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, 0);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep && ms > 0) best_dma = std::max(best_dma, bytes / (ms * 1e-3));
+    cudaEventRecord(a);
+    sm_copy<<<sms * 4, 512>>>((const uint4*)d, (uint4*)hd, bytes / 16);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep && ms > 0) best_sm = std::max(best_sm, bytes / (ms * 1e-3));
+  }
+  if (cudaGetLastError() != cudaSuccess) rc = 1;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFreeHost(h);
+  cudaFree(d);
+  if (dma) *dma = best_dma;
+  if (sm) *sm = best_sm;
+  return rc;
+}
 
 extern "C" int cofx_pipe_rates(int device, double* lop3, double* popc, double* iadd) {
   if (cudaSetDevice(device) != cudaSuccess) return 1;

@@ -352,7 +352,7 @@ cof_status format_request(cof_server* s, Request& r, std::string& err) {
   append_format_tables(r.job, vf, sf, pool);
   COF_FIN(s->fmt_vf.ensure(vf.size() * sizeof(VariantFmt)));
   COF_FIN(s->fmt_sf.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
-  COF_FIN(s->fmt_pool.ensure(pool.size() + kBytePoolPad));
+  COF_FIN(s->fmt_pool.ensure(std::max<size_t>(pool.size(), 1)));
   COF_FIN(s->fmt_hits.ensure(nh * 8));
   COF_FIN(s->fmt_bytes.ensure(nh * 8));
   COF_FIN(s->fmt_off.ensure(nh * 8));
@@ -453,9 +453,13 @@ void finisher_main(cof_server* s) {
   }
 }
 
+// Ring steps merge segments while one segment takes less than this (ms).
+constexpr double kMergeSegmentsBelowMs = 2.0;
+
 void worker_main(cof_server* s) {
   cof_handle* h = s->h;
   cudaSetDevice(h->device);
+  double last_seg_ms = 0;  // host time per segment of the latest step
   const uint64_t words = (h->genome.n + 31) / 32;
   s->ring = std::max<uint64_t>(1, (words + s->seg_words - 1) / s->seg_words);
   for (;;) {
@@ -509,12 +513,17 @@ void worker_main(cof_server* s) {
       }
     }
     if (!tables_live(s)) continue;
-    // Segments this step: at most the step limit, and no more than any
-    // request of the tables still needs to complete its ring.
-    uint64_t k = std::max<uint64_t>(1, s->step_segments.load());
+    // Segments this step: up to the step limit while segments are quick to
+    // search (the host round trips of a step are then a large share of it);
+    // one at a time once the ring is loaded, so that the finisher's short
+    // launches find the GPU between steps.  Never more than any request of
+    // the tables still needs to complete its ring.
+    uint64_t k = last_seg_ms < kMergeSegmentsBelowMs ? std::max<uint64_t>(1, s->step_segments.load()) : 1;
     for (const ReqPtr& r : s->tables->reqs)
       if (!r->ran) k = std::min<uint64_t>(k, s->ring - std::min<uint64_t>(r->steps_seen, s->ring - 1));
+    const double t_step = now_s();
     const cof_status st = run_step(s, k);
+    last_seg_ms = (now_s() - t_step) * 1e3 / (double)k;
     {
       std::lock_guard<std::mutex> lock(s->mu);
       uint64_t held = s->finishing_bytes;

@@ -189,12 +189,14 @@ cof_status cof_server_timing(cof_server* s, uint64_t ticket, double* admission_m
                              double* format_ms);
 cof_status cof_server_stats(cof_server* s, uint64_t* steps, uint64_t* admitted, uint64_t* completed,
                             uint64_t* pending, uint64_t* active, uint64_t* max_active);
-/* Ring segments one step searches at most (default 4): a step runs the PAM
- * scans and comparers of that many consecutive segments back to back (the
- * next segment's scan overlapping the current comparer) before the host
- * sorts the step's hits and admits requests, so fewer host round trips per
- * ring; a step never spans more segments than a running request still
- * needs.  Requests join only at step boundaries.  Applies from the next step. */
+/* Ring segments one step searches at most (default 4): while a segment takes
+ * less than 2 ms to search, a step runs the PAM scans and comparers of that
+ * many consecutive segments back to back (the next segment's scan
+ * overlapping the current comparer) before the host sorts the step's hits
+ * and admits requests, so fewer host round trips per ring; slower segments
+ * (a loaded ring) are stepped one at a time.  A step never spans more
+ * segments than a running request still needs.  Requests join only at step
+ * boundaries.  Applies from the next step. */
 cof_status cof_server_set_step_segments(cof_server* s, uint32_t segments);
 /* Hit memory charged per running request at least (default 64 MiB); applies
  * to admissions after the call. */
