@@ -230,7 +230,7 @@ def run_served_burst(P, eng, lens):
         eng.readInputFile(t)
         eng.search_view()
     plain_ms = eng.timer_stop() / 32
-    lat = [None] * len(texts)
+    lat, parts = [None] * len(texts), [None] * len(texts)
     with P.Server(eng) as srv:
         t0 = time.perf_counter()
         tickets = [srv.submit(t) for t in texts]
@@ -238,6 +238,7 @@ def run_served_burst(P, eng, lens):
         def waiter(lo, hi):
             for j in range(lo, hi):
                 lat[j] = srv.wait_view(tickets[j])[2]
+                parts[j] = srv.timing(tickets[j])
                 srv.release(tickets[j])
 
         ths = [threading.Thread(target=waiter, args=(i * 128, (i + 1) * 128)) for i in range(len(texts) // 128)]
@@ -251,7 +252,11 @@ def run_served_burst(P, eng, lens):
     plain_value = gbp / (plain_ms / 1e3)
     return {"workload": "the 1,024 single-guide input files of the batched leg, submitted at once as requests",
             "value": value, "unit": "guide-Gbp/s", "makespan_s": span, "p50_ms": statistics.median(lat),
-            "p99_ms": percentile(lat, 0.99), "max_active": st["max_active"], "plain_value": plain_value,
+            "p99_ms": percentile(lat, 0.99), "max_active": st["max_active"], "ring_steps": st["steps"],
+            "latency_parts_ms": {k: {"p50": statistics.median(p[k] for p in parts),
+                                     "mean": statistics.fmean(p[k] for p in parts)}
+                                 for k in ("admission", "build", "ring", "format")},
+            "plain_value": plain_value,
             "speedup_vs_plain": value / plain_value}
 
 
@@ -337,7 +342,7 @@ class ClockSampler:
                  "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                  "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
             # Timing starts once sampling runs, so nvidia-smi's start-up
             # stays outside the timed region.

@@ -29,7 +29,7 @@
 // request, so admitting a request adds no candidate memory.  What grows with
 // the admitted set is each request's own device hit buffer (8 B per hit,
 // kept until its rows are formatted).  A running request is charged the
-// larger of that buffer and a per-request reservation (hit_reserve_bytes),
+// larger of that buffer and a per-request reservation (reserve_of),
 // and a waiting request is admitted only while the charges of the running
 // and finishing requests plus its own reservation fit hit_buffer_bytes;
 // nothing running always admits one.
@@ -108,7 +108,7 @@ struct cof_server {
   cof_handle* h = nullptr;
   uint64_t max_active_variants = 0;
   uint64_t hit_buffer_bytes = 0;
-  uint64_t hit_reserve_bytes = 64ull << 20;  // charged per running request at least
+  uint64_t hit_reserve_bytes = 0;  // charged per running request at least; 0: by its variants (reserve_of)
   uint64_t finishing_bytes = 0;              // hit buffers handed to the finisher, not yet freed (under mu)
   uint64_t held_hit_bytes = 0, max_held_hit_bytes = 0;  // after the latest step (under mu)
 
@@ -196,7 +196,15 @@ void want_build(cof_server* s) {
 
 // Device bytes a running request is charged against the hit budget.  Runs
 // on the worker thread, the only thread that grows a running request's hits.
-uint64_t hit_charge(const cof_server* s, const Request& r) { return std::max<uint64_t>(r.hits.cap, s->hit_reserve_bytes); }
+// A request's reservation: the set value, or by default 32 KiB per compare
+// variant (about the hits a variant finds over a human-sized genome at the
+// mismatch limits of the served mix) between 1 and 64 MiB, so a burst of
+// small requests is admitted together while a large one still reserves 64 MiB.
+uint64_t reserve_of(const cof_server* s, const Request& r) {
+  if (s->hit_reserve_bytes) return s->hit_reserve_bytes;
+  return std::min<uint64_t>(64ull << 20, std::max<uint64_t>(1ull << 20, (uint64_t)r.nvar << 15));
+}
+uint64_t hit_charge(const cof_server* s, const Request& r) { return std::max<uint64_t>(r.hits.cap, reserve_of(s, r)); }
 
 // True when the front pending request fits the variant budget and the hit
 // memory budget (under mu, on the worker thread).
@@ -209,7 +217,7 @@ bool admissible(const cof_server* s) {
     bytes += hit_charge(s, *r);
   }
   return used + s->pending.front()->nvar <= s->max_active_variants &&
-         bytes + s->hit_reserve_bytes <= s->hit_buffer_bytes;
+         bytes + reserve_of(s, *s->pending.front()) <= s->hit_buffer_bytes;
 }
 
 // True when the current tables hold a request still walking the ring.

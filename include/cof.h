@@ -155,8 +155,9 @@ cof_status cof_job_rows(const cof_handle* h, uint32_t job, const char** rows, si
  * Memory: the candidate queues are sized by the ring segment and shared by
  * all requests, so admission adds no candidate memory; each running request
  * holds a device hit buffer (8 B per hit) until its rows are formatted.  A
- * request is charged the larger of its hit buffer and a reservation (64 MiB
- * unless cof_server_set_hit_reserve says otherwise), and a waiting request is
+ * request is charged the larger of its hit buffer and a reservation (32 KiB
+ * per compare variant within [1, 64] MiB unless cof_server_set_hit_reserve
+ * says otherwise), and a waiting request is
  * admitted only while the charges of the running and finishing requests plus
  * its own reservation fit `hit_buffer_bytes` (0 = 8 GiB); nothing running
  * always admits one.  One step's hits must fit `hit_buffer_bytes` as well.
@@ -198,8 +199,9 @@ cof_status cof_server_stats(cof_server* s, uint64_t* steps, uint64_t* admitted, 
  * segments than a running request still needs.  Requests join only at step
  * boundaries.  Applies from the next step. */
 cof_status cof_server_set_step_segments(cof_server* s, uint32_t segments);
-/* Hit memory charged per running request at least (default 64 MiB); applies
- * to admissions after the call. */
+/* Hit memory charged per running request at least; applies to admissions
+ * after the call.  By default (or after a call with 0) a request reserves
+ * 32 KiB per compare variant, at least 1 MiB and at most 64 MiB. */
 cof_status cof_server_set_hit_reserve(cof_server* s, uint64_t bytes);
 /* Device bytes of request hit buffers after the latest ring step, their
  * maximum so far, and the bytes of the two shared candidate queues. */
