@@ -669,6 +669,42 @@ void launch_run_starts(const uint64_t* sorted, uint64_t n, const uint32_t* gid0,
   run_starts_kernel<<<(m + 127) / 128, 128, 0, stream>>>(sorted, n, gid0, m, out);
 }
 
+// Each sorted step hit goes to its request's buffer: request a owns ids
+// from gid0[a] and the hits [start[a], start[a + 1]) of the step; dst[a] is
+// where its run goes (null: the request takes no more hits).
+__global__ void scatter_runs_kernel(const uint64_t* __restrict__ sorted, uint64_t n, const uint32_t* __restrict__ gid0,
+                                    const uint64_t* __restrict__ start, uint64_t* const* __restrict__ dst, uint32_t m) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint64_t key = sorted[i];
+  const uint32_t gid = (uint32_t)(key >> 44);
+  uint32_t lo = 0, hi = m;  // last request whose first id <= gid
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (gid0[mid] <= gid) lo = mid;
+    else hi = mid;
+  }
+  uint64_t* d = dst[lo];
+  if (d) d[i - start[lo]] = key - ((uint64_t)gid0[lo] << 44);
+}
+
+void launch_scatter_runs(const uint64_t* sorted, uint64_t n, const uint32_t* gid0, const uint64_t* start,
+                         uint64_t* const* dst, uint32_t m, cudaStream_t stream) {
+  if (!n || !m) return;
+  scatter_runs_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(sorted, n, gid0, start, dst, m);
+}
+
+__global__ void offset_ids_kernel(const uint64_t* __restrict__ src, uint64_t n, uint32_t add,
+                                  uint64_t* __restrict__ dst) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i] + ((uint64_t)add << 44);
+}
+
+void launch_offset_ids(const uint64_t* src, uint64_t n, uint32_t add, uint64_t* dst, cudaStream_t stream) {
+  if (!n) return;
+  offset_ids_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(src, n, add, dst);
+}
+
 void launch_rebase_hits(const uint64_t* src, uint64_t n, uint32_t gid0, uint64_t* dst, cudaStream_t stream) {
   if (!n) return;
   rebase_hits_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(src, n, gid0, dst);

@@ -171,5 +171,12 @@ void launch_hit_histogram(const uint64_t* keys, uint64_t n, uint32_t levels, uin
 void launch_run_starts(const uint64_t* sorted, uint64_t n, const uint32_t* gid0, uint32_t m, uint64_t* out,
                        cudaStream_t stream);
 void launch_rebase_hits(const uint64_t* src, uint64_t n, uint32_t gid0, uint64_t* dst, cudaStream_t stream);
+// All requests' runs of sorted step keys in one launch: request a (ids from
+// gid0[a], keys [start[a], start[a + 1])) gets its run, ids rebased, at
+// dst[a] (null: skipped).
+void launch_scatter_runs(const uint64_t* sorted, uint64_t n, const uint32_t* gid0, const uint64_t* start,
+                         uint64_t* const* dst, uint32_t m, cudaStream_t stream);
+// The reverse of launch_rebase_hits: a copy of n keys with `add` added to their variant ids.
+void launch_offset_ids(const uint64_t* src, uint64_t n, uint32_t add, uint64_t* dst, cudaStream_t stream);
 
 }  // namespace cof

@@ -81,7 +81,7 @@ struct Request {
   std::string err;
   char* rows = nullptr;  // pinned buffer from the handle's pool (rows_cap bytes)
   size_t rows_cap = 0;
-  uint64_t rows_len = 0, n_rows = 0;
+  uint64_t rows_len = 0;
   cof_handle* pool = nullptr;  // returns `rows` to the pool on destruction
   Request() = default;
   Request(const Request&) = delete;
@@ -137,10 +137,11 @@ struct cof_server {
   uint64_t seg_words = kSegWords;  // plane words (32 start positions each) per ring segment
   std::atomic<uint32_t> step_segments{4};  // ring segments per step at most (cof_server_set_step_segments)
   uint64_t ring = 0, cur = 0;      // ring length in segments, current segment
-  DevBuf step_hits, step_sorted, step_count, step_bounds, step_gid0, sort_tmp;
+  DevBuf step_hits, step_sorted, step_count, step_bounds, step_gid0, step_dst, sort_tmp;
   // finisher-only state
   cudaStream_t fin_stream = nullptr;
-  DevBuf fmt_hits, fmt_bytes, fmt_off, fmt_cnt, fmt_tmp, fmt_text, fmt_vf, fmt_sf, fmt_pool, fmt_small;
+  DevBuf fmt_in, fmt_hits, fmt_bytes, fmt_off, fmt_cnt, fmt_tmp, fmt_text, fmt_vf, fmt_sf, fmt_pool, fmt_small,
+      fmt_gid0, fmt_bounds;
 };
 
 namespace {
@@ -315,6 +316,9 @@ cof_status run_step(cof_server* s, uint64_t k) {
     COF_CUDA(h, cudaMemcpyAsync(start.data(), s->step_bounds.p, A * 8, cudaMemcpyDeviceToHost, h->stream));
     COF_CUDA(h, cudaStreamSynchronize(h->stream));
     start[A] = count;
+    // Destinations of each request's run (buffers grown first), then one
+    // launch moves every run.
+    std::vector<uint64_t*> dst(A, nullptr);
     for (size_t a = 0; a < A; ++a) {
       Request& r = *T.reqs[a];
       const uint64_t k = start[a + 1] - start[a];
@@ -326,10 +330,14 @@ cof_status run_step(cof_server* s, uint64_t k) {
           COF_CUDA(h, cudaMemcpyAsync(bigger.p, r.hits.p, r.n_hits * 8, cudaMemcpyDeviceToDevice, h->stream));
         r.hits = std::move(bigger);  // the old buffer is freed in stream order
       }
-      launch_rebase_hits(s->step_sorted.as<uint64_t>() + start[a], k, T.gid0[a],
-                         r.hits.as<uint64_t>() + r.n_hits, h->stream);
+      dst[a] = r.hits.as<uint64_t>() + r.n_hits;
       r.n_hits += k;
     }
+    COF_CUDA(h, s->step_dst.ensure(A * sizeof(uint64_t*)));
+    COF_CUDA(h, cudaMemcpyAsync(s->step_bounds.p, start.data(), (A + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+    COF_CUDA(h, cudaMemcpyAsync(s->step_dst.p, dst.data(), A * sizeof(uint64_t*), cudaMemcpyHostToDevice, h->stream));
+    launch_scatter_runs(s->step_sorted.as<uint64_t>(), count, s->step_gid0.as<uint32_t>(),
+                        s->step_bounds.as<uint64_t>(), s->step_dst.as<uint64_t*>(), (uint32_t)A, h->stream);
     COF_CUDA(h, cudaGetLastError());
   }
   s->steps += k;
@@ -346,43 +354,68 @@ cof_status run_step(cof_server* s, uint64_t k) {
     }                                                                                   \
   } while (0)
 
-// Sorts a finished request's hits and formats its rows on the finisher's
-// stream, into a pinned host buffer from the handle's pool.
-cof_status format_request(cof_server* s, Request& r, std::string& err) {
+// Formats a batch of finished requests together on the finisher's stream:
+// their hits are copied into one buffer with the variant ids of request j
+// offset by the variants of the requests before it (the layout of a batched
+// search, each request keeping its own ids, thresholds and rows), sorted
+// once, their rows written in one pass, and each request's byte range copied
+// into a pinned host buffer of its own from the handle's pool.  Requests that
+// complete together (a burst that shared a ring pass) thus cost one sort and
+// one row pass instead of one each.
+cof_status format_batch(cof_server* s, const std::vector<ReqPtr>& rs, std::string& err) {
   cof_handle* h = s->h;
   cudaStream_t st = s->fin_stream;
-  if (r.last_append) COF_FIN(cudaStreamWaitEvent(st, r.last_append, 0));
-  const uint64_t nh = r.n_hits;
+  const size_t k = rs.size();
+  std::vector<uint32_t> gid0(k);
+  uint64_t nh = 0;
+  uint32_t ids = 0;
+  for (size_t j = 0; j < k; ++j) {
+    if (rs[j]->last_append) COF_FIN(cudaStreamWaitEvent(st, rs[j]->last_append, 0));
+    gid0[j] = ids;
+    ids += rs[j]->nvar;
+    nh += rs[j]->n_hits;
+  }
   if (!nh) return COF_OK;
   std::vector<VariantFmt> vf;
   std::vector<ShapeFmt> sf;
   std::string pool;
-  append_format_tables(r.job, vf, sf, pool);
+  for (const ReqPtr& r : rs) append_format_tables(r->job, vf, sf, pool);
   COF_FIN(s->fmt_vf.ensure(vf.size() * sizeof(VariantFmt)));
   COF_FIN(s->fmt_sf.ensure(std::max<size_t>(sf.size(), 1) * sizeof(ShapeFmt)));
   COF_FIN(s->fmt_pool.ensure(std::max<size_t>(pool.size(), 1)));
+  COF_FIN(s->fmt_in.ensure(nh * 8));
   COF_FIN(s->fmt_hits.ensure(nh * 8));
   COF_FIN(s->fmt_bytes.ensure(nh * 8));
   COF_FIN(s->fmt_off.ensure(nh * 8));
   COF_FIN(s->fmt_cnt.ensure(nh * 4));
-  COF_FIN(s->fmt_small.ensure(16));
+  COF_FIN(s->fmt_gid0.ensure(k * 4));
+  COF_FIN(s->fmt_bounds.ensure((k + 1) * 8));
   COF_FIN(cudaMemcpyAsync(s->fmt_vf.p, vf.data(), vf.size() * sizeof(VariantFmt), cudaMemcpyHostToDevice, st));
   if (!sf.empty())
     COF_FIN(cudaMemcpyAsync(s->fmt_sf.p, sf.data(), sf.size() * sizeof(ShapeFmt), cudaMemcpyHostToDevice, st));
   if (!pool.empty()) COF_FIN(cudaMemcpyAsync(s->fmt_pool.p, pool.data(), pool.size(), cudaMemcpyHostToDevice, st));
-  size_t t0 = 0, t1 = 0, t2 = 0;
-  COF_FIN(cub::DeviceRadixSort::SortKeys(nullptr, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(), (int64_t)nh,
-                                         0, 64, st));
+  COF_FIN(cudaMemcpyAsync(s->fmt_gid0.p, gid0.data(), k * 4, cudaMemcpyHostToDevice, st));
+  uint64_t at = 0;
+  for (size_t j = 0; j < k; ++j) {
+    Request& r = *rs[j];
+    launch_offset_ids(r.hits.as<uint64_t>(), r.n_hits, gid0[j], s->fmt_in.as<uint64_t>() + at, st);
+    at += r.n_hits;
+    r.hits.st = st;  // freed in order after its copy on this stream
+    r.hits.release();
+  }
+  // Row order depends on the strand bit, the position and the variant id.
+  int end_bit = 44;
+  for (uint32_t v = std::max<uint32_t>(ids, 2) - 1; v; v >>= 1) ++end_bit;
+  end_bit = std::min(end_bit, 64);
+  size_t t0 = 0, t1 = 0;
+  COF_FIN(cub::DeviceRadixSort::SortKeys(nullptr, t0, s->fmt_in.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
+                                         (int64_t)nh, 7, end_bit, st));
   COF_FIN(cub::DeviceScan::ExclusiveSum(nullptr, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
                                         (int64_t)nh, st));
-  COF_FIN(cub::DeviceReduce::Sum(nullptr, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(), (int64_t)nh,
-                                 st));
-  COF_FIN(s->fmt_tmp.ensure(std::max(t0, std::max(t1, t2))));
+  COF_FIN(s->fmt_tmp.ensure(std::max(t0, t1)));
   t0 = s->fmt_tmp.cap;
-  COF_FIN(cub::DeviceRadixSort::SortKeys(s->fmt_tmp.p, t0, r.hits.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
-                                         (int64_t)nh, 0, 64, st));
-  r.hits.st = st;  // freed in order after the sort on this stream
-  r.hits.release();
+  COF_FIN(cub::DeviceRadixSort::SortKeys(s->fmt_tmp.p, t0, s->fmt_in.as<uint64_t>(), s->fmt_hits.as<uint64_t>(),
+                                         (int64_t)nh, 7, end_bit, st));
   const GenomeView gv = h->genome.view();
   FormatTables ft{s->fmt_vf.as<VariantFmt>(), s->fmt_sf.as<ShapeFmt>(), s->fmt_pool.as<char>()};
   launch_row_lengths(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_bytes.as<uint64_t>(), s->fmt_cnt.as<uint32_t>(),
@@ -390,34 +423,39 @@ cof_status format_request(cof_server* s, Request& r, std::string& err) {
   t1 = s->fmt_tmp.cap;
   COF_FIN(cub::DeviceScan::ExclusiveSum(s->fmt_tmp.p, t1, s->fmt_bytes.as<uint64_t>(), s->fmt_off.as<uint64_t>(),
                                         (int64_t)nh, st));
-  t2 = s->fmt_tmp.cap;
-  COF_FIN(cub::DeviceReduce::Sum(s->fmt_tmp.p, t2, s->fmt_cnt.as<uint32_t>(), s->fmt_small.as<uint64_t>(),
-                                 (int64_t)nh, st));
-  uint64_t last[3] = {0, 0, 0};
-  COF_FIN(cudaMemcpyAsync(&last[0], s->fmt_off.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, st));
-  COF_FIN(cudaMemcpyAsync(&last[1], s->fmt_bytes.as<uint64_t>() + nh - 1, 8, cudaMemcpyDeviceToHost, st));
-  COF_FIN(cudaMemcpyAsync(&last[2], s->fmt_small.p, 8, cudaMemcpyDeviceToHost, st));
+  launch_job_bounds(s->fmt_hits.as<uint64_t>(), nh, s->fmt_gid0.as<uint32_t>(), (uint32_t)k, s->fmt_off.as<uint64_t>(),
+                    s->fmt_bytes.as<uint64_t>(), s->fmt_bounds.as<uint64_t>(), st);
+  std::vector<uint64_t> bounds(k + 1);
+  COF_FIN(cudaMemcpyAsync(bounds.data(), s->fmt_bounds.p, (k + 1) * 8, cudaMemcpyDeviceToHost, st));
   COF_FIN(cudaStreamSynchronize(st));
-  const uint64_t bytes = last[0] + last[1];
+  const uint64_t bytes = bounds[k];
   COF_FIN(s->fmt_text.ensure(bytes + 1));
   launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), 0, bytes,
                     s->fmt_text.as<char>(), st);
   COF_FIN(cudaGetLastError());
-  // Rows go straight to a pinned host buffer from the handle's pool.
-  size_t cap = 0;
-  char* dst = (char*)pinned_acquire(h, bytes + 1, &cap);
-  if (!dst) {
-    err = "no pinned host memory for " + std::to_string(bytes) + " bytes of rows";
-    return COF_ERR_NOMEM;
+  // Each request's rows go straight to a pinned host buffer from the pool.
+  std::vector<char*> dst(k, nullptr);
+  for (size_t j = 0; j < k; ++j) {
+    const uint64_t len = bounds[j + 1] - bounds[j];
+    if (!len) continue;
+    size_t cap = 0;
+    dst[j] = (char*)pinned_acquire(h, len + 1, &cap);
+    if (!dst[j]) {
+      err = "no pinned host memory for " + std::to_string(len) + " bytes of rows";
+      COF_FIN(cudaStreamSynchronize(st));
+      return COF_ERR_NOMEM;
+    }
+    rs[j]->pool = h;
+    rs[j]->rows = dst[j];
+    rs[j]->rows_cap = cap;
+    COF_FIN(cudaMemcpyAsync(dst[j], s->fmt_text.as<char>() + bounds[j], len, cudaMemcpyDeviceToHost, st));
   }
-  r.pool = h;
-  r.rows = dst;
-  r.rows_cap = cap;
-  COF_FIN(cudaMemcpyAsync(dst, s->fmt_text.p, bytes, cudaMemcpyDeviceToHost, st));
   COF_FIN(cudaStreamSynchronize(st));
-  dst[bytes] = 0;
-  r.rows_len = bytes;
-  r.n_rows = last[2];
+  for (size_t j = 0; j < k; ++j) {
+    const uint64_t len = bounds[j + 1] - bounds[j];
+    if (dst[j]) dst[j][len] = 0;
+    rs[j]->rows_len = len;
+  }
   return COF_OK;
 }
 
@@ -433,31 +471,48 @@ void finish(cof_server* s, const ReqPtr& r, cof_status st, const std::string& er
   s->cv_done.notify_all();
 }
 
-// Finisher thread: formats completed requests in completion order.
+// Finisher thread: formats completed requests in completion order, every
+// request waiting when it looks (up to kFinishBatch requests and 2^20 compare
+// variants) in one batch.
+constexpr size_t kFinishBatch = 1024;
+
 void finisher_main(cof_server* s) {
   cudaSetDevice(s->h->device);
   for (;;) {
-    ReqPtr r;
+    std::vector<ReqPtr> batch;
     {
       std::unique_lock<std::mutex> lock(s->mu);
       s->cv_finish.wait(lock, [&] { return s->worker_gone || !s->to_finish.empty(); });
       if (s->to_finish.empty()) return;  // the worker has stopped and everything is drained
-      r = s->to_finish.front();
-      s->to_finish.pop_front();
+      uint64_t ids = 0;
+      while (!s->to_finish.empty() && batch.size() < kFinishBatch &&
+             (batch.empty() || ids + s->to_finish.front()->nvar < (1u << 20))) {
+        ids += s->to_finish.front()->nvar;
+        batch.push_back(s->to_finish.front());
+        s->to_finish.pop_front();
+      }
     }
-    std::string err = r->err;
-    const cof_status st = r->status ? r->status : format_request(s, *r, err);
-    r->hits.st = s->fin_stream;
-    r->hits.release();
-    {
-      std::lock_guard<std::mutex> lock(s->mu);
-      s->finishing_bytes -= r->charged;
+    // Requests that failed on the ring finish with their error; the rest are
+    // formatted together.
+    std::vector<ReqPtr> ok;
+    for (const ReqPtr& r : batch)
+      if (!r->status) ok.push_back(r);
+    std::string err;
+    const cof_status st = ok.empty() ? COF_OK : format_batch(s, ok, err);
+    for (const ReqPtr& r : batch) {
+      r->hits.st = s->fin_stream;
+      r->hits.release();
+      {
+        std::lock_guard<std::mutex> lock(s->mu);
+        s->finishing_bytes -= r->charged;
+      }
+      if (r->last_append) {
+        cudaEventDestroy(r->last_append);
+        r->last_append = nullptr;
+      }
+      if (r->status) finish(s, r, r->status, r->err);
+      else finish(s, r, st, st ? err : std::string());
     }
-    if (r->last_append) {
-      cudaEventDestroy(r->last_append);
-      r->last_append = nullptr;
-    }
-    finish(s, r, st, st ? err : std::string());
   }
 }
 
@@ -620,10 +675,11 @@ cof_status cof_server_start(cof_handle* h, uint64_t max_active_variants, uint64_
   }
   // Buffers that grow with the request mix are stream-ordered on the stream
   // that uses them (a plain cudaFree would wait for the whole device).
-  for (DevBuf* b : {&s->step_hits, &s->step_sorted, &s->step_count, &s->step_bounds, &s->step_gid0, &s->sort_tmp})
+  for (DevBuf* b : {&s->step_hits, &s->step_sorted, &s->step_count, &s->step_bounds, &s->step_gid0, &s->step_dst,
+                    &s->sort_tmp})
     b->st = h->stream;
   for (DevBuf* b : {&s->fmt_hits, &s->fmt_bytes, &s->fmt_off, &s->fmt_cnt, &s->fmt_tmp, &s->fmt_text, &s->fmt_vf,
-                    &s->fmt_sf, &s->fmt_pool, &s->fmt_small})
+                    &s->fmt_sf, &s->fmt_pool, &s->fmt_small, &s->fmt_in, &s->fmt_gid0, &s->fmt_bounds})
     b->st = s->fin_stream;
   s->worker = std::thread(worker_main, s);
   s->builder = std::thread(builder_main, s);
