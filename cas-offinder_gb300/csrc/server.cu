@@ -45,6 +45,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -362,7 +363,8 @@ cof_status run_step(cof_server* s, uint64_t k) {
 // into a pinned host buffer of its own from the handle's pool.  Requests that
 // complete together (a burst that shared a ring pass) thus cost one sort and
 // one row pass instead of one each.
-cof_status format_batch(cof_server* s, const std::vector<ReqPtr>& rs, std::string& err) {
+cof_status format_batch(cof_server* s, const std::vector<ReqPtr>& rs, std::string& err,
+                        const std::function<void(size_t)>& delivered) {
   cof_handle* h = s->h;
   cudaStream_t st = s->fin_stream;
   const size_t k = rs.size();
@@ -375,7 +377,10 @@ cof_status format_batch(cof_server* s, const std::vector<ReqPtr>& rs, std::strin
     ids += rs[j]->nvar;
     nh += rs[j]->n_hits;
   }
-  if (!nh) return COF_OK;
+  if (!nh) {
+    for (size_t j = 0; j < k; ++j) delivered(j);
+    return COF_OK;
+  }
   std::vector<VariantFmt> vf;
   std::vector<ShapeFmt> sf;
   std::string pool;
@@ -433,28 +438,30 @@ cof_status format_batch(cof_server* s, const std::vector<ReqPtr>& rs, std::strin
   launch_write_rows(gv, ft, s->fmt_hits.as<uint64_t>(), nh, s->fmt_off.as<uint64_t>(), 0, bytes,
                     s->fmt_text.as<char>(), st);
   COF_FIN(cudaGetLastError());
-  // Each request's rows go straight to a pinned host buffer from the pool.
-  std::vector<char*> dst(k, nullptr);
-  for (size_t j = 0; j < k; ++j) {
-    const uint64_t len = bounds[j + 1] - bounds[j];
-    if (!len) continue;
-    size_t cap = 0;
-    dst[j] = (char*)pinned_acquire(h, len + 1, &cap);
-    if (!dst[j]) {
-      err = "no pinned host memory for " + std::to_string(len) + " bytes of rows";
-      COF_FIN(cudaStreamSynchronize(st));
-      return COF_ERR_NOMEM;
-    }
-    rs[j]->pool = h;
-    rs[j]->rows = dst[j];
-    rs[j]->rows_cap = cap;
-    COF_FIN(cudaMemcpyAsync(dst[j], s->fmt_text.as<char>() + bounds[j], len, cudaMemcpyDeviceToHost, st));
-  }
   COF_FIN(cudaStreamSynchronize(st));
+  // Each request's rows go straight to a pinned host buffer from the pool,
+  // one request after the other, and each request is delivered as soon as
+  // its rows have landed: callers that release their rows promptly hand
+  // their buffers back for the next requests of the batch, so a batch does
+  // not need all of its rows pinned at once.
   for (size_t j = 0; j < k; ++j) {
     const uint64_t len = bounds[j + 1] - bounds[j];
-    if (dst[j]) dst[j][len] = 0;
     rs[j]->rows_len = len;
+    if (len) {
+      size_t cap = 0;
+      char* dst = (char*)pinned_acquire(h, len + 1, &cap);
+      if (!dst) {
+        err = "no pinned host memory for " + std::to_string(len) + " bytes of rows";
+        return COF_ERR_NOMEM;
+      }
+      rs[j]->pool = h;
+      rs[j]->rows = dst;
+      rs[j]->rows_cap = cap;
+      COF_FIN(cudaMemcpyAsync(dst, s->fmt_text.as<char>() + bounds[j], len, cudaMemcpyDeviceToHost, st));
+      COF_FIN(cudaStreamSynchronize(st));
+      dst[len] = 0;
+    }
+    delivered(j);
   }
   return COF_OK;
 }
@@ -493,13 +500,8 @@ void finisher_main(cof_server* s) {
       }
     }
     // Requests that failed on the ring finish with their error; the rest are
-    // formatted together.
-    std::vector<ReqPtr> ok;
-    for (const ReqPtr& r : batch)
-      if (!r->status) ok.push_back(r);
-    std::string err;
-    const cof_status st = ok.empty() ? COF_OK : format_batch(s, ok, err);
-    for (const ReqPtr& r : batch) {
+    // formatted together and delivered one by one as their rows land.
+    auto close = [&](const ReqPtr& r, cof_status st, const std::string& e) {
       r->hits.st = s->fin_stream;
       r->hits.release();
       {
@@ -510,9 +512,21 @@ void finisher_main(cof_server* s) {
         cudaEventDestroy(r->last_append);
         r->last_append = nullptr;
       }
-      if (r->status) finish(s, r, r->status, r->err);
-      else finish(s, r, st, st ? err : std::string());
+      finish(s, r, st, e);
+    };
+    std::vector<ReqPtr> ok;
+    for (const ReqPtr& r : batch) {
+      if (r->status) close(r, r->status, r->err);
+      else ok.push_back(r);
     }
+    std::vector<bool> closed(ok.size(), false);
+    std::string err;
+    const cof_status st = ok.empty() ? COF_OK : format_batch(s, ok, err, [&](size_t j) {
+      closed[j] = true;
+      close(ok[j], COF_OK, std::string());
+    });
+    for (size_t j = 0; j < ok.size(); ++j)
+      if (!closed[j]) close(ok[j], st ? st : COF_ERR_STATE, st ? err : std::string("not formatted"));
   }
 }
 
