@@ -478,10 +478,12 @@ void finish(cof_server* s, const ReqPtr& r, cof_status st, const std::string& er
   s->cv_done.notify_all();
 }
 
-// Finisher thread: formats completed requests in completion order, every
-// request waiting when it looks (up to kFinishBatch requests and 2^20 compare
-// variants) in one batch.
+// Finisher thread: formats completed requests in completion order, the
+// requests waiting when it looks in batches of up to kFinishBatch requests,
+// kFinishBatchHits hits (so the batch buffers stay modest and are reused
+// from batch to batch) and 2^20 compare variants.
 constexpr size_t kFinishBatch = 1024;
+constexpr uint64_t kFinishBatchHits = 1ull << 22;
 
 void finisher_main(cof_server* s) {
   cudaSetDevice(s->h->device);
@@ -491,10 +493,12 @@ void finisher_main(cof_server* s) {
       std::unique_lock<std::mutex> lock(s->mu);
       s->cv_finish.wait(lock, [&] { return s->worker_gone || !s->to_finish.empty(); });
       if (s->to_finish.empty()) return;  // the worker has stopped and everything is drained
-      uint64_t ids = 0;
+      uint64_t ids = 0, hits = 0;
       while (!s->to_finish.empty() && batch.size() < kFinishBatch &&
-             (batch.empty() || ids + s->to_finish.front()->nvar < (1u << 20))) {
+             (batch.empty() || (ids + s->to_finish.front()->nvar < (1u << 20) &&
+                                hits + s->to_finish.front()->n_hits <= kFinishBatchHits))) {
         ids += s->to_finish.front()->nvar;
+        hits += s->to_finish.front()->n_hits;
         batch.push_back(s->to_finish.front());
         s->to_finish.pop_front();
       }
