@@ -94,6 +94,25 @@ def test_server_step_segments_keep_rows(P, built, oracle, tmp_path):
             assert stats["completed"] == len(texts)
 
 
+def test_server_burst_is_formatted_together(P, built, oracle, tmp_path):
+    """Requests submitted back to back share the ring; those that complete at
+    the same step are formatted as one batch (one sort and one row pass over
+    all of their hits, each request's byte range copied out on its own); each
+    still gets exactly its own rows."""
+    genome, texts = make_genome_and_requests(P, tmp_path)
+    want = oracle_rows(oracle, tmp_path, texts)
+    with P.CasOFFinder(0) as eng:
+        eng.load_genome_file(genome)
+        with P.Server(eng, segment_positions=1 << 15) as srv:
+            tickets = [srv.submit(t) for t in texts]
+            got = [srv.wait(t) for t in tickets]
+            stats = srv.stats()
+        for j, (rows, _) in enumerate(got):
+            assert P.HEADER.encode() + rows == want[j], f"request {j} of the burst"
+        assert stats["completed"] == len(texts)
+        assert stats["max_active"] >= 2  # requests shared the ring
+
+
 def test_server_admits_by_hit_memory(P, built, oracle, tmp_path):
     """Admission by device memory: each running request is charged at least
     its hit reservation against hit_buffer_bytes, so a reservation of half the
