@@ -678,6 +678,7 @@ def main():
     eng.search_view()
     eng.set_profiling(False)
     stats = {k: eng.kernel_stats(k) for k in ("finder", "comparer", "format")}
+    stages = {k: eng.kernel_stats(k)["ms"] for k in ("sort", "rows_to_host")}
     tests_stat = eng.kernel_stats("comparer.tests")
 
     # ---- value: genome resident in HBM (passes replayed as a CUDA graph)
@@ -806,7 +807,8 @@ def main():
                     "d2h_bytes_per_step": rows_len + 16, "ms_per_step": e2e_ms,
                     "planes_h2d_alone_ms": h2d_alone_ms,
                     "planes_h2d_alone_gbs": 3 * W * 4 / (h2d_alone_ms * 1e-3) / 1e9,
-                    "d2h_1gb_gbs": {"copy_engine": d2h["dma"] / 1e9, "sm_stores": d2h["sm"] / 1e9}},
+                    "d2h_1gb_gbs": {"copy_engine": d2h["dma"] / 1e9, "sm_stores": d2h["sm"] / 1e9,
+                                    "two_copy_engines": d2h["dma2"] / 1e9}},
             "roofline": {"bound": "int-pipe", "kernel": "comparer", "achieved": achieved, "peak": peak,
                          "unit": "G base-comparisons/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,
@@ -817,7 +819,7 @@ def main():
                                 "us_per_launch": fnd["ms"] * 1e3 / max(fnd["launches"], 1),
                                 "basis": "0.375 B per genome position (3 bit planes read) + 4 B per candidate "
                                          "(queue entry written); launches timed alone"},
-            "kernel_ms_per_step": {k: v["ms"] for k, v in stats.items()},
+            "kernel_ms_per_step": dict({k: v["ms"] for k, v in stats.items()}, **stages),
             "batched": batched,
             "pam_variety": pam_variety,
             "served": served,
@@ -855,7 +857,7 @@ def run_batched(P, eng, lens, rates, args, capture=None):
     eng.search_view()
     eng.set_profiling(False)
     cmp = eng.kernel_stats("comparer")
-    kernel_ms = {k: eng.kernel_stats(k)["ms"] for k in ("finder", "comparer", "format")}
+    kernel_ms = {k: eng.kernel_stats(k)["ms"] for k in ("finder", "comparer", "sort", "format", "rows_to_host")}
     eng.synchronize()
     eng.timer_start()
     for _ in range(args.batched_steps):

@@ -655,16 +655,16 @@ def pipe_rates(device=0):
 
 def d2h_rates(device=0, nbytes=1 << 30):
     """Device -> pinned host copy rates (bytes/s) of `nbytes`: {'dma': one
-    cudaMemcpyAsync, 'sm': a kernel storing into the mapped host buffer}.
+    cudaMemcpyAsync, 'sm': a kernel storing into the mapped host buffer,
+    'dma2': two half-size copies on two streams at once}.
     From libcofrates.so, the measurement library built beside the engine."""
     L = ctypes.CDLL(RATES_LIB_PATH)
     L.cofx_d2h_rates.restype = ctypes.c_int
-    L.cofx_d2h_rates.argtypes = [ctypes.c_int, ctypes.c_size_t, ctypes.POINTER(ctypes.c_double),
-                                 ctypes.POINTER(ctypes.c_double)]
-    a, b = ctypes.c_double(), ctypes.c_double()
-    if L.cofx_d2h_rates(device, nbytes, ctypes.byref(a), ctypes.byref(b)) != 0:
+    L.cofx_d2h_rates.argtypes = [ctypes.c_int, ctypes.c_size_t] + [ctypes.POINTER(ctypes.c_double)] * 3
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    if L.cofx_d2h_rates(device, nbytes, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)) != 0:
         raise RuntimeError("cofx_d2h_rates failed")
-    return {"dma": a.value, "sm": b.value}
+    return {"dma": a.value, "sm": b.value, "dma2": c.value}
 
 
 # ---------------------------------------------------------------- synthetic genomes

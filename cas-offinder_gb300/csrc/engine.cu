@@ -930,8 +930,10 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
                                      (int64_t)nhits, h->stream));
   COF_CUDA(h, h->sort_tmp.ensure(std::max(tmp, std::max(tmp2, tmp3))));
   tmp = h->sort_tmp.cap;
+  if ((st = record_start(h, evs, "sort", (double)nhits, h->stream))) return st;
   COF_CUDA(h, cub::DeviceRadixSort::SortKeys(h->sort_tmp.p, tmp, h->hits.as<uint64_t>(), h->hits_sorted.as<uint64_t>(),
                                              (int64_t)nhits, 7, end_bit, h->stream));
+  if ((st = record_stop(h, evs, h->stream))) return st;
   // Row sizes, offsets, per-job byte ranges, then the rows themselves.
   const GenomeView gv = h->genome.view();
   FormatTables ft{h->vfmt.as<VariantFmt>(), h->sfmt.as<ShapeFmt>(), h->pool.as<char>()};
@@ -977,21 +979,38 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
     if (!h->stream_ev[0]) COF_CUDA(h, cudaEventCreateWithFlags(&h->stream_ev[0], cudaEventDisableTiming));
     ck[0] = 0;
     ck[nck] = bytes;
+    // Profiled searches also time the row copies to the host (second stream).
+    cudaEvent_t copy_ev[2] = {nullptr, nullptr};
+    if (h->profiling)
+      for (cudaEvent_t& e : copy_ev) COF_CUDA(h, cudaEventCreate(&e));
     for (uint64_t k = 0; k < nck; ++k) {
       const uint64_t i0 = k * chunk_hits, i1 = std::min(nhits, i0 + chunk_hits);
       launch_write_rows(gv, ft, h->hits_sorted.as<uint64_t>() + i0, i1 - i0, h->row_offsets.as<uint64_t>() + i0, 0,
                         ck[k + 1], h->text.as<char>(), h->stream);
       COF_CUDA(h, cudaEventRecord(h->stream_ev[0], h->stream));
       COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->stream_ev[0], 0));
+      if (k == 0 && copy_ev[0]) COF_CUDA(h, cudaEventRecord(copy_ev[0], h->stream2));
       if (ck[k + 1] > ck[k])
         COF_CUDA(h, cudaMemcpyAsync((char*)h->host_text.p + ck[k], h->text.as<char>() + ck[k], ck[k + 1] - ck[k],
                                     cudaMemcpyDeviceToHost, h->stream2));
     }
+    if (copy_ev[1]) COF_CUDA(h, cudaEventRecord(copy_ev[1], h->stream2));
     if ((st = record_stop(h, evs, h->stream))) return st;
     COF_CUDA(h, cudaGetLastError());
     COF_CUDA(h, cudaStreamSynchronize(h->stream2));
     COF_CUDA(h, cudaStreamSynchronize(h->stream));
     ((char*)h->host_text.p)[bytes] = 0;
+    if (copy_ev[0]) {
+      // From the first chunk's copy becoming ready to the last copy's end.
+      float ms = 0;
+      if (nck && cudaEventElapsedTime(&ms, copy_ev[0], copy_ev[1]) == cudaSuccess) {
+        KernelStat& ks = h->stats["rows_to_host"];
+        ks.launches += 1;
+        ks.ms += ms;
+        ks.units += (double)bytes;
+      }
+      for (cudaEvent_t e : copy_ev) cudaEventDestroy(e);
+    }
   } else {
     // Rows in chunks of kBatch hits: chunk k+1 is formatted and copied while
     // the caller writes chunk k (two device and two pinned host buffers).

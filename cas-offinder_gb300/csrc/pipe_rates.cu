@@ -99,13 +99,13 @@ __global__ void sm_copy(const uint4* __restrict__ src, uint4* __restrict__ dst, 
 
 }  // namespace
 
-//   int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm);
+//   int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm, double* dma2);
 // Device -> pinned host copy rates in bytes/s for a buffer of `bytes` (a
-// multiple of 16): one cudaMemcpyAsync (copy engine) and a kernel whose
-// threads store into the mapped host buffer.  Best of three each.  Returns 0
-// on success.
-extern "C" int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm) {
-  if (cudaSetDevice(device) != cudaSuccess || bytes == 0 || bytes % 16) return 1;
+// multiple of 32): one cudaMemcpyAsync (copy engine), a kernel whose threads
+// store into the mapped host buffer, and two copies of half the buffer each
+// on two streams at once.  Best of three each.  Returns 0 on success.
+extern "C" int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm, double* dma2) {
+  if (cudaSetDevice(device) != cudaSuccess || bytes == 0 || bytes % 32) return 1;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   void *d = nullptr, *h = nullptr, *hd = nullptr;
@@ -116,10 +116,13 @@ extern "C" int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm)
   }
   int rc = 0;
   if (cudaHostGetDevicePointer(&hd, h, 0) != cudaSuccess || cudaMemset(d, 1, bytes) != cudaSuccess) rc = 1;
-  cudaEvent_t a, b;
+  cudaEvent_t a, b, j;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  double best_dma = 0, best_sm = 0;
+  cudaEventCreate(&j);
+  cudaStream_t s2 = nullptr;
+  if (cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess) rc = 1;
+  double best_dma = 0, best_sm = 0, best_dma2 = 0;
   for (int rep = 0; rc == 0 && rep < 4; ++rep) {  // the first of each is a warm-up
     float ms = 0;
     cudaEventRecord(a);
@@ -134,14 +137,28 @@ extern "C" int cofx_d2h_rates(int device, size_t bytes, double* dma, double* sm)
     cudaEventSynchronize(b);
     cudaEventElapsedTime(&ms, a, b);
     if (rep && ms > 0) best_sm = std::max(best_sm, bytes / (ms * 1e-3));
+    // Two halves at once, on the legacy stream and on s2.
+    cudaEventRecord(a);
+    cudaStreamWaitEvent(s2, a, 0);
+    cudaMemcpyAsync(h, d, bytes / 2, cudaMemcpyDeviceToHost, 0);
+    cudaMemcpyAsync((char*)h + bytes / 2, (const char*)d + bytes / 2, bytes / 2, cudaMemcpyDeviceToHost, s2);
+    cudaEventRecord(j, s2);
+    cudaStreamWaitEvent(0, j, 0);
+    cudaEventRecord(b);
+    cudaEventSynchronize(b);
+    cudaEventElapsedTime(&ms, a, b);
+    if (rep && ms > 0) best_dma2 = std::max(best_dma2, bytes / (ms * 1e-3));
   }
   if (cudaGetLastError() != cudaSuccess) rc = 1;
   cudaEventDestroy(a);
   cudaEventDestroy(b);
+  cudaEventDestroy(j);
+  if (s2) cudaStreamDestroy(s2);
   cudaFreeHost(h);
   cudaFree(d);
   if (dma) *dma = best_dma;
   if (sm) *sm = best_sm;
+  if (dma2) *dma2 = best_dma2;
   return rc;
 }
 

@@ -354,7 +354,9 @@ cof_status cof_set_profiling(cof_handle* h, int enable);
 /* Totals since profiling was enabled for kernel `name` ("finder", "comparer",
  * "format"; "comparer.tests" counts variant tests in `units`,
  * "comparer.lop3" the lane LOP3 instructions the bit-sliced comparer's count
- * issues by its op model, "finder.candidates" the queue entries written): launches,
+ * issues by its op model, "finder.candidates" the queue entries written,
+ * "sort" the hit-key sort, "rows_to_host" the row copies to host memory from
+ * the first chunk's copy to the last's end, `units` = bytes): launches,
  * summed device milliseconds and algorithmic units
  * (finder: genome positions scanned; comparer: base comparisons, i.e. the
  * non-N positions of each compare variant times the strand-oriented
