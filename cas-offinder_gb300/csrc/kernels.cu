@@ -183,7 +183,11 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(qcount, total);
     base = __shfl_sync(kFull, base, 0);
-    // Within a word: descending bit order, '+' before '-'.
+    // Within a word: the '+' entries, then the '-' entries, each strand two
+    // bits per iteration (its highest and lowest remaining candidates), so a
+    // loop runs about half as often as the lane with the most candidates
+    // has set bits.  The order inside a word does not matter (the comparer
+    // reads a word's windows together; hits are sorted afterwards).
     auto emit = [&](uint32_t* dst) {
       uint32_t pass0 = 0;  // entries of the earlier passes
 #pragma unroll
@@ -191,17 +195,21 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
         const uint32_t mine = (k & 1) ? incl[k / 2] >> 16 : incl[k / 2] & 0xFFFFu;
         uint32_t at = pass0 + mine - cnt[k];
         pass0 += tot[k];
-        const uint32_t rel = (uint32_t)((wb + 32 * k + lane - w_begin) << 5);
+        const uint32_t e0 = (uint32_t)((wb + 32 * k + lane - w_begin) << 6);  // entry of bit 0, '+'
         uint32_t f = fwd[k], r = rev[k];
         while (f) {
-          const unsigned b = 31 - __clz(f);
-          f ^= 1u << b;
-          dst[at++] = (rel + b) << 1;
+          const unsigned hb = 31 - __clz(f), lb = __ffs(f) - 1;
+          dst[at] = e0 + 2 * hb;
+          if (lb != hb) dst[at + 1] = e0 + 2 * lb;
+          at += lb != hb ? 2 : 1;
+          f &= ~((1u << hb) | (1u << lb));
         }
         while (r) {
-          const unsigned b = 31 - __clz(r);
-          r ^= 1u << b;
-          dst[at++] = ((rel + b) << 1) | 1u;
+          const unsigned hb = 31 - __clz(r), lb = __ffs(r) - 1;
+          dst[at] = e0 + 2 * hb + 1;
+          if (lb != hb) dst[at + 1] = e0 + 2 * lb + 1;
+          at += lb != hb ? 2 : 1;
+          r &= ~((1u << hb) | (1u << lb));
         }
       }
     };
