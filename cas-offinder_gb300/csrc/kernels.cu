@@ -59,13 +59,37 @@ constexpr int kFinderWords = 4;     // plane words per lane per pass
 constexpr int kFinderStage = 1024;  // staged entries per warp; denser warps store directly
 
 // Device form of a FinderPattern: per pattern position that can mismatch its
-// window offset and the five class masks (T, C, A, G, other byte) as
-// all-ones / all-zeros words, so the scan does no decoding.
+// window offset and its class bits, which pick the LOP3 truth table of the
+// mismatch rule (one instruction per position and word).
 struct FinderMasks {
   uint32_t L, nf, nr;
   uint8_t fk[kMaxL], rk[kMaxL];
-  uint32_t fm[kMaxL][5], rm[kMaxL][5];
+  uint8_t fc[kMaxL], rc[kMaxL];  // class bits of each position (class_bits_of)
 };
+
+// One LOP3 with truth table LUT over (a, b, c) = (0xF0, 0xCC, 0xAA).
+template <uint32_t LUT>
+__device__ __forceinline__ uint32_t lop3(uint32_t a, uint32_t b, uint32_t c) {
+  uint32_t d;
+  asm("lop3.b32 %0, %1, %2, %3, %4;" : "=r"(d) : "r"(a), "r"(b), "r"(c), "n"(LUT));
+  return d;
+}
+
+// The mismatch rule of one pattern byte as one LOP3 of (hi, lo, other) bits:
+// class bits T, C, A, G, other (bits 0-4) select the truth-table entries of
+// (h, l, o) = (0,0,0), (0,1,0), (1,0,0), (1,1,0) and every o = 1.
+__host__ __device__ constexpr uint32_t class_lut(uint32_t v) {
+  return ((v & 1) ? 0x01u : 0u) | ((v & 2) ? 0x04u : 0u) | ((v & 4) ? 0x10u : 0u) | ((v & 8) ? 0x40u : 0u) |
+         ((v & 16) ? 0xAAu : 0u);
+}
+
+// bad[k] |= mismatches of pattern class `cls` at window offset q, for the K
+// words of a lane.  The class is the same for every lane (one pattern), so
+// the switch is warp-uniform.
+template <int NK, int K>
+__device__ __forceinline__ void accumulate_position(uint32_t cls, unsigned q, const uint32_t (&h)[K][NK + 1],
+                                                    const uint32_t (&l)[K][NK + 1], const uint32_t (&o)[K][NK + 1],
+                                                    uint32_t (&bad)[K]);
 
 // 32 consecutive bits starting at bit k of the window words x0|x1|x2 (NK = 1:
 // k < 32 and x2 unused).
@@ -73,6 +97,29 @@ template <int NK>
 __device__ __forceinline__ uint32_t window_bits(uint32_t x0, uint32_t x1, uint32_t x2, unsigned k) {
   if (NK == 1) return __funnelshift_r(x0, x1, k);
   return bits_at(x0, x1, x2, k);
+}
+
+template <int NK, int K>
+__device__ __forceinline__ void accumulate_position(uint32_t cls, unsigned q, const uint32_t (&h)[K][NK + 1],
+                                                    const uint32_t (&l)[K][NK + 1], const uint32_t (&o)[K][NK + 1],
+                                                    uint32_t (&bad)[K]) {
+  switch (cls) {
+#define COF_CLASS_CASE(V)                                                                    \
+  case V:                                                                                    \
+    _Pragma("unroll") for (int k = 0; k < K; ++k) bad[k] |= lop3<class_lut(V)>(             \
+        window_bits<NK>(h[k][0], h[k][1], h[k][NK], q), window_bits<NK>(l[k][0], l[k][1], l[k][NK], q), \
+        window_bits<NK>(o[k][0], o[k][1], o[k][NK], q));                                     \
+    break;
+    COF_CLASS_CASE(1) COF_CLASS_CASE(2) COF_CLASS_CASE(3) COF_CLASS_CASE(4) COF_CLASS_CASE(5) COF_CLASS_CASE(6)
+    COF_CLASS_CASE(7) COF_CLASS_CASE(8) COF_CLASS_CASE(9) COF_CLASS_CASE(10) COF_CLASS_CASE(11) COF_CLASS_CASE(12)
+    COF_CLASS_CASE(13) COF_CLASS_CASE(14) COF_CLASS_CASE(15) COF_CLASS_CASE(16) COF_CLASS_CASE(17)
+    COF_CLASS_CASE(18) COF_CLASS_CASE(19) COF_CLASS_CASE(20) COF_CLASS_CASE(21) COF_CLASS_CASE(22)
+    COF_CLASS_CASE(23) COF_CLASS_CASE(24) COF_CLASS_CASE(25) COF_CLASS_CASE(26) COF_CLASS_CASE(27)
+    COF_CLASS_CASE(28) COF_CLASS_CASE(29) COF_CLASS_CASE(30) COF_CLASS_CASE(31)
+#undef COF_CLASS_CASE
+    default:
+      break;
+  }
 }
 
 template <int NK>
@@ -108,24 +155,8 @@ __global__ void __launch_bounds__(kFinderThreads) finder_kernel(
     uint32_t badf[K], badr[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) badf[k] = badr[k] = 0;
-    for (uint32_t j = 0; j < pat.nf; ++j) {
-      const unsigned q = pat.fk[j];
-      const uint32_t mt = pat.fm[j][0], mc = pat.fm[j][1], ma = pat.fm[j][2], mg = pat.fm[j][3], mo = pat.fm[j][4];
-#pragma unroll
-      for (int k = 0; k < K; ++k)
-        badf[k] |= mismatch_word(window_bits<NK>(h[k][0], h[k][1], h[k][NK], q),
-                                 window_bits<NK>(l[k][0], l[k][1], l[k][NK], q),
-                                 window_bits<NK>(o[k][0], o[k][1], o[k][NK], q), mt, mc, ma, mg, mo);
-    }
-    for (uint32_t j = 0; j < pat.nr; ++j) {
-      const unsigned q = pat.rk[j];
-      const uint32_t mt = pat.rm[j][0], mc = pat.rm[j][1], ma = pat.rm[j][2], mg = pat.rm[j][3], mo = pat.rm[j][4];
-#pragma unroll
-      for (int k = 0; k < K; ++k)
-        badr[k] |= mismatch_word(window_bits<NK>(h[k][0], h[k][1], h[k][NK], q),
-                                 window_bits<NK>(l[k][0], l[k][1], l[k][NK], q),
-                                 window_bits<NK>(o[k][0], o[k][1], o[k][NK], q), mt, mc, ma, mg, mo);
-    }
+    for (uint32_t j = 0; j < pat.nf; ++j) accumulate_position<NK, K>(pat.fc[j], pat.fk[j], h, l, o, badf);
+    for (uint32_t j = 0; j < pat.nr; ++j) accumulate_position<NK, K>(pat.rc[j], pat.rk[j], h, l, o, badr);
     uint32_t fwd[K], rev[K], cnt[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -260,11 +291,11 @@ void launch_finder(const GenomeView& g, uint64_t w_begin, uint64_t w_end, const 
   fm.nr = pat.nr;
   for (uint32_t j = 0; j < pat.nf; ++j) {
     fm.fk[j] = pat.fk[j];
-    for (int c = 0; c < 5; ++c) fm.fm[j][c] = 0u - ((pat.fm[j] >> c) & 1u);
+    fm.fc[j] = (uint8_t)(pat.fm[j] & 31u);
   }
   for (uint32_t j = 0; j < pat.nr; ++j) {
     fm.rk[j] = pat.rk[j];
-    for (int c = 0; c < 5; ++c) fm.rm[j][c] = 0u - ((pat.rm[j] >> c) & 1u);
+    fm.rc[j] = (uint8_t)(pat.rm[j] & 31u);
   }
   if (pat.L <= 32)
     finder_kernel<1><<<(unsigned)blocks, kFinderThreads, 0, stream>>>(g.hi, g.lo, g.ot, w_begin, w_end, pos_end, fm,
