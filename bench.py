@@ -760,10 +760,9 @@ def main():
             cpu = {"failed": f"{e}"[:300]}
 
     # Kernels of ours per search (finder and comparer per segment; row
-    # lengths and job bounds once; row writing in one launch per chunk of
-    # max(2^16, ceil(hits / 8)) hits), times the timed searches.
-    chunk_hits = max(1 << 16, -(-nh // 8))
-    row_chunks = -(-nh // chunk_hits) if nh else 0
+    # lengths and job bounds once; row writing in one launch per chunk, as
+    # the profiled search counted them), times the timed searches.
+    row_chunks = int(eng.kernel_stats("rows.chunks")["units"])
     launches = args.steps * int(stats["finder"]["launches"] + stats["comparer"]["launches"] +
                                 (2 + row_chunks) * stats["format"]["launches"])
     batched = None if args.no_batched else run_batched(P, eng, lens, rates, args, capture)

@@ -953,11 +953,16 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
   COF_CUDA(h, cudaMemcpyAsync(h->job_byte0.data(), h->job_bytes.p, (J + 1) * 8, cudaMemcpyDeviceToHost, h->stream));
   uint64_t nrows = 0;
   COF_CUDA(h, cudaMemcpyAsync(&nrows, h->small.p, 8, cudaMemcpyDeviceToHost, h->stream));
-  // Rows returned in one buffer are written in up to kRowChunks chunks of
-  // hits; each chunk's first byte offset comes back with this sync.
+  // Rows returned in one buffer are written in about kRowChunks chunks of
+  // hits, each a whole number of waves of the row writer (a chunk's launch
+  // lasts as long as its last wave); each chunk's first byte offset comes
+  // back with this sync.
   constexpr uint64_t kRowChunks = 8, kMinChunkHits = 1u << 16;
-  const uint64_t chunk_hits = std::max<uint64_t>(kMinChunkHits, (nhits + kRowChunks - 1) / kRowChunks);
+  const uint64_t wave = write_rows_wave_hits(h->sm_count);
+  const uint64_t chunk_hits = std::max<uint64_t>(
+      kMinChunkHits, ((nhits + kRowChunks - 1) / kRowChunks + wave - 1) / wave * wave);
   const uint64_t nck = sink ? 0 : (nhits + chunk_hits - 1) / chunk_hits;
+  if (h->profiling) h->stats["rows.chunks"].units += (double)nck;  // row-writing launches
   std::vector<uint64_t> ck(nck + 1, 0);
   if (nck > 1)
     COF_CUDA(h, cudaMemcpy2DAsync(ck.data(), 8, h->row_offsets.as<uint64_t>(), chunk_hits * 8, 8, nck,

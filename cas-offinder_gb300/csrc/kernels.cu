@@ -23,6 +23,8 @@
 // compare string against the forward genome.
 #include "kernels.cuh"
 
+#include <algorithm>
+
 namespace cof {
 
 namespace {
@@ -622,6 +624,15 @@ void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint6
                         uint64_t* row_bytes, uint32_t* row_count, cudaStream_t stream) {
   if (!n_hits) return;
   row_len_kernel<<<(unsigned)((n_hits + 255) / 256), 256, 0, stream>>>(g, ft, hits, n_hits, row_bytes, row_count);
+}
+
+uint64_t write_rows_wave_hits(int sm_count) {
+  static int per_sm = 0;
+  if (!per_sm && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, write_rows_kernel, kRowThreads, 0) !=
+                      cudaSuccess ||
+                  per_sm < 1))
+    per_sm = 1;
+  return (uint64_t)per_sm * (uint64_t)std::max(sm_count, 1) * kRowThreads;
 }
 
 void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,

@@ -151,6 +151,9 @@ void launch_row_lengths(const GenomeView& g, const FormatTables& ft, const uint6
 // Writes the rows of hits [0, n_hits) at out + (offsets[i] - base) (offsets:
 // exclusive scan of row_bytes; `end` = the byte offset just past the last
 // hit's rows).
+// Hits one wave of write_rows blocks covers on the whole GPU (one thread per
+// hit): launches sized to whole waves leave no SM idle at their tail.
+uint64_t write_rows_wave_hits(int sm_count);
 void launch_write_rows(const GenomeView& g, const FormatTables& ft, const uint64_t* hits, uint64_t n_hits,
                        const uint64_t* offsets, uint64_t base, uint64_t end, char* out, cudaStream_t stream);
 
