@@ -479,13 +479,12 @@ __device__ __forceinline__ void full_count(const uint32_t (&addr)[S], uint32_t (
 }
 
 // Runs one lane program on pair P of the current tile (`addr` points at pair
-// 0 of the current buffer, `tbase` is that buffer's base).  PF >= 0: P is the
-// constant PF; PF < 0: P is a run-time index and only the full count is
-// compiled once per pair index, while the steps, which address their words
+// 0 of the current buffer, `tbase` is that buffer's base).  Only the full
+// count is compiled once per pair index; the steps, which address their words
 // from the pair's base, run from one copy of the code for every pair (one
 // copy per pair made the loop of an eight-warp CTA larger than the
 // instruction cache).
-template <int PF, int S, int ROW, int NK, bool CONC>
+template <int S, int ROW, int NK, bool CONC>
 __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
                                          uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
                                          const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase,
@@ -496,20 +495,15 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
   static_assert(kMaxWarps == 8, "one full_count case per pair index");
   {
     uint32_t ba[NB], bb[NB];
-    if constexpr (PF >= 0) {
-      P = PF;
-      full_count<PF, S, ROW, CONC>(addr, ba, bb);
-    } else {
-      switch (P) {
-        case 0: full_count<0, S, ROW, CONC>(addr, ba, bb); break;
-        case 1: full_count<1, S, ROW, CONC>(addr, ba, bb); break;
-        case 2: full_count<2, S, ROW, CONC>(addr, ba, bb); break;
-        case 3: full_count<3, S, ROW, CONC>(addr, ba, bb); break;
-        case 4: full_count<4, S, ROW, CONC>(addr, ba, bb); break;
-        case 5: full_count<5, S, ROW, CONC>(addr, ba, bb); break;
-        case 6: full_count<6, S, ROW, CONC>(addr, ba, bb); break;
-        default: full_count<7, S, ROW, CONC>(addr, ba, bb); break;
-      }
+    switch (P) {
+      case 0: full_count<0, S, ROW, CONC>(addr, ba, bb); break;
+      case 1: full_count<1, S, ROW, CONC>(addr, ba, bb); break;
+      case 2: full_count<2, S, ROW, CONC>(addr, ba, bb); break;
+      case 3: full_count<3, S, ROW, CONC>(addr, ba, bb); break;
+      case 4: full_count<4, S, ROW, CONC>(addr, ba, bb); break;
+      case 5: full_count<5, S, ROW, CONC>(addr, ba, bb); break;
+      case 6: full_count<6, S, ROW, CONC>(addr, ba, bb); break;
+      default: full_count<7, S, ROW, CONC>(addr, ba, bb); break;
     }
     const uint32_t* pe = ents + P * 64;
     const uint32_t pbase = tbase + P * kPairBytes;  // this pair's class words
@@ -569,23 +563,10 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
     // slot is padding then).
     const uint32_t ns = m - 1, sp = ns / 2;
     uint2 wn = make_uint2(0u, 0u);
-    // One-warp CTAs (PF >= 0) keep their program's step words in shared
-    // memory (copied once per CTA: every tile runs the same program).
-    auto ldstep = [&](const uint2* q) {
-      if constexpr (PF >= 0) {
-        uint2 r;
-        asm volatile("ld.shared.v2.u32 {%0, %1}, [%2];"
-                     : "=r"(r.x), "=r"(r.y)
-                     : "r"((uint32_t)__cvta_generic_to_shared(q)));
-        return r;
-      } else {
-        return __ldg(q);
-      }
-    };
-    if (ns) wn = ldstep(steps);
+    if (ns) wn = __ldg(steps);
     for (uint32_t j = 0; j < sp; ++j) {
       const uint2 w2 = wn;
-      if (2 * (j + 1) < ns) wn = ldstep(steps + (j + 1) * 32);
+      if (2 * (j + 1) < ns) wn = __ldg(steps + (j + 1) * 32);
       uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
       lds64<0>(pbase + (w2.x & 0x7FFFu), a0, a1);
       lds64<0>(pbase + (w2.x >> 16), b0, b1);
@@ -619,35 +600,132 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
   }
 }
 
-// Runs one lane program on pairs 0 .. W-1 of the current tile; ONE: the CTA
-// is one warp (W = 1), so the pair index is the constant 0.
-template <int S, int ROW, int NK, bool CONC, bool ONE>
+// 128-bit shared-memory load (four step addresses).
+__device__ __forceinline__ uint4 lds128(uint32_t addr) {
+  uint4 r;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];" : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w) : "r"(addr));
+  return r;
+}
+
+// One-warp CTAs: the lane's program on the tile's only pair, read from table
+// buffer CUR (a compile-time constant; a buffer is one pair).  Every class
+// word address is a register holding the word's shared address in buffer 0
+// -- the full count's `addr`, the steps' four addresses per pair of steps in
+// `steps` (uint4 per lane, lane stride 32) -- plus the buffer's offset as the
+// load's immediate, so no address arithmetic runs per tile.  `emask` (the
+// lane's word in shared memory) has bit s set when step s ends a variant; it
+// is read only when some candidate passed.
+template <int CUR, int S, int ROW, int NK, bool CONC>
+__device__ __forceinline__ void run_one(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
+                                        uint32_t kadd, uint32_t first_on, uint32_t steps, const uint32_t* emask,
+                                        const uint32_t* __restrict__ gids, uint32_t m, const uint32_t* pe,
+                                        uint64_t seg_pos0, uint64_t* __restrict__ hits,
+                                        unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
+  constexpr int NB = bit_width(S);
+  constexpr uint32_t kBuf = CUR * TableRows<CONC>::kRows * ROW * 8;
+  uint32_t ba[NB], bb[NB];
+  full_count<CUR, S, ROW, CONC>(addr, ba, bb);  // pair CUR of buffer 0 = buffer CUR's pair
+  if (m == 1) {
+    uint32_t ca = 0, cb = 0;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      ca = maj3(ba[i], kmask[i], ca);
+      cb = maj3(bb[i], kmask[i], cb);
+    }
+    const uint32_t hita = ~ca & first_on, hitb = ~cb & first_on;
+    if (__any_sync(kFull, hita | hitb)) {
+      const uint32_t gid = __ldg(gids);
+      emit_hits<NB>(hita, ba, 0u, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NB>(hitb, bb, 0u, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+    }
+    return;
+  }
+  uint32_t pa[NB + 1], pb[NB + 1];
+  add_bias<NB>(ba, kmask, pa);
+  add_bias<NB>(bb, kmask, pb);
+  const uint32_t hita = ~pa[NB] & first_on, hitb = ~pb[NB] & first_on;
+  if (__any_sync(kFull, hita | hitb)) {
+    const uint32_t gid = __ldg(gids);
+    emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+    emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+  }
+  auto emit_step = [&](bool any, uint32_t st) {
+    const uint32_t on = any ? kFull : 0u;
+    const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
+    const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
+    emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+    emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+  };
+  // The same schedule as run_pair: pairs of steps, the next pair's addresses
+  // loaded ahead, one vote per pair, the second step undone to report the
+  // first step's hits.
+  const uint32_t ns = m - 1, sp = ns / 2;
+  uint4 wn = make_uint4(0u, 0u, 0u, 0u);
+  if (ns) wn = lds128(steps);
+  for (uint32_t j = 0; j < sp; ++j) {
+    const uint4 w = wn;
+    if (2 * (j + 1) < ns) wn = lds128(steps + (j + 1) * 32 * 16);
+    uint32_t a0, a1, b0, b1, c0, c1, d0, d1;
+    lds64<kBuf>(w.x, a0, a1);
+    lds64<kBuf>(w.y, b0, b1);
+    lds64<kBuf>(w.z, c0, c1);
+    lds64<kBuf>(w.w, d0, d1);
+    step_update<NB + 1>(pa, a0, b0);
+    step_update<NB + 1>(pb, a1, b1);
+    const uint32_t t0 = pa[NB] & pb[NB];
+    step_update<NB + 1>(pa, c0, d0);
+    step_update<NB + 1>(pb, c1, d1);
+    const uint32_t t1 = pa[NB] & pb[NB];
+    if (__any_sync(kFull, (t0 & t1) != kFull)) {
+      const uint32_t em = *emask >> (2 * j);
+      const bool e0 = (em & 1u) && t0 != kFull;
+      const bool e1 = (em & 2u) && t1 != kFull;
+      if (__any_sync(kFull, e0)) {
+        step_update<NB + 1>(pa, d0, c0);
+        step_update<NB + 1>(pb, d1, c1);
+        emit_step(e0, 2 * j);
+        step_update<NB + 1>(pa, c0, d0);
+        step_update<NB + 1>(pb, c1, d1);
+      }
+      if (__any_sync(kFull, e1)) emit_step(e1, 2 * j + 1);
+    }
+  }
+  if (ns & 1) {
+    uint32_t a0, a1, b0, b1;
+    lds64<kBuf>(wn.x, a0, a1);
+    lds64<kBuf>(wn.y, b0, b1);
+    step_update<NB + 1>(pa, a0, b0);
+    step_update<NB + 1>(pb, a1, b1);
+    const bool any = ((*emask >> (ns - 1)) & 1u) && (pa[NB] & pb[NB]) != kFull;
+    if (__any_sync(kFull, any)) emit_step(any, ns - 1);
+  }
+}
+
+// Runs one lane program on pairs 0 .. W-1 of the current tile (CTAs of
+// several warps; one-warp CTAs use run_one).
+template <int S, int ROW, int NK, bool CONC>
 __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
                                             uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
                                             const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase, unsigned W,
                                             const uint32_t* ents, uint64_t seg_pos0, uint64_t* __restrict__ hits,
                                             unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
-  if constexpr (ONE) {
-    run_pair<0, S, ROW, NK, CONC>(0, addr, kmask, kadd, first_on, steps, gids, m, tbase, ents, seg_pos0, hits,
-                                  hit_count, hit_cap);
-  } else {
 #pragma unroll 1
-    for (unsigned P = 0; P < W; ++P)
-      run_pair<-1, S, ROW, NK, CONC>(P, addr, kmask, kadd, first_on, steps, gids, m, tbase, ents, seg_pos0, hits,
-                                     hit_count, hit_cap);
-  }
+  for (unsigned P = 0; P < W; ++P)
+    run_pair<S, ROW, NK, CONC>(P, addr, kmask, kadd, first_on, steps, gids, m, tbase, ents, seg_pos0, hits, hit_count,
+                               hit_cap);
 }
 
 // Shared memory of a CTA of W warps: two table buffers of W pairs, their
 // candidate entries, the per-thread staging slots and the per-warp window
-// copies (with their meta word); one-warp CTAs add their program's step words
-// (m / 2 pairs per lane).
+// copies (with their meta word); one-warp CTAs add their program's step
+// addresses (m / 2 pairs of steps per lane, four addresses each) and each
+// lane's mask of testing steps.
 constexpr uint32_t kMaxM = 24;  // longest lane program (the host's cost model and autotuner stay within it)
 template <int ROW, int NK, bool CONC>
 __host__ __device__ constexpr size_t bs_smem_bytes(unsigned W, uint32_t m) {
   return 2 * ((size_t)W * TableRows<CONC>::kRows * ROW * sizeof(uint2) + W * 64 * 4) +
          2 * Stage<NK>::kSlots * (32 * W) * 4 + (size_t)W * kCoopWords * 4 +
-         (W == 1 ? (size_t)(m / 2) * 32 * sizeof(uint2) : 0);
+         (W == 1 ? (size_t)(m / 2) * 32 * sizeof(uint4) + 32 * 4 : 0);
 }
 
 template <int S, int ROW, int NK, bool CONC, bool ONE>
@@ -665,7 +743,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   const unsigned tile_n = W * 64;
   const uint32_t kBufWords = W * kPairWords;
   const uint32_t kBufBytes = kBufWords * (uint32_t)sizeof(uint2);
-  extern __shared__ uint2 smem2[];
+  extern __shared__ __align__(16) uint2 smem2[];
   uint2* tables = smem2;                                    // [2 buffers][W pairs][rows][ROW]
   uint32_t* ents_all = (uint32_t*)(smem2 + 2 * kBufWords);  // [2 buffers][W pairs][64]
   const uint32_t table_base = (uint32_t)__cvta_generic_to_shared(tables);
@@ -702,13 +780,24 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   uint32_t addr[S], kmask[NB], kadd = 0, first_on = 0;
   if (resident && warp < chunks)
     load_program<S>(prog + (size_t)warp * words * 32 + lane, table_base, addr, kmask, kadd, first_on);
-  // One-warp CTAs: the program's step words, lane-minor as in `prog` (each
-  // lane reads back only its own words).
-  uint2* steps_sh = (uint2*)(ents_all + 2 * W * 64 + 2 * Stage<NK>::kSlots * kS + W * kCoopWords);
+  // One-warp CTAs: the program's steps as shared addresses in table buffer 0
+  // (added word, removed word, for both steps of a pair), lane-minor, then
+  // each lane's mask of the steps that end a variant.  Each lane reads back
+  // only its own words.
+  uint4* steps_sh = (uint4*)(ents_all + 2 * W * 64 + 2 * Stage<NK>::kSlots * kS + W * kCoopWords);
+  uint32_t* emask_sh = (uint32_t*)(steps_sh + (m / 2) * 32);
   if (ONE && chunks == 1) {
     const uint2* src = (const uint2*)(prog + (1 + S / 2) * 32) + lane;
-    for (uint32_t j = 0; j < m / 2; ++j) steps_sh[j * 32 + lane] = __ldg(src + j * 32);
+    uint32_t em = 0;
+    for (uint32_t j = 0; j < m / 2; ++j) {
+      const uint2 w = __ldg(src + j * 32);
+      steps_sh[j * 32 + lane] = make_uint4(table_base + (w.x & 0x7FFFu), table_base + (w.x >> 16),
+                                           table_base + (w.y & 0x7FFFu), table_base + (w.y >> 16));
+      em |= ((w.x >> 15) & 1u) << (2 * j) | ((w.y >> 15) & 1u) << (2 * j + 1);
+    }
+    emask_sh[lane] = em;
   }
+  const uint32_t steps_addr = (uint32_t)__cvta_generic_to_shared(steps_sh + lane);
   // Entries: e* of the tile being staged, n* of the tile after it.
   {
     uint32_t* cw = coop_words();
@@ -742,14 +831,23 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     nb = load_entry(queue, tnn * tile_n + cb, n);
     const uint32_t* ents = ents_all + cur * (W * 64);
     const uint32_t tbase = table_base + cur * kBufBytes;
-    for (uint32_t c = warp; c < chunks; c += W) {
-      const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
-      if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
-      run_program<S, ROW, NK, CONC, ONE>(addr, kmask, kadd, first_on,
-                                   ONE ? (const uint2*)steps_sh + lane
-                                       : (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
-                                   pgid + (size_t)c * m * 32 + lane, m, tbase, W, ents, seg_pos0, hits, hit_count,
-                                   hit_cap);
+    if constexpr (ONE) {
+      // chunks == 1 (launch_bs): the program is resident; the buffer picks
+      // the instance.
+      if (cur)
+        run_one<1, S, ROW, NK, CONC>(addr, kmask, kadd, first_on, steps_addr, emask_sh + lane, pgid + lane, m,
+                                     ents, seg_pos0, hits, hit_count, hit_cap);
+      else
+        run_one<0, S, ROW, NK, CONC>(addr, kmask, kadd, first_on, steps_addr, emask_sh + lane, pgid + lane, m,
+                                     ents, seg_pos0, hits, hit_count, hit_cap);
+    } else {
+      for (uint32_t c = warp; c < chunks; c += W) {
+        const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
+        if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
+        run_program<S, ROW, NK, CONC>(addr, kmask, kadd, first_on, (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
+                                      pgid + (size_t)c * m * 32 + lane, m, tbase, W, ents, seg_pos0, hits, hit_count,
+                                      hit_cap);
+      }
     }
     cp_async_wait_all();
     if (tn < ntiles) {
@@ -761,7 +859,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
     }
     if (threadIdx.x == 0) claimed[par ^ 1] = claim;
     __syncthreads();
-    if (resident) {
+    if (!ONE && resident) {  // one-warp CTAs address buffer 1 by immediates
       const uint32_t d = cur ? 0u - kBufBytes : kBufBytes;
 #pragma unroll
       for (int s = 0; s < S; ++s) addr[s] += d;
