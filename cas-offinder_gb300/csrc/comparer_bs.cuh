@@ -388,7 +388,9 @@ __device__ __forceinline__ void lds64(uint32_t addr, uint32_t& x, uint32_t& y) {
 // A lane program's first variant (program layout in kernels.cuh): the shared
 // addresses of its slots' class words (pair 0 of the buffer at `tbase`), the
 // carry masks of its threshold bias and whether it is a real variant.
-template <int S>
+// NARROW: the bias is lowered by 2^(NB-1) so that NB count planes suffice
+// (the top plane, 2^(NB-1), is then set exactly where count > threshold).
+template <int S, bool NARROW>
 __device__ __forceinline__ void load_program(const uint32_t* __restrict__ pr, uint32_t tbase, uint32_t (&addr)[S],
                                              uint32_t (&kmask)[bit_width(S)], uint32_t& kadd, uint32_t& first_on) {
   constexpr int NB = bit_width(S);
@@ -400,6 +402,7 @@ __device__ __forceinline__ void load_program(const uint32_t* __restrict__ pr, ui
     addr[s + 1] = tbase + (pk >> 16);
   }
   kadd = h & 0xFFu;
+  if (NARROW) kadd -= 1u << (NB - 1);  // the bias for NB planes (the host checked kadd >= 2^(NB-1))
 #pragma unroll
   for (int i = 0; i < NB; ++i) kmask[i] = 0u - ((kadd >> i) & 1u);
   first_on = (h & 0x100u) ? kFull : 0u;
@@ -427,16 +430,18 @@ __device__ __forceinline__ void emit_hits(uint32_t hm, const uint32_t (&bits)[NP
 }
 
 // Count planes + a per-lane constant (bit i of it as the all-ones / all-zeros
-// word kmask[i]): NB + 1 planes out.
-template <int NB>
-__device__ __forceinline__ void add_bias(const uint32_t (&b)[NB], const uint32_t (&kmask)[NB], uint32_t (&p)[NB + 1]) {
+// word kmask[i]): NP planes out, NB + 1 (the carry out of the top count plane
+// kept) or NB (the sum taken modulo 2^NB, exact when it stays below 2^NB).
+template <int NB, int NP>
+__device__ __forceinline__ void add_bias(const uint32_t (&b)[NB], const uint32_t (&kmask)[NB], uint32_t (&p)[NP]) {
+  static_assert(NP == NB || NP == NB + 1, "NB or NB + 1 planes");
   uint32_t c = 0;
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     p[i] = xor3(b[i], kmask[i], c);
-    c = maj3(b[i], kmask[i], c);
+    if (i + 1 < NP) c = maj3(b[i], kmask[i], c);
   }
-  p[NB] = c;
+  if constexpr (NP > NB) p[NP - 1] = c;
 }
 
 // One update step of bit-sliced counters: + a - b (one bit each per
@@ -484,13 +489,14 @@ __device__ __forceinline__ void full_count(const uint32_t (&addr)[S], uint32_t (
 // from the pair's base, run from one copy of the code for every pair (one
 // copy per pair made the loop of an eight-warp CTA larger than the
 // instruction cache).
-template <int S, int ROW, int NK, bool CONC>
+template <int S, int ROW, int NK, bool CONC, bool NARROW>
 __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
                                          uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
                                          const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase,
                                          const uint32_t* ents, uint64_t seg_pos0, uint64_t* __restrict__ hits,
                                          unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
   constexpr int NB = bit_width(S);
+  constexpr int NP = NARROW ? NB : NB + 1;  // count planes
   constexpr uint32_t kPairBytes = TableRows<CONC>::kRows * ROW * 8;
   static_assert(kMaxWarps == 8, "one full_count case per pair index");
   {
@@ -523,16 +529,16 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
       }
       return;
     }
-    // Biased counters (count + bias in NB + 1 planes): a variant passes
+    // Biased counters (count + bias in NP planes): a variant passes
     // while the top plane is clear.
-    uint32_t pa[NB + 1], pb[NB + 1];
-    add_bias<NB>(ba, kmask, pa);
-    add_bias<NB>(bb, kmask, pb);
-    const uint32_t hita = ~pa[NB] & first_on, hitb = ~pb[NB] & first_on;
+    uint32_t pa[NP], pb[NP];
+    add_bias<NB, NP>(ba, kmask, pa);
+    add_bias<NB, NP>(bb, kmask, pb);
+    const uint32_t hita = ~pa[NP - 1] & first_on, hitb = ~pb[NP - 1] & first_on;
     if (__any_sync(kFull, hita | hitb)) {
       const uint32_t gid = __ldg(gids);
-      emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-      emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NP>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NP>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
     }
     // Step st tests its variant when it emits (bit 15); the variant's id is
     // entry st + 1 of the lane's id list.  A candidate passes while the top
@@ -540,15 +546,15 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
     // candidate of the pair has that plane clear.
     auto emit_step = [&](bool any, uint32_t st) {
       const uint32_t on = any ? kFull : 0u;
-      const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
+      const uint32_t ha = ~pa[NP - 1] & on, hb = ~pb[NP - 1] & on;
       const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
-      emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-      emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NP>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+      emit_hits<NP>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
     };
     auto step = [&](uint32_t w, uint32_t st, uint32_t a0, uint32_t a1, uint32_t b0, uint32_t b1) {
-      step_update<NB + 1>(pa, a0, b0);
-      step_update<NB + 1>(pb, a1, b1);
-      const bool any = (w & 0x8000u) && (pa[NB] & pb[NB]) != kFull;
+      step_update<NP>(pa, a0, b0);
+      step_update<NP>(pb, a1, b1);
+      const bool any = (w & 0x8000u) && (pa[NP - 1] & pb[NP - 1]) != kFull;
       if (__any_sync(kFull, any)) emit_step(any, st);
     };
     // Steps come in pairs (one 64-bit load), the next pair loaded ahead.
@@ -572,21 +578,21 @@ __device__ __forceinline__ void run_pair(unsigned P, const uint32_t (&addr)[S], 
       lds64<0>(pbase + (w2.x >> 16), b0, b1);
       lds64<0>(pbase + (w2.y & 0x7FFFu), c0, c1);
       lds64<0>(pbase + (w2.y >> 16), d0, d1);
-      step_update<NB + 1>(pa, a0, b0);
-      step_update<NB + 1>(pb, a1, b1);
-      const uint32_t t0 = pa[NB] & pb[NB];
-      step_update<NB + 1>(pa, c0, d0);
-      step_update<NB + 1>(pb, c1, d1);
-      const uint32_t t1 = pa[NB] & pb[NB];
+      step_update<NP>(pa, a0, b0);
+      step_update<NP>(pb, a1, b1);
+      const uint32_t t0 = pa[NP - 1] & pb[NP - 1];
+      step_update<NP>(pa, c0, d0);
+      step_update<NP>(pb, c1, d1);
+      const uint32_t t1 = pa[NP - 1] & pb[NP - 1];
       if (__any_sync(kFull, (t0 & t1) != kFull)) {
         const bool e0 = (w2.x & 0x8000u) && t0 != kFull;
         const bool e1 = (w2.y & 0x8000u) && t1 != kFull;
         if (__any_sync(kFull, e0)) {
-          step_update<NB + 1>(pa, d0, c0);
-          step_update<NB + 1>(pb, d1, c1);
+          step_update<NP>(pa, d0, c0);
+          step_update<NP>(pb, d1, c1);
           emit_step(e0, 2 * j);
-          step_update<NB + 1>(pa, c0, d0);
-          step_update<NB + 1>(pb, c1, d1);
+          step_update<NP>(pa, c0, d0);
+          step_update<NP>(pb, c1, d1);
         }
         if (__any_sync(kFull, e1)) emit_step(e1, 2 * j + 1);
       }
@@ -615,13 +621,14 @@ __device__ __forceinline__ uint4 lds128(uint32_t addr) {
 // load's immediate, so no address arithmetic runs per tile.  `emask` (the
 // lane's word in shared memory) has bit s set when step s ends a variant; it
 // is read only when some candidate passed.
-template <int CUR, int S, int ROW, int NK, bool CONC>
+template <int CUR, int S, int ROW, int NK, bool CONC, bool NARROW>
 __device__ __forceinline__ void run_one(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
                                         uint32_t kadd, uint32_t first_on, uint32_t steps, const uint32_t* emask,
                                         const uint32_t* __restrict__ gids, uint32_t m, const uint32_t* pe,
                                         uint64_t seg_pos0, uint64_t* __restrict__ hits,
                                         unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
   constexpr int NB = bit_width(S);
+  constexpr int NP = NARROW ? NB : NB + 1;  // count planes
   constexpr uint32_t kBuf = CUR * TableRows<CONC>::kRows * ROW * 8;
   uint32_t ba[NB], bb[NB];
   full_count<CUR, S, ROW, CONC>(addr, ba, bb);  // pair CUR of buffer 0 = buffer CUR's pair
@@ -640,21 +647,21 @@ __device__ __forceinline__ void run_one(const uint32_t (&addr)[S], const uint32_
     }
     return;
   }
-  uint32_t pa[NB + 1], pb[NB + 1];
-  add_bias<NB>(ba, kmask, pa);
-  add_bias<NB>(bb, kmask, pb);
-  const uint32_t hita = ~pa[NB] & first_on, hitb = ~pb[NB] & first_on;
+  uint32_t pa[NP], pb[NP];
+  add_bias<NB, NP>(ba, kmask, pa);
+  add_bias<NB, NP>(bb, kmask, pb);
+  const uint32_t hita = ~pa[NP - 1] & first_on, hitb = ~pb[NP - 1] & first_on;
   if (__any_sync(kFull, hita | hitb)) {
     const uint32_t gid = __ldg(gids);
-    emit_hits<NB + 1>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-    emit_hits<NB + 1>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+    emit_hits<NP>(hita, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+    emit_hits<NP>(hitb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
   }
   auto emit_step = [&](bool any, uint32_t st) {
     const uint32_t on = any ? kFull : 0u;
-    const uint32_t ha = ~pa[NB] & on, hb = ~pb[NB] & on;
+    const uint32_t ha = ~pa[NP - 1] & on, hb = ~pb[NP - 1] & on;
     const uint32_t gid = any ? __ldg(gids + (st + 1) * 32) : 0u;
-    emit_hits<NB + 1>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
-    emit_hits<NB + 1>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
+    emit_hits<NP>(ha, pa, kadd, pe, gid, seg_pos0, hits, hit_count, hit_cap);
+    emit_hits<NP>(hb, pb, kadd, pe + 32, gid, seg_pos0, hits, hit_count, hit_cap);
   };
   // The same schedule as run_pair: pairs of steps, the next pair's addresses
   // loaded ahead, one vote per pair, the second step undone to report the
@@ -670,22 +677,22 @@ __device__ __forceinline__ void run_one(const uint32_t (&addr)[S], const uint32_
     lds64<kBuf>(w.y, b0, b1);
     lds64<kBuf>(w.z, c0, c1);
     lds64<kBuf>(w.w, d0, d1);
-    step_update<NB + 1>(pa, a0, b0);
-    step_update<NB + 1>(pb, a1, b1);
-    const uint32_t t0 = pa[NB] & pb[NB];
-    step_update<NB + 1>(pa, c0, d0);
-    step_update<NB + 1>(pb, c1, d1);
-    const uint32_t t1 = pa[NB] & pb[NB];
+    step_update<NP>(pa, a0, b0);
+    step_update<NP>(pb, a1, b1);
+    const uint32_t t0 = pa[NP - 1] & pb[NP - 1];
+    step_update<NP>(pa, c0, d0);
+    step_update<NP>(pb, c1, d1);
+    const uint32_t t1 = pa[NP - 1] & pb[NP - 1];
     if (__any_sync(kFull, (t0 & t1) != kFull)) {
       const uint32_t em = *emask >> (2 * j);
       const bool e0 = (em & 1u) && t0 != kFull;
       const bool e1 = (em & 2u) && t1 != kFull;
       if (__any_sync(kFull, e0)) {
-        step_update<NB + 1>(pa, d0, c0);
-        step_update<NB + 1>(pb, d1, c1);
+        step_update<NP>(pa, d0, c0);
+        step_update<NP>(pb, d1, c1);
         emit_step(e0, 2 * j);
-        step_update<NB + 1>(pa, c0, d0);
-        step_update<NB + 1>(pb, c1, d1);
+        step_update<NP>(pa, c0, d0);
+        step_update<NP>(pb, c1, d1);
       }
       if (__any_sync(kFull, e1)) emit_step(e1, 2 * j + 1);
     }
@@ -694,16 +701,16 @@ __device__ __forceinline__ void run_one(const uint32_t (&addr)[S], const uint32_
     uint32_t a0, a1, b0, b1;
     lds64<kBuf>(wn.x, a0, a1);
     lds64<kBuf>(wn.y, b0, b1);
-    step_update<NB + 1>(pa, a0, b0);
-    step_update<NB + 1>(pb, a1, b1);
-    const bool any = ((*emask >> (ns - 1)) & 1u) && (pa[NB] & pb[NB]) != kFull;
+    step_update<NP>(pa, a0, b0);
+    step_update<NP>(pb, a1, b1);
+    const bool any = ((*emask >> (ns - 1)) & 1u) && (pa[NP - 1] & pb[NP - 1]) != kFull;
     if (__any_sync(kFull, any)) emit_step(any, ns - 1);
   }
 }
 
 // Runs one lane program on pairs 0 .. W-1 of the current tile (CTAs of
 // several warps; one-warp CTAs use run_one).
-template <int S, int ROW, int NK, bool CONC>
+template <int S, int ROW, int NK, bool CONC, bool NARROW>
 __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uint32_t (&kmask)[bit_width(S)],
                                             uint32_t kadd, uint32_t first_on, const uint2* __restrict__ steps,
                                             const uint32_t* __restrict__ gids, uint32_t m, uint32_t tbase, unsigned W,
@@ -711,7 +718,7 @@ __device__ __forceinline__ void run_program(const uint32_t (&addr)[S], const uin
                                             unsigned long long* __restrict__ hit_count, uint64_t hit_cap) {
 #pragma unroll 1
   for (unsigned P = 0; P < W; ++P)
-    run_pair<S, ROW, NK, CONC>(P, addr, kmask, kadd, first_on, steps, gids, m, tbase, ents, seg_pos0, hits, hit_count,
+    run_pair<S, ROW, NK, CONC, NARROW>(P, addr, kmask, kadd, first_on, steps, gids, m, tbase, ents, seg_pos0, hits, hit_count,
                                hit_cap);
 }
 
@@ -728,7 +735,7 @@ __host__ __device__ constexpr size_t bs_smem_bytes(unsigned W, uint32_t m) {
          (W == 1 ? (size_t)(m / 2) * 32 * sizeof(uint4) + 32 * 4 : 0);
 }
 
-template <int S, int ROW, int NK, bool CONC, bool ONE>
+template <int S, int ROW, int NK, bool CONC, bool ONE, bool NARROW>
 __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::value)) comparer_bs_kernel(
     const uint32_t* __restrict__ hi, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ ot,
     const uint32_t* __restrict__ queue, const uint32_t* __restrict__ qcount, uint64_t seg_pos0,
@@ -779,7 +786,7 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
   const bool resident = chunks <= W;
   uint32_t addr[S], kmask[NB], kadd = 0, first_on = 0;
   if (resident && warp < chunks)
-    load_program<S>(prog + (size_t)warp * words * 32 + lane, table_base, addr, kmask, kadd, first_on);
+    load_program<S, NARROW>(prog + (size_t)warp * words * 32 + lane, table_base, addr, kmask, kadd, first_on);
   // One-warp CTAs: the program's steps as shared addresses in table buffer 0
   // (added word, removed word, for both steps of a pair), lane-minor, then
   // each lane's mask of the steps that end a variant.  Each lane reads back
@@ -835,16 +842,16 @@ __global__ void __launch_bounds__(32 * kMaxWarps) __maxnreg__((MaxRegs<S, NK>::v
       // chunks == 1 (launch_bs): the program is resident; the buffer picks
       // the instance.
       if (cur)
-        run_one<1, S, ROW, NK, CONC>(addr, kmask, kadd, first_on, steps_addr, emask_sh + lane, pgid + lane, m,
+        run_one<1, S, ROW, NK, CONC, NARROW>(addr, kmask, kadd, first_on, steps_addr, emask_sh + lane, pgid + lane, m,
                                      ents, seg_pos0, hits, hit_count, hit_cap);
       else
-        run_one<0, S, ROW, NK, CONC>(addr, kmask, kadd, first_on, steps_addr, emask_sh + lane, pgid + lane, m,
+        run_one<0, S, ROW, NK, CONC, NARROW>(addr, kmask, kadd, first_on, steps_addr, emask_sh + lane, pgid + lane, m,
                                      ents, seg_pos0, hits, hit_count, hit_cap);
     } else {
       for (uint32_t c = warp; c < chunks; c += W) {
         const uint32_t* pr = prog + (size_t)c * words * 32 + lane;
-        if (!resident) load_program<S>(pr, tbase, addr, kmask, kadd, first_on);
-        run_program<S, ROW, NK, CONC>(addr, kmask, kadd, first_on, (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
+        if (!resident) load_program<S, NARROW>(pr, tbase, addr, kmask, kadd, first_on);
+        run_program<S, ROW, NK, CONC, NARROW>(addr, kmask, kadd, first_on, (const uint2*)(pr - lane + (1 + S / 2) * 32) + lane,
                                       pgid + (size_t)c * m * 32 + lane, m, tbase, W, ents, seg_pos0, hits, hit_count,
                                       hit_cap);
       }
@@ -888,7 +895,7 @@ inline unsigned bs_warps(uint32_t chunks) {
 
 template <int S, int ROW, int NK, bool CONC>
 bool launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-               const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L,
+               const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, bool narrow, uint32_t L,
                uint32_t* tile_ctr, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
                cudaStream_t stream) {
   if (m > kMaxM) return false;  // the shared step words are sized for kMaxM
@@ -898,8 +905,14 @@ bool launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcoun
   if (warps == 1 && chunks != 1) return false;
   const int threads = 32 * (int)warps;
   const size_t smem = bs_smem_bytes<ROW, NK, CONC>(warps, m);
-  // One-warp CTAs (one chunk) get the instance with the pair index constant.
-  auto kernel = warps == 1 ? comparer_bs_kernel<S, ROW, NK, CONC, true> : comparer_bs_kernel<S, ROW, NK, CONC, false>;
+  // One-warp CTAs (one chunk) get the instance with the pair index constant;
+  // programs of one variant (m = 1) test the carry of NB planes and never
+  // take the narrow counters.
+  const bool nar = narrow && m > 1;
+  auto kernel = warps == 1 ? (nar ? comparer_bs_kernel<S, ROW, NK, CONC, true, true>
+                                  : comparer_bs_kernel<S, ROW, NK, CONC, true, false>)
+                           : (nar ? comparer_bs_kernel<S, ROW, NK, CONC, false, true>
+                                  : comparer_bs_kernel<S, ROW, NK, CONC, false, false>);
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)std::max(bs_smem_bytes<ROW, NK, CONC>(kMaxWarps, 0), bs_smem_bytes<ROW, NK, CONC>(1, kMaxM)));
   int per_sm = 0;
@@ -914,12 +927,12 @@ bool launch_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcoun
 
 template <int ROW, int NK, bool CONC>
 bool dispatch_s(int slots, const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
-                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, uint32_t L,
+                const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, bool narrow, uint32_t L,
                 uint32_t* tile_ctr, uint64_t* hits, unsigned long long* hit_count, uint64_t hit_cap, int sm_count,
                 cudaStream_t stream) {
 #define COF_BS_CASE(SV)                                                                                  \
   case SV:                                                                                               \
-    return launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, prog, pgid, chunks, m, L, tile_ctr, hits, \
+    return launch_bs<SV, ROW, NK, CONC>(g, queue, qcount, seg_pos0, prog, pgid, chunks, m, narrow, L, tile_ctr, hits, \
                                         hit_count, hit_cap, sm_count, stream);
   switch (slots) {
     COF_BS_CASE(8)

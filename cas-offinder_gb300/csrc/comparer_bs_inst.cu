@@ -9,4 +9,4 @@
 
 template bool cof::bs::dispatch_s<COF_BS_ROW, COF_BS_NK, (COF_BS_CONC != 0)>(
     int, const cof::GenomeView&, const uint32_t*, const uint32_t*, uint64_t, const uint32_t*, const uint32_t*, uint32_t,
-    uint32_t, uint32_t, uint32_t*, uint64_t*, unsigned long long*, uint64_t, int, cudaStream_t);
+    uint32_t, bool, uint32_t, uint32_t*, uint64_t*, unsigned long long*, uint64_t, int, cudaStream_t);

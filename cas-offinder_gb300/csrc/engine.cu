@@ -379,6 +379,7 @@ void build_group_host(bool force_popc, PatternGroup& g, const std::vector<const 
   int maxpos = 0;
   g.nonN_sum = 0;
   g.concrete_only = true;
+  std::vector<uint32_t> thr(V), npos(V);
   for (size_t i = 0; i < V; ++i) {
     const Variant& var = *vars[i];
     if (g.nw == 1) fill_mask<1>(((VariantMask<1>*)gh.masks.data())[i], var.key, var.threshold, g.gids[i]);
@@ -391,8 +392,11 @@ void build_group_host(bool force_popc, PatternGroup& g, const std::vector<const 
       g.nonN_sum += ch != 'N';
     }
     maxpos = std::max(maxpos, c);
+    thr[i] = var.threshold;
+    npos[i] = (uint32_t)c;
   }
   g.bs_slots = force_popc ? 0 : bs_slots_for(maxpos);
+  g.bs_narrow = g.bs_slots && bs_narrow_ok(g.bs_slots, thr.data(), npos.data(), V);
   gh.prog.clear();
   gh.pgid.clear();
   g.bs_chunks = 0;
@@ -511,7 +515,7 @@ cof_status autotune_group(cof_handle* h, PatternGroup& g, const std::vector<cons
         COF_CUDA(h, cudaMemsetAsync(qc + 1, 0, 4, h->stream));
         COF_CUDA(h, cudaEventRecord(ev[0], h->stream));
         if (!launch_comparer_bs(gv, q, qc, w0 * 32, dprog.as<uint32_t>(), dpgid.as<uint32_t>(), chunks, mm,
-                                g.bs_slots, g.L, g.concrete_only, qc + 1, h->hits.as<uint64_t>(),
+                                g.bs_slots, g.bs_narrow, g.L, g.concrete_only, qc + 1, h->hits.as<uint64_t>(),
                                 h->hit_count.as<unsigned long long>(), cap, h->sm_count, h->stream)) {
           declined = true;
           return COF_OK;
@@ -713,7 +717,7 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       const uint32_t V = (uint32_t)g.gids.size();
       if (!g.bs_slots ||
           !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_prog.as<uint32_t>(), g.bs_pgid.as<uint32_t>(),
-                              g.bs_chunks, g.bs_m, g.bs_slots, g.L, g.concrete_only, qc + nq,
+                              g.bs_chunks, g.bs_m, g.bs_slots, g.bs_narrow, g.L, g.concrete_only, qc + nq,
                               h->hits.as<uint64_t>(), h->hit_count.as<unsigned long long>(), hit_cap, h->sm_count,
                               h->stream))
         launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, h->hits.as<uint64_t>(),
@@ -756,7 +760,7 @@ std::string pass_graph_key(const cof_handle* h, uint64_t cap) {
   put64(cap);
   put64((uint64_t)h->sm_count);
   for (const PatternGroup& g : h->groups) {
-    for (uint64_t v : {(uint64_t)g.L, (uint64_t)g.nw, (uint64_t)g.bs_slots, (uint64_t)g.bs_chunks, (uint64_t)g.bs_m,
+    for (uint64_t v : {(uint64_t)g.L, (uint64_t)g.nw, (uint64_t)g.bs_slots, (uint64_t)g.bs_narrow, (uint64_t)g.bs_chunks, (uint64_t)g.bs_m,
                        (uint64_t)g.concrete_only, (uint64_t)g.gids.size()})
       put64(v);
     for (const void* p : {g.bs_prog.p, g.bs_pgid.p, g.vmask.p}) put64((uint64_t)p);
@@ -898,7 +902,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
         h->stats["comparer.tests"].units += (double)qc[idx] * (double)g.gids.size();
         if (g.bs_slots && g.bs_chunks)  // lane LOP3 ops the bit-sliced count issues (op model)
           h->stats["comparer.lop3"].units +=
-              (double)((qc[idx] + 63) / 64) * 32.0 * g.bs_chunks * bs_lane_lop3(g.bs_slots, g.bs_m);
+              (double)((qc[idx] + 63) / 64) * 32.0 * g.bs_chunks * bs_lane_lop3(g.bs_slots, g.bs_m, g.bs_narrow);
         h->stats["finder.candidates"].units += (double)qc[idx];  // queue entries the finder wrote
       }
     collect(h, evs);
@@ -1569,7 +1573,8 @@ cof_status cof_schedule_text(cof_handle* h, const char** text, size_t* len) {
     snprintf(line, sizeof line, "%s variants=%zu slots=%d", g.pattern.c_str(), g.gids.size(), g.bs_slots);
     t += line;
     if (g.bs_slots) {
-      snprintf(line, sizeof line, " m=%u chunks=%u", g.bs_m, g.bs_chunks);
+      snprintf(line, sizeof line, " m=%u chunks=%u planes=%s", g.bs_m, g.bs_chunks,
+               g.bs_narrow && g.bs_m > 1 ? "NB" : "NB+1");
       t += line;
       if (!g.bs_tuned.empty()) {
         t += " tuned:";

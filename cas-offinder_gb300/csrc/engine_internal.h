@@ -115,6 +115,7 @@ struct PatternGroup {
   int nw = 1;                  // 32-bit words per window (popcount comparer)
   int bs_slots = 0;            // bit-sliced slot count, 0 = popcount comparer
   bool concrete_only = true;   // no variant uses a degenerate IUPAC code
+  bool bs_narrow = false;      // bit-sliced counts fit bit_width(bs_slots) planes (bs_narrow_ok)
   std::vector<uint32_t> gids;  // global variant ids, ascending
   double nonN_sum = 0;         // sum of non-N positions over the group's variants
   // Bit-sliced comparer programs (layout in kernels.cuh): bs_chunks chunks of

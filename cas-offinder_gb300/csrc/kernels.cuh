@@ -129,18 +129,27 @@ void launch_comparer(const GenomeView& g, const uint32_t* queue, const uint32_t*
 // launch_comparer; also when seg_pos0 is not a multiple of 32: the kernels
 // address windows from the segment's first plane word).  `concrete_only`: no
 // variant uses a degenerate IUPAC code (only the four concrete-base class rows
-// are built).  `tile_ctr`: a u32 the caller zeroes before each launch (CTAs
-// claim tiles from it).
+// are built).  `narrow` (see bs_narrow_ok): every variant's count fits NB =
+// bit_width(slots) planes under the lowered bias, so the update steps carry
+// NB planes instead of NB + 1.  `tile_ctr`: a u32 the caller zeroes before
+// each launch (CTAs claim tiles from it).
 bool launch_comparer_bs(const GenomeView& g, const uint32_t* queue, const uint32_t* qcount, uint64_t seg_pos0,
                         const uint32_t* prog, const uint32_t* pgid, uint32_t chunks, uint32_t m, int slots,
-                        uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,
+                        bool narrow, uint32_t L, bool concrete_only, uint32_t* tile_ctr, uint64_t* hits,
                         unsigned long long* hit_count, uint64_t hit_cap, int sm_count, cudaStream_t stream);
+// Whether lane programs with `slots` class words may count in NB =
+// bit_width(slots) planes: with the bias 2^(NB-1) - 1 - t the top plane
+// (2^(NB-1)) is set exactly where count > t, and the sum stays below 2^NB,
+// when every variant's threshold t < 2^(NB-1) and its positions that can
+// mismatch c satisfy c - t <= 2^(NB-1).  (Update steps are exact modulo
+// 2^NB, so only the tested variants' counts must fit.)
+bool bs_narrow_ok(int slots, const uint32_t* thresholds, const uint32_t* positions, size_t n);
 // Op model of the count phase: LOP3-class logic instructions one lane issues
 // per pair of 32-candidate groups for a lane program of m variants with
 // `slots` class words (full count, bias, m - 1 update steps, hit votes; hit
 // emission and the table build aside).  Every lane of a launch runs the same
 // count, so a launch issues ceil(candidates / 64) * 32 * chunks times this.
-double bs_lane_lop3(int slots, uint32_t m);
+double bs_lane_lop3(int slots, uint32_t m, bool narrow);
 int bs_slots_for(int max_positions);  // 0 when more than 32 positions can mismatch
 int bs_row_for(uint32_t L);           // words per class row of the shared table
 uint32_t bs_class_of(unsigned char p);  // class row of a pattern byte (0: never mismatches)

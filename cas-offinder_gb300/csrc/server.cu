@@ -276,7 +276,7 @@ cof_status run_step(cof_server* s, uint64_t k) {
       const uint32_t V = (uint32_t)g.gids.size();
       if (!g.bs_slots ||
           !launch_comparer_bs(gv, q, qc, w0 * 32, g.bs_prog.as<uint32_t>(), g.bs_pgid.as<uint32_t>(),
-                              g.bs_chunks, g.bs_m, g.bs_slots, g.L, g.concrete_only, qc + nq,
+                              g.bs_chunks, g.bs_m, g.bs_slots, g.bs_narrow, g.L, g.concrete_only, qc + nq,
                               s->step_hits.as<uint64_t>(), s->step_count.as<unsigned long long>(), cap, h->sm_count,
                               h->stream))
         launch_comparer(gv, q, qc, w0 * 32, g.vmask.p, V, g.nw, g.L, s->step_hits.as<uint64_t>(),

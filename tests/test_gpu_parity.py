@@ -62,6 +62,11 @@ RANDOM_CASES = [
     dict(seed=211, lens=[80000, 20000], pattern="N" * 45 + "NGG", dna=1, rna=1, mm=5, per_guide=40,
          guides=["N" * 18 + "".join(random.Random(211 + i).choice("ACGT") for _ in range(27)) + "NNN"
                  for i in range(3)]),
+    # Thresholds at the edges of the bit-sliced comparer's narrow counters
+    # (20 positions, 5 count planes: thresholds 4 and 15 fit them, 3 and 16
+    # take the sixth plane).
+    dict(seed=212, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[4, 15], n_guides=2, per_guide=20),
+    dict(seed=213, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[3, 16], n_guides=2, per_guide=20),
 ]
 
 
