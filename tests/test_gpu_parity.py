@@ -63,10 +63,17 @@ RANDOM_CASES = [
          guides=["N" * 18 + "".join(random.Random(211 + i).choice("ACGT") for _ in range(27)) + "NNN"
                  for i in range(3)]),
     # Thresholds at the edges of the bit-sliced comparer's narrow counters
-    # (20 positions, 5 count planes: thresholds 4 and 15 fit them, 3 and 16
-    # take the sixth plane).
-    dict(seed=212, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[4, 15], n_guides=2, per_guide=20),
-    dict(seed=213, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[3, 16], n_guides=2, per_guide=20),
+    # (20-nt guides, 20 slots, 5 count planes: thresholds 4 and 15 fit them,
+    # 3 and 16 take the sixth plane).
+    dict(seed=212, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[4, 15], per_guide=20,
+         guides=["".join(random.Random(212 + i).choice("ACGT") for _ in range(20)) + "NNN" for i in range(2)]),
+    dict(seed=213, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[3, 16], per_guide=20,
+         guides=["".join(random.Random(213 + i).choice("ACGT") for _ in range(20)) + "NNN" for i in range(2)]),
+    # More lane programs than one 32-lane chunk (~700 variants, 3 chunks):
+    # CTAs of several warps, with narrow counters (21 positions, mm 5) and
+    # without (mm 3 among them).
+    dict(seed=214, lens=[100000], pattern="N" * 21 + "RG", dna=2, rna=1, mm=5, n_guides=12, per_guide=10),
+    dict(seed=215, lens=[100000], pattern="N" * 21 + "RG", dna=2, rna=1, mm=[3, 5], n_guides=12, per_guide=10),
 ]
 
 
