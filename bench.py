@@ -811,7 +811,10 @@ def main():
             "roofline": {"bound": "int-pipe", "kernel": "comparer", "achieved": achieved, "peak": peak,
                          "unit": "G base-comparisons/s", "frac": achieved / peak if peak else None,
                          "traffic": traffic,
-                         "peak_basis": basis, "base_comparisons_per_test": mean_nonN, "issued": issued},
+                         "peak_basis": basis, "base_comparisons_per_test": mean_nonN, "issued": issued,
+                         "note": "the peak assumes every variant counted in full; the lane programs' update "
+                                 "steps cost less per base comparison, so frac can pass 1 -- `issued` is the "
+                                 "fraction of the LOP3 pipe the count phase itself occupies"},
             "roofline_finder": {"bound": "hbm", "achieved": finder_gbs, "peak": peaks.get("hbm_gbs"),
                                 "unit": "GB/s", "frac": finder_gbs / peaks["hbm_gbs"] if peaks.get("hbm_gbs")
                                 else None, "bytes_per_launch": finder_bytes / max(fnd["launches"], 1),
