@@ -483,20 +483,21 @@ __device__ __forceinline__ uint32_t decimal_len(uint64_t v) {
   return d;
 }
 
+// Writes the digits last to first at their final places (no digit buffer:
+// a per-thread array would live in local memory).
 __device__ __forceinline__ char* put_decimal(char* o, uint64_t v) {
-  char tmp[20];
-  int k = 0;
+  const uint32_t len = decimal_len(v);
+  char* e = o + len;
   while (v > 0xFFFFFFFFull) {
-    tmp[k++] = (char)('0' + v % 10);
+    *--e = (char)('0' + v % 10);
     v /= 10;
   }
   uint32_t x = (uint32_t)v;
   do {
-    tmp[k++] = (char)('0' + x % 10);
+    *--e = (char)('0' + x % 10);
     x /= 10;
   } while (x);
-  while (k) *o++ = tmp[--k];
-  return o;
+  return o + len;
 }
 
 struct HitView {
@@ -536,9 +537,12 @@ __global__ void row_len_kernel(GenomeView g, FormatTables ft, const uint64_t* __
 // Rows of one hit at `o` (the bytes row_len_kernel counted).
 __device__ __forceinline__ void write_row(const GenomeView& g, const FormatTables& ft, uint64_t key, char* o) {
   const HitView h = decode(key);
-  const VariantFmt vf = ft.var[h.gid];
-  const uint32_t L = vf.L;
-  const char* comp = ft.pool + vf.comp_off;
+  // Fields read in place: a local copy of the struct, indexed by strand,
+  // would live in local memory.
+  const VariantFmt* vf = ft.var + h.gid;
+  const uint32_t L = vf->L;
+  const char* comp = ft.pool + vf->comp_off;
+  const uint32_t s_begin = vf->shape_begin[h.strand], s_end = vf->shape_end[h.strand];
   // Oriented window with mismatches lower-cased (indicate_mismatches,
   // cas-offinder.cpp:299-317: byte += 32).
   // The window's plane bits, 64 positions from h.pos (three words per plane
@@ -550,28 +554,30 @@ __device__ __forceinline__ void write_row(const GenomeView& g, const FormatTable
     return b0 ? (lo64 >> b0) | ((uint64_t)plane[w0 + 2] << (64 - b0)) : lo64;
   };
   const uint64_t H = bits64(g.hi), Lo = bits64(g.lo), O = bits64(g.ot);
-  unsigned char win[kMaxL];
-  for (uint32_t k = 0; k < L; ++k) {
+  // Oriented position k of the window, as printed; computed where the DNA
+  // column asks for it (a per-thread window array would live in local
+  // memory).
+  auto win = [&](uint32_t k) {
     const uint32_t q = h.strand ? L - 1 - k : k;  // window position of oriented position k
     const unsigned hb = (unsigned)(H >> q) & 1u, lb = (unsigned)(Lo >> q) & 1u;
     unsigned char c;
-    if (!((O >> q) & 1u)) c = (unsigned char)"TCAG"[hb * 2 + lb];
-    else if (!hb) c = lb ? ';' : 'N';
-    else c = genome_byte(g, h.pos + q);  // another byte: from the exception list
-    if (h.strand) c = dev_complement(c);
+    // Bytes T, C, A, G (and their complements A, G, T, C) packed low to high.
+    if (!((O >> q) & 1u)) c = (unsigned char)((h.strand ? 0x43544741u : 0x47414354u) >> (8 * (hb * 2 + lb)));
+    else if (!hb) c = lb ? ';' : 'N';  // complement_byte leaves both as they are
+    else c = h.strand ? dev_complement(genome_byte(g, h.pos + q)) : genome_byte(g, h.pos + q);
     if (dev_mismatch((unsigned char)comp[k], c)) c = (unsigned char)(c + 32);
-    win[k] = c;
-  }
+    return c;
+  };
   const uint32_t rec = record_of(g, h.pos);
   const uint64_t rel = h.pos - g.rec_start[rec];
   const char* name = g.rec_names + g.rec_name_off[rec];
   const uint32_t name_len = g.rec_name_len[rec];
-  for (uint32_t s = vf.shape_begin[h.strand]; s < vf.shape_end[h.strand]; ++s) {
+  for (uint32_t s = s_begin; s < s_end; ++s) {
     const ShapeFmt sh = ft.shape[s];
     for (uint32_t k = 0; k < sh.head_len; ++k) *o++ = ft.pool[sh.head_off + k];
     for (uint32_t k = 0; k < sh.dna_len; ++k) {
       const unsigned char c = (unsigned char)ft.pool[sh.dna_off + k];
-      *o++ = (char)(c >= 0x80 ? win[c - 0x80] : c);
+      *o++ = (char)(c >= 0x80 ? win(c - 0x80u) : c);
     }
     *o++ = '\t';
     for (uint32_t k = 0; k < name_len; ++k) *o++ = name[k];
