@@ -192,21 +192,23 @@ def genome_text(path):
 
 def bs_programs(text):
     """The bit-sliced comparer's lane programs for one input file (test hook):
-    dict with chunks, m, slots, row, prog / pgid (uint32 arrays) and the
-    variants as (key, threshold) in id order."""
+    dict with chunks, m, slots, row, prog / pgid (uint32 arrays), the
+    variants as (key, threshold) in id order and `narrow` (the counts fit
+    bit_width(slots) planes)."""
     import numpy as np
     raw = text.encode() if isinstance(text, str) else bytes(text)
-    info = np.zeros(6, dtype=np.uint32)
+    info = np.zeros(7, dtype=np.uint32)
     st = lib().cofx_bs_programs(raw, len(raw), _ptr(info), None, 0, None, 0, None, 0)
     if st != 0:
         raise CofError(st, "input does not fit the bit-sliced comparer" if st == 2 else "parse error")
-    chunks, m, slots, row, nvar, kb = (int(x) for x in info)
+    chunks, m, slots, row, nvar, kb, narrow = (int(x) for x in info)
     prog = np.zeros(max(chunks, 1) * (1 + slots // 2 + 2 * (m // 2)) * 32, dtype=np.uint32)
     pgid = np.zeros(max(chunks, 1) * m * 32, dtype=np.uint32)
     keys = ctypes.create_string_buffer(kb + 1)
     lib().cofx_bs_programs(raw, len(raw), _ptr(info), _ptr(prog), prog.size, _ptr(pgid), pgid.size, keys, kb + 1)
     variants = [(ln.split("\t")[0], int(ln.split("\t")[1])) for ln in keys.raw[:kb].decode().splitlines()]
-    return {"chunks": chunks, "m": m, "slots": slots, "row": row, "prog": prog, "pgid": pgid, "variants": variants}
+    return {"chunks": chunks, "m": m, "slots": slots, "row": row, "prog": prog, "pgid": pgid, "variants": variants,
+            "narrow": bool(narrow)}
 
 
 def plane_words(n):

@@ -1498,12 +1498,15 @@ int cofx_bs_programs(const char* input, size_t len, uint32_t* info, uint32_t* pr
   std::vector<const Variant*> vars;
   std::vector<uint32_t> gids;
   int maxpos = 0;
+  std::vector<uint32_t> thr, npos;
   for (size_t v = 0; v < job.variants.size(); ++v) {
     vars.push_back(&job.variants[v]);
     gids.push_back((uint32_t)v);
     int c = 0;
     for (char ch : job.variants[v].key) c += bs_class_of((unsigned char)ch) != 0;
     maxpos = std::max(maxpos, c);
+    thr.push_back(job.variants[v].threshold);
+    npos.push_back((uint32_t)c);
   }
   const int S = bs_slots_for(maxpos);
   if (!S || vars.empty()) return 2;
@@ -1519,6 +1522,7 @@ int cofx_bs_programs(const char* input, size_t len, uint32_t* info, uint32_t* pr
   info[3] = row;
   info[4] = (uint32_t)vars.size();
   info[5] = (uint32_t)kt.size();
+  info[6] = bs_narrow_ok(S, thr.data(), npos.data(), thr.size()) ? 1u : 0u;
   if (prog && prog_cap >= pv.size()) std::memcpy(prog, pv.data(), pv.size() * 4);
   if (pgid && pgid_cap >= gv.size()) std::memcpy(pgid, gv.data(), gv.size() * 4);
   if (keys && keys_cap >= kt.size()) std::memcpy(keys, kt.data(), kt.size());

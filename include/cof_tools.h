@@ -38,8 +38,10 @@ int cofx_genome_text(const char* path, char* out, uint64_t cap, uint64_t* n);
 
 /* Test hook: parses one input file (the whole text) and builds the lane
  * programs of the bit-sliced comparer for its compare variants (layout in
- * cas-offinder_gb300/csrc/kernels.cuh, launch_comparer_bs).  info[0..5] =
- * {chunks, m, slots, class-row words, variants, bytes of keys}.  Each output
+ * cas-offinder_gb300/csrc/kernels.cuh, launch_comparer_bs).  info[0..6] =
+ * {chunks, m, slots, class-row words, variants, bytes of keys, narrow}, where
+ * narrow = 1 when the counts fit bit_width(slots) planes (bs_narrow_ok; the
+ * kernels then use them for programs of more than one variant).  Each output
  * is filled when its capacity suffices: prog chunks * (1 + slots/2 + 2 *
  * (m / 2)) * 32 words, pgid chunks * m * 32 words, keys one "key\tthreshold\n" line per
  * variant in id order.  Returns 0; 1 on a parse error; 2 when the variants do
