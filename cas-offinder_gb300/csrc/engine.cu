@@ -58,9 +58,53 @@ cof_status issue_upload(cof_handle* h, size_t upto) {
   return COF_OK;
 }
 
+// Words of chunk c + 1 that segment c's windows read (a window of up to 64
+// positions starting in the chunk's last word ends two words later).
+constexpr uint64_t kUploadHeadWords = 2;
+
+// Events upload_ev[0 .. n), created outside any stream capture.
+cof_status ensure_upload_events(cof_handle* h, size_t n) {
+  while (h->upload_ev.size() < n) {
+    cudaEvent_t e = nullptr;
+    COF_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    h->upload_ev.push_back(e);
+  }
+  return COF_OK;
+}
+
+// Page-locked planes: queues the whole upload on stream3 after the work
+// already on h->stream -- chunk 0, then for each c the first words of chunk
+// c + 1 and the rest of it -- with upload_ev[c] recorded once chunk c and the
+// first words of chunk c + 1 are copied.  The copies then run back to back at
+// the link's rate, ahead of the scans that wait for them.
+cof_status queue_upload_ahead(cof_handle* h) {
+  DevGenome& dg = h->genome;
+  const uint64_t W = h->upload_words;
+  const size_t chunks = h->upload_pending;
+  uint32_t* dst[3] = {dg.hi.as<uint32_t>(), dg.lo.as<uint32_t>(), dg.ot.as<uint32_t>()};
+  auto copy = [&](uint64_t w0, uint64_t w1) -> cof_status {
+    if (w0 >= w1) return COF_OK;
+    for (int p = 0; p < 3; ++p)
+      COF_CUDA(h, cudaMemcpyAsync(dst[p] + w0, h->upload_src[p] + w0, (w1 - w0) * 4, cudaMemcpyHostToDevice,
+                                  h->stream3));
+    return COF_OK;
+  };
+  COF_CUDA(h, cudaStreamWaitEvent(h->stream3, h->ev_start, 0));
+  cof_status st = copy(0, std::min<uint64_t>(W, kSegWords));
+  for (size_t c = 0; c < chunks && st == COF_OK; ++c) {
+    const uint64_t n0 = (c + 1) * kSegWords;                 // chunk c + 1
+    const uint64_t h1 = std::min<uint64_t>(W, n0 + kUploadHeadWords);
+    if ((st = copy(n0, h1))) break;
+    COF_CUDA(h, cudaEventRecord(h->upload_ev[c], h->stream3));
+    st = copy(h1, std::min<uint64_t>(W, n0 + kSegWords));
+  }
+  h->upload_issued = chunks;
+  return st;
+}
+
 // With `streamed` the plane copies are left to the search (run_passes queues
-// them on the finders' stream one segment ahead of the scan): the host
-// planes must stay valid until that search is done.
+// them: see queue_upload_ahead and issue_upload): the host planes must stay
+// valid until that search is done.
 cof_status upload_genome(cof_handle* h, DevGenome& dg, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot,
                          uint64_t n, const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
                          const std::vector<std::string>& names, const std::vector<uint64_t>& starts,
@@ -683,6 +727,15 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   COF_CUDA(h, cudaMemsetAsync(h->hit_count.p, 0, 8, h->stream));
   COF_CUDA(h, cudaEventRecord(h->ev_start, h->stream));
   COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_start, 0));
+  // A streamed upload from page-locked planes is queued whole on stream3;
+  // from pageable planes it follows the scans (issue_upload below).
+  const bool ahead = h->upload_pending && h->upload_pinned;
+  if (ahead) {
+    if (h->upload_ev.size() < h->upload_pending)
+      return fail(h, COF_ERR_STATE, "upload events not created before the passes");
+    cof_status st = queue_upload_ahead(h);
+    if (st) return st;
+  }
   uint64_t pass = 0;
   for (uint64_t s = 0; s < nseg; ++s) {
     for (size_t gi = 0; gi < G; ++gi) {
@@ -699,7 +752,10 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
       // for the previous pass's comparer, or its events would count the time
       // it spends queued behind that comparer's CTAs.
       if (h->profiling && pass >= 1) COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->ev_used[1 - b], 0));
-      if (h->upload_pending) {
+      if (ahead) {
+        // Segment s reads chunk s and the first words of chunk s + 1.
+        COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->upload_ev[std::min<size_t>(s, h->upload_pending - 1)], 0));
+      } else if (h->upload_pending) {
         // Segment s reads plane words up to w1 + 2 (chunks s and s + 1); its
         // finder follows the copies up to chunk s + 1 on the same stream, and
         // the copy of chunk s + 2 runs under the comparer of segment s.
@@ -729,7 +785,9 @@ cof_status run_passes(cof_handle* h, uint64_t hit_cap, std::vector<EventPair>& e
   }
   // Row formatting reads the planes: the rest of a streamed upload goes
   // before the join.
-  if (h->upload_pending) {
+  if (ahead) {
+    COF_CUDA(h, cudaStreamWaitEvent(h->stream2, h->upload_ev[h->upload_pending - 1], 0));
+  } else if (h->upload_pending) {
     cof_status st = issue_upload(h, h->upload_pending);
     if (st) return st;
   }
@@ -786,6 +844,10 @@ cof_status run_passes_graph(cof_handle* h, uint64_t cap, uint64_t* nseg) {
     h->pass_graph = nullptr;
     std::vector<EventPair> none;
     h->upload_issued = 0;  // a streamed upload is captured whole
+    if (h->upload_pending) {
+      cof_status se = ensure_upload_events(h, h->upload_pending);
+      if (se) return se;
+    }
     COF_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     const cof_status st = run_passes(h, cap, none, nseg);
     cudaGraph_t graph = nullptr;
@@ -874,6 +936,7 @@ cof_status do_search(cof_handle* h, const char** rows, size_t* rows_len, StreamS
   // Profiled searches time each launch with events, and copies from pageable
   // host memory cannot be graph nodes: both run the passes directly.
   const bool graph = h->use_graphs && !h->profiling && (!h->upload_pending || h->upload_pinned);
+  if (h->upload_pending && (st = ensure_upload_events(h, h->upload_pending))) return st;
   for (;;) {
     st = graph ? run_passes_graph(h, cap, &nseg) : run_passes(h, cap, evs, &nseg);
     if (st) return st;
@@ -1125,6 +1188,7 @@ cof_status cof_open(int device, cof_handle** out) {
   cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device);
   e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream3, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming);
   for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
     e = cudaEventCreateWithFlags(&h->ev_found[i], cudaEventDisableTiming);
@@ -1144,7 +1208,9 @@ void cof_close(cof_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->stream2) cudaStreamSynchronize(h->stream2);
-  cudaStream_t s = h->stream, s2 = h->stream2;
+  if (h->stream3) cudaStreamSynchronize(h->stream3);
+  cudaStream_t s = h->stream, s2 = h->stream2, s3 = h->stream3;
+  for (cudaEvent_t e : h->upload_ev) cudaEventDestroy(e);
   cudaEvent_t evs[7] = {h->timer_a, h->timer_b, h->ev_start, h->ev_found[0], h->ev_found[1], h->ev_used[0],
                         h->ev_used[1]};
   for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
@@ -1157,6 +1223,7 @@ void cof_close(cof_handle* h) {
     if (ev) cudaEventDestroy(ev);
   if (s) cudaStreamDestroy(s);
   if (s2) cudaStreamDestroy(s2);
+  if (s3) cudaStreamDestroy(s3);
 }
 
 const char* cof_last_error(const cof_handle* h) { return h ? h->err.c_str() : "null handle"; }
@@ -1333,7 +1400,9 @@ cof_status cof_search_planes(cof_handle* h, const uint32_t* hi, const uint32_t* 
   // the host planes are not read after this call returns.
   if (h->upload_pending) {
     const cof_status ri = issue_upload(h, h->upload_pending);
-    const cudaError_t e = cudaStreamSynchronize(h->stream2);
+    cudaError_t e = cudaStreamSynchronize(h->stream3);
+    const cudaError_t e2 = cudaStreamSynchronize(h->stream2);
+    if (e == cudaSuccess) e = e2;
     h->upload_pending = h->upload_issued = 0;
     if (ri && r == COF_OK) return ri;
     if (e != cudaSuccess && r == COF_OK) return fail(h, COF_ERR_CUDA, cudaGetErrorString(e));

@@ -138,8 +138,13 @@ struct cof_handle {
   cudaStream_t stream = nullptr;   // comparer, formatting, copies
   cudaStream_t stream2 = nullptr;  // finder passes, one segment ahead of the comparer
   cudaEvent_t ev_start = nullptr, ev_found[2] = {nullptr, nullptr}, ev_used[2] = {nullptr, nullptr};
-  // Streamed upload (cof_search_planes): plane copies per segment, queued on
-  // stream2 ahead of the finders that read them.
+  // Streamed upload (cof_search_planes): plane copies per segment.  From
+  // page-locked planes every copy is queued at once on stream3, which runs
+  // ahead at the link's rate; upload_ev[c] marks chunk c and the first words
+  // of chunk c + 1 (what segment c's windows read) as copied.  From pageable
+  // planes the copies go on stream2, one segment ahead of the finders.
+  cudaStream_t stream3 = nullptr;
+  std::vector<cudaEvent_t> upload_ev;
   size_t upload_pending = 0;  // chunks of the current streamed upload (0: none)
   size_t upload_issued = 0;   // chunks whose copies are queued so far
   bool upload_pinned = false;  // the host planes are page-locked (copies can be graph nodes)
