@@ -12,8 +12,8 @@ formatting on the GPU, rows copied to host memory).
   value : steps with the packed genome already resident in HBM.
   e2e   : steps through the C ABI from host buffers: each step uploads the
           genome planes from pinned host memory and searches them in one call
-          (cof_search_planes: the upload of segment s+1 overlaps the scan of
-          segment s), and copies the rows back.
+          (cof_search_planes: the upload runs ahead on a copy stream while
+          the segments already copied are scanned), and copies the rows back.
 The genome planes (1.16 GB) are larger than L2, so no flush is needed between
 steps.  Timing: CUDA events on the engine's stream (cof_timer_start/stop),
 after warm-up steps, max over ranks.  Under torchrun each rank runs an

@@ -119,12 +119,13 @@ cof_status cof_search_stream(cof_handle* h, cof_write_fn write, void* ctx, uint6
 /* Load + search in one call, for a genome that lives in host memory (the
  * reference's per-file loop: setChrData, then loadNextChunk / findPattern /
  * compareAll per chunk, cas-offinder.cpp:175-297, 330-469).  Arguments as
- * cof_genome_load_planes, results as cof_search.  The planes are copied one
- * segment at a time on a copy stream while earlier segments are already
- * being scanned, so the copy hides under the search.  The host planes are
- * read only during the call (pinned memory gives the overlap; pageable memory
- * works, copied synchronously); afterwards the genome stays resident as
- * after cof_genome_load_planes. */
+ * cof_genome_load_planes, results as cof_search.  From page-locked planes
+ * every segment's copy is queued at once on a copy stream and each segment's
+ * scan starts as soon as its planes (and the next segment's first words) have
+ * arrived, so the copy hides under the search; pageable planes are copied a
+ * segment ahead of the scans, each copy synchronous.  The host planes are read
+ * only during the call; afterwards the genome stays resident as after
+ * cof_genome_load_planes. */
 cof_status cof_search_planes(cof_handle* h, const uint32_t* hi, const uint32_t* lo, const uint32_t* ot, uint64_t n,
                              const uint64_t* exc_pos, const uint8_t* exc_byte, uint64_t n_exc,
                              const char* const* names, const uint64_t* starts, uint32_t n_records,
