@@ -5,6 +5,7 @@ make_golden.py); the oracle must reproduce each byte for byte when run with
 one thread.  When the reference checkout is present, seeded random cases are
 also run through both programs here."""
 import os
+import random
 import subprocess
 
 import pytest
@@ -46,6 +47,13 @@ RANDOM_CASES = [
     dict(seed=104, lens=[20000], pattern="N" * 19 + "NNGRRT", dna=1, rna=0, mm=[2, 6], iupac_frac=0.15,
          sprinkle_chars="RYSWnX"),
     dict(seed=105, lens=[8000, 8000], pattern="N" * 30 + "NGG", dna=1, rna=1, mm=6),
+    # The GPU parity cases at the edges of the bit-sliced comparer's narrow
+    # counters (tests/test_gpu_parity.py seeds 212 and 213, the same inputs):
+    # 20-nt guides at thresholds 4 / 15 and 3 / 16, tens of thousands of rows.
+    dict(seed=212, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[4, 15], per_guide=20,
+         guides=["".join(random.Random(212 + i).choice("ACGT") for _ in range(20)) + "NNN" for i in range(2)]),
+    dict(seed=213, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[3, 16], per_guide=20,
+         guides=["".join(random.Random(213 + i).choice("ACGT") for _ in range(20)) + "NNN" for i in range(2)]),
 ]
 
 
