@@ -54,6 +54,9 @@ RANDOM_CASES = [
          guides=["".join(random.Random(212 + i).choice("ACGT") for _ in range(20)) + "NNN" for i in range(2)]),
     dict(seed=213, lens=[20000], pattern="N" * 21 + "RG", dna=1, rna=1, mm=[3, 16], per_guide=20,
          guides=["".join(random.Random(213 + i).choice("ACGT") for _ in range(20)) + "NNN" for i in range(2)]),
+    # and its multi-chunk groups (seeds 214, 215): ~700 variants.
+    dict(seed=214, lens=[100000], pattern="N" * 21 + "RG", dna=2, rna=1, mm=5, n_guides=12, per_guide=10),
+    dict(seed=215, lens=[100000], pattern="N" * 21 + "RG", dna=2, rna=1, mm=[3, 5], n_guides=12, per_guide=10),
 ]
 
 
